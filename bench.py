@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Benchmark of the full-physics fire simulation step on GB300.
+
+Workload: the 128x256x128 full-physics step (5 mm cells, 0.64 x 1.28 x 0.64 m, dt = 1/240 s, FP32) with
+6 seeded pyrolysis spots of 1-4 g/s, vorticity confinement 0.3, curl-noise amplitude 0.2, soot forming
+after a gas age of 20-60 ms, and the pressure solved each step to a 1e-5 relative residual (at most 8
+V(2,2) cycles).  Synthetic: the state evolves from rest under the seeded emitter; no dataset is involved.
+
+A step is one FireSim.step (src/sim.js:627-648): advection, forces, divergence, multigrid, projection.
+  value      steps/s over the timed region (device time, CUDA events on the launching stream; inputs resident)
+  e2e        steps/s through the C ABI with a host parameter update, the parameter-block upload and a
+             device->host read of the step's diagnostics (S stats + heat release) every step (host clock)
+  roofline   the dominant stage's algorithmic bytes / its average duration, against measured HBM peak
+  cpu_baseline  the CPU oracle (FP32, OpenMP on all host cores) on a bounded sample of the same workload
+
+`--impl reference` times the CPU implementation of the step (the oracle port of the reference's WGSL; the
+reference's own WebGPU step cannot run on this machine) on the same workload and prints the same line.
+Multi-GPU (`torchrun --nproc-per-node N`): replicas only, one independent simulation per GPU; value is the
+aggregate steps/s of all ranks over the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "procedural-fire_gb300"
+for p in (PKG, ROOT / "oracle"):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+WORKLOAD = dict(
+    name="fire-step-128x256x128-fp32", res=(128, 256, 128), size=(0.64, 1.28, 0.64), dt=1.0 / 240.0,
+    spots=6, spot_seed=2, flux=(1.0, 4.0), sigma=0.02, radius=0.2, vortEps=0.3, turbAmp=0.2,
+    soot_age=(0.02, 0.06), mg_tol=1e-5, mg_max_cycles=8, preroll=60,
+)
+METRIC = "steps/s, full-physics fire step at 128x256x128 (FP32)"
+
+# Algorithmic bytes per cell of each stage: every array the stage must read once and write once (float4
+# fields of 16 B, pressure/divergence of 4 B).  forces adds the 16 MiB curl table once per step.
+B_ALG = {"adv1": 96.0, "adv2": 144.0, "forces": 112.0, "div": 20.0, "project": 40.0}
+B_MG_CYCLE = 75.0      # V(2,2): level 0 (4 sweeps x 12 + restrict 9 + prolong 8.5) x 8/7 over the levels
+FALLBACK_HBM_GBS = 6800.0
+
+
+# ------------------------------------------------------------------------------------------ distributed
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def dist_init(backend: str):
+    import torch.distributed as dist
+    rank, world, _ = dist_env()
+    if world > 1 and not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", "29511")
+        dist.init_process_group(backend, rank=rank, world_size=world)
+    return rank, world
+
+
+def barrier():
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def max_over_ranks(x: float, device=None) -> float:
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, max_mhz_default=2070.0):
+        rows = []
+        try:
+            for line in self.path.read_text().splitlines():
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": max_mhz_default, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        mx = float(rows[0][2])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        loaded = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------------------------------ helpers
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel_stage: str):
+    """Per-launch DRAM bytes of a stage's kernel at the bench workload, from the committed ncu summary."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    try:
+        d = json.loads(p.read_text())
+        v = d.get(WORKLOAD["name"], {}).get(kernel_stage)
+        return None if v is None else float(v)
+    except Exception:
+        return None
+
+
+def make_sim(F, device: int):
+    W = WORKLOAD
+    sim = F.FireSim(res=W["res"], size=W["size"], logs=None, vcycles=4, device=device,
+                    mg_max_cycles=W["mg_max_cycles"], mg_tol=W["mg_tol"])
+    sim.set_params({"vortEps": W["vortEps"], "turbAmp": W["turbAmp"]})
+    sim.set_soot_age(*W["soot_age"])
+    sim.set_bed_gain(0.0)
+    sim.set_spots(F.make_spots(W["spot_seed"], W["spots"], W["flux"][0], W["flux"][1], W["sigma"], W["radius"]))
+    return sim
+
+
+def launches_per_step(sim, cycles_per_step: float) -> float:
+    """Kernels launched per step by the captured graph: 5 stencil kernels, the counter reset, and per
+    V-cycle 10 per level above the shared-memory tail, the tail kernel, 2 residual kernels and the decision."""
+    n = len(sim.levels)
+    cells = [l["dims"][0] * l["dims"][1] * l["dims"][2] for l in sim.levels]
+    T = n
+    for l in range(n - 1, -1, -1):
+        if 8 * sum(cells[l:]) <= 200 * 1024:
+            T = l
+        else:
+            break
+    per_cycle = 10 * min(T, n - 1) + (1 if T < n else 2 * sim.coarse_iters) + 3
+    return 6 + per_cycle * cycles_per_step
+
+
+def cpu_baseline(O, sim_tables, cycles: int, steps: int = 2):
+    """The oracle (FP32, OpenMP on all cores) on `steps` steps of the same workload from rest."""
+    import fire_sim as F
+    W = WORKLOAD
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    dx = np.float32(np.float64(np.float32(W["size"][0])) / W["res"][0])
+    orc = O.OracleSim(W["res"], float(dx))
+    noise, curl = sim_tables
+    orc.set_tables(noise, curl)
+    orc.set_logs(np.zeros(0, np.float32))
+    blk = _block(F)
+    orc.set_params(blk[:64])
+    orc.set_ext(blk[64:])
+    t0 = time.perf_counter()
+    for s in range(steps):
+        orc.step_raw(s == 0, cycles)
+    dt = time.perf_counter() - t0
+    return steps / dt, threads, f"{steps} steps of {W['res'][0]}x{W['res'][1]}x{W['res'][2]} from rest, {cycles} V-cycles each"
+
+
+def _block(F):
+    """The 200-float block for the workload (as the GPU builds it for the first step)."""
+    W = WORKLOAD
+    blk = np.zeros(200, np.float32)
+    blk[:64] = F.param_defaults()
+    for i, v in enumerate(W["res"]):
+        blk[i] = v
+    size0 = np.float32(W["size"][0])
+    blk[3] = np.float32(np.float64(size0) / W["res"][0])
+    blk[4] = np.float32(W["dt"])
+    blk[8] = np.float32(-size0 / np.float32(2))
+    blk[10] = np.float32(-np.float32(W["size"][2]) / np.float32(2))
+    blk[F.SIM_FIELDS.index("vortEps")] = W["vortEps"]
+    blk[F.SIM_FIELDS.index("turbAmp")] = W["turbAmp"]
+    e = blk[64:]
+    e[0], e[1], e[2], e[4] = W["soot_age"][0], W["soot_age"][1], 0.0, 4.0
+    spots = F.make_spots(W["spot_seed"], W["spots"], W["flux"][0], W["flux"][1], W["sigma"], W["radius"])
+    e[3] = len(spots)
+    for i, s in enumerate(spots):
+        e[8 + 8 * i: 8 + 8 * i + 5] = s
+    return blk
+
+
+# ------------------------------------------------------------------------------------------ arms
+def run_ours(args):
+    import torch
+    import fire_sim as F
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist_init("nccl")
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    W = WORKLOAD
+    cells = W["res"][0] * W["res"][1] * W["res"][2]
+    sim = make_sim(F, dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    dt = W["dt"]
+
+    sim.step(dt, W["preroll"] + args.warmup, stream=sh)
+    torch.cuda.synchronize(dev)
+    info0 = sim.info()
+
+    # ---- timed region: K steps, inputs resident in HBM (the fields exceed L2 several times over)
+    sampler = ClockSampler(dev) if rank == 0 else None
+    if sampler:
+        sampler.__enter__()
+    barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.step(dt, args.steps, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    if sampler:
+        sampler.__exit__()
+    ms = e0.elapsed_time(e1)
+    ms_max = max_over_ranks(ms, device=torch.device("cuda", dev))
+    info1 = sim.info()
+    cycles = (info1.total_cycles - info0.total_cycles) / max(args.steps, 1)
+    value = world * args.steps / (ms_max / 1e3)
+
+    # ---- per-stage profile (graph with event nodes between stages), averaged over steps
+    nprof = max(3, min(args.steps, 40))
+    sim.profile(True)
+    acc = {}
+    for _ in range(nprof):
+        sim.step(dt, 1, stream=sh)
+        for k, v in sim.stage_times().items():
+            acc[k] = acc.get(k, 0.0) + v / nprof
+    sim.profile(False)
+
+    # ---- end to end through the C ABI: host param update + block upload + stats readback per step
+    pinned = torch.empty(17, dtype=torch.float64, pin_memory=True)
+    torch.cuda.synchronize(dev)
+    barrier()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        sim.set_params({"windX": 0.05 * np.sin(0.01 * s)})
+        sim.step(dt, 1, stream=sh)
+        sim.stats_async(pinned.data_ptr(), stream=sh)
+    torch.cuda.synchronize(dev)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, device=torch.device("cuda", dev))
+    barrier()
+    e2e = world * args.steps / e2e_s
+    diag = pinned.numpy().copy()
+
+    if rank != 0:
+        return None
+
+    # ---- roofline of the dominant single-kernel stage
+    peak, peak_kind = measured_peak()
+    stage_bytes = {k: B_ALG[k] * cells for k in B_ALG}
+    stage_bytes["forces"] += 128 ** 3 * 8
+    single = {k: acc[k] for k in B_ALG}
+    dom = max(single, key=single.get)
+    achieved = stage_bytes[dom] / (single[dom] * 1e-3) / 1e9
+    mg_ms = acc["vcycle"]
+    mg_gbs = B_MG_CYCLE * cycles * cells / (mg_ms * 1e-3) / 1e9 if mg_ms > 0 else None
+    step_bytes = sum(stage_bytes.values()) + B_MG_CYCLE * cycles * cells
+    traffic = ncu_traffic(dom)
+
+    # ---- CPU baseline: oracle on a bounded sample
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        import oracle as O
+        tabs = (sim.download("noise").astype(np.float32), sim.download("curl").astype(np.float32))
+        v, cores, sample = cpu_baseline(O, tabs, max(1, int(round(cycles))), steps=2)
+        cpu = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
+
+    clocks = sampler.summary() if sampler else None
+    out = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": W["name"], "grid": list(W["res"]), "cell_m": 0.005, "dt": W["dt"],
+                   "spots": W["spots"], "mg": f"V(2,2) to {W['mg_tol']} rel. residual, max {W['mg_max_cycles']}",
+                   "mean_vcycles_per_step": cycles, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (fields ~740 MB vs 129 MB L2)"},
+        "gcell_updates_per_s": value * cells / 1e9,
+        "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 200 * 4, "d2h_bytes_per_step": 17 * 8},
+        "gpu_launches": int(round(args.steps * launches_per_step(sim, cycles))),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "bytes_per_cell": B_ALG[dom] + (128 ** 3 * 8 / cells if dom == "forces" else 0.0)},
+        "stage_ms": {k: round(v, 5) for k, v in acc.items()},
+        "step_roofline": {"alg_bytes_per_step": step_bytes, "achieved_gbs": step_bytes / (ms_max / args.steps * 1e-3) / 1e9,
+                          "frac": step_bytes / (ms_max / args.steps * 1e-3) / 1e9 / peak, "mg_gbs": mg_gbs},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "diag_last_step": {"hrr_kw": float(diag[16]), "T_max": 293.0 + 1000.0 * float(diag[1])},
+    }
+    return out
+
+
+def run_reference(args):
+    """CPU implementation of the step (oracle port, all host threads) on the same workload."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return None
+    import fire_sim as F
+    import oracle as O
+    O.build()
+    W = WORKLOAD
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    noise = O.noise_table(128, 1)
+    curl = O.curl_table(noise)
+    dx = np.float32(np.float64(np.float32(W["size"][0])) / W["res"][0])
+    orc = O.OracleSim(W["res"], float(dx))
+    orc.set_tables(noise, curl)
+    orc.set_logs(np.zeros(0, np.float32))
+    blk = _block(F)
+    orc.set_params(blk[:64])
+    orc.set_ext(blk[64:])
+    t_step = None
+    for s in range(max(args.warmup, 1)):
+        t0 = time.perf_counter()
+        orc.step_raw(s == 0, -W["mg_max_cycles"], W["mg_tol"])
+        t_step = time.perf_counter() - t0
+    budget = 150.0
+    k = max(2, min(args.steps, int(budget / max(t_step, 1e-3))))
+    t0 = time.perf_counter()
+    for s in range(k):
+        orc.step_raw(False, -W["mg_max_cycles"], W["mg_tol"])
+    el = time.perf_counter() - t0
+    v = k / el
+    return {
+        "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world, "steps": k, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": W["name"], "grid": list(W["res"]), "cell_m": 0.005, "dt": W["dt"],
+                   "spots": W["spots"], "mg": f"V(2,2) to {W['mg_tol']} rel. residual, max {W['mg_max_cycles']}"},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{k} timed steps after {max(args.warmup, 1)} warm-up steps from rest "
+                                   f"(the reference's WebGPU step needs a browser GPU stack, unavailable on this box)"},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,236 @@
+/*
+ * fire_sim.h - C ABI of the GB300-native procedural-fire simulation step.
+ *
+ * This is the drop-in boundary for the reference's `FireSim` class (src/sim.js) and the parts of the
+ * deterministic page API that drive it (src/main.js `window.FIRE`).  Every entry point uses plain C types:
+ * pointers, sizes and status codes; CUDA streams are passed as `void*` (a cudaStream_t, or NULL for the
+ * legacy default stream).  Each declaration names the reference interface it replaces (file:line,
+ * relative to the reference project).
+ *
+ * Threading: a FireSim handle is not thread-safe; drive each handle from one host thread.  Several
+ * handles may run concurrently on different streams.
+ *
+ * Errors: every function returns FIRE_OK (0) or a FIRE_ERR_* code; fire_sim_last_error() gives a
+ * message for the most recent failure on a handle (the reference only logs WebGPU validation errors,
+ * src/gpu.js:25-26, 102-104).
+ */
+#ifndef FIRE_SIM_H
+#define FIRE_SIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------------- */
+#define FIRE_OK 0
+#define FIRE_ERR_BAD_ARG 1     /* null pointer, bad dims, wrong buffer size, unknown field id       */
+#define FIRE_ERR_BAD_PARAM 2   /* unknown parameter name (src/gpu.js:65 throws `unknown uniform`)    */
+#define FIRE_ERR_CUDA 3        /* a CUDA runtime call failed (message in fire_sim_last_error)        */
+#define FIRE_ERR_NO_DEVICE 4   /* no CUDA device, or the device is not an sm_103 part               */
+#define FIRE_ERR_OOM 5         /* device or pinned-host allocation failed                            */
+#define FIRE_ERR_STATE 6       /* call not valid in the current state (e.g. stage before geometry)  */
+
+/* ---- parameter block ---------------------------------------------------------------------------
+ * The 60 scalar parameters in SIM_FIELDS order (src/sim.js:14-23), padded to 64 floats exactly like
+ * the reference's uniform buffer (UniformStruct, src/gpu.js:48-61).  Defaults: SIM_DEFAULTS
+ * (src/sim.js:25-44).  The first 12 entries (nx..nLogs) are owned by the simulation and rewritten
+ * every step, as uploadUniforms does (src/sim.js:620-624).                                         */
+#define FIRE_PARAM_COUNT 60
+#define FIRE_PARAM_STRIDE 64
+
+/* Build-defined extension block: the soot age gate, a coal-bed gain and Gaussian pyrolysis spots.
+ * These have no counterpart in the reference uniform; with their defaults (0.015, 0.05, 1, no spots)
+ * the step is the reference step.                                                                   */
+#define FIRE_MAX_SPOTS 16
+#define FIRE_MAX_LOGS 16
+
+/* ---- fields --------------------------------------------------------------------------------------
+ * The reference's 3D textures (src/sim.js:71-76) and multigrid level 0 (src/sim.js:79-87).  Layout in
+ * device memory: dense, x fastest, then y, then z; 4 channels per cell for the rgba fields (float32
+ * each), 1 channel for P/B; noise/curl tables are 128^3 texels of 4 IEEE halves (rgba16float).       */
+enum FireField {
+  FIRE_FIELD_VEL = 0,   /* xyz velocity (m/s), w = 0 after projection          sim.vel  */
+  FIRE_FIELD_VELX = 1,  /* forward-advected hats, then pre-projection velocity sim.velX */
+  FIRE_FIELD_VELY = 2,  /* MacCormack-corrected velocity                       sim.velY */
+  FIRE_FIELD_S = 3,     /* theta, fuel, soot, heat release                     sim.S    */
+  FIRE_FIELD_SX = 4,
+  FIRE_FIELD_SY = 5,
+  FIRE_FIELD_S2 = 6,    /* products, gas age, smoke, CO fraction               sim.S2   */
+  FIRE_FIELD_S2X = 7,
+  FIRE_FIELD_S2Y = 8,
+  FIRE_FIELD_VORT = 9,  /* curl of velY; written only by the stand-alone curl stage (the step fuses it) */
+  FIRE_FIELD_GEO = 10,  /* band, bed, solid, sdf                               sim.geo  */
+  FIRE_FIELD_P = 11,    /* pressure, multigrid level 0                         levels[0].p */
+  FIRE_FIELD_B = 12,    /* divergence right-hand side, level 0                 levels[0].b */
+  FIRE_FIELD_NOISE = 13,/* 128^3 rgba16f noise table (src/noise.js:6-64)                  */
+  FIRE_FIELD_CURL = 14, /* 128^3 rgba16f curl table  (src/noise.js:67-90)                 */
+  FIRE_FIELD_COUNT = 15
+};
+
+/* Pipeline stages (the dispatches of FireSim.step, src/sim.js:632-644), for stage-level runs and
+ * per-stage timing.  FIRE_STAGE_FORCES is the fused curl + forces kernel.                            */
+enum FireStage {
+  FIRE_STAGE_GEO = 0, FIRE_STAGE_ADV1 = 1, FIRE_STAGE_ADV2 = 2, FIRE_STAGE_CURL = 3,
+  FIRE_STAGE_FORCES = 4, FIRE_STAGE_DIV = 5, FIRE_STAGE_VCYCLE = 6, FIRE_STAGE_PROJECT = 7,
+  FIRE_STAGE_COUNT = 8
+};
+
+typedef struct FireSim FireSim;
+
+/* Construction options: the FireSim constructor's {res, size, vcycles} (src/sim.js:49) plus the noise
+ * table seed the page passes to makeNoiseTexture (src/main.js:36).                                  */
+typedef struct FireConfig {
+  int res[3];          /* cells in x, y, z                                                        */
+  float size[3];       /* domain size in metres; dx = size[0] / res[0] (src/sim.js:53)            */
+  int vcycles;         /* multigrid V(2,2) cycles per step (src/sim.js:55, 642)                    */
+  int device;          /* CUDA device ordinal                                                     */
+  int noise_seed;      /* seed of the baked noise table (reference page: 1)                        */
+  int mg_max_cycles;   /* > 0: residual-driven solve, at most this many cycles (0 = fixed vcycles) */
+  double mg_tol;       /* relative residual ||b - A p|| / ||b|| target of the residual-driven mode   */
+} FireConfig;
+
+typedef struct FireFieldDesc {
+  void* data;          /* device pointer, owned by the simulation, valid until destroy              */
+  int dims[3];         /* texels in x, y, z                                                        */
+  int channels;        /* 4 (rgba) or 1                                                            */
+  int elem_bytes;      /* bytes per channel: 4 (float32) or 2 (float16)                             */
+  size_t strides[3];   /* byte strides of x, y, z                                                  */
+  size_t bytes;        /* total size                                                                */
+} FireFieldDesc;
+
+typedef struct FireInfo {
+  int res[3];
+  float size[3];
+  float dx;
+  float origin[3];     /* (-sx/2, 0, -sz/2) (src/sim.js:54)                                        */
+  double time;         /* sim.time (src/sim.js:57, 646)                                            */
+  long long frame;     /* sim.frame                                                                 */
+  int n_levels;        /* multigrid levels (src/sim.js:79-87)                                       */
+  int coarse_iters;    /* red-black sweeps on the coarsest level (src/sim.js:88-92)                 */
+  int vcycles;
+  int last_cycles;     /* V-cycles run by the most recent step (residual-driven mode)               */
+  double last_rel_residual; /* relative residual after the most recent step (if measured)          */
+  long long total_cycles;   /* V-cycles run since creation (residual-driven mode; else steps x vcycles) */
+} FireInfo;
+
+/* ---- lifetime ------------------------------------------------------------------------------------ */
+/* new FireSim(device, {res, size, logs, vcycles, noiseTex, curlTex}) (src/sim.js:49-101).  Bakes the noise
+ * and curl tables on the device (makeNoiseTexture/makeCurlTexture, src/noise.js:6-90).  `logs` holds
+ * n_logs capsules of 8 floats (a.xyz, r, b.xyz, burn) as packLogs writes them (src/scene.js:92-98);
+ * the reference passes all 16 packed slots, so n_logs = 16 with zero padding reproduces it.       */
+int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSim** out);
+int fire_sim_destroy(FireSim* sim);
+
+/* FireSim.step(enc, dt) x n_steps (src/sim.js:627-648): each step uploads the parameter block, rebuilds
+ * the emitter geometry if it is stale (src/sim.js:632), then runs advection, forces, divergence, the
+ * multigrid solve and projection as one CUDA graph on `stream`.  Asynchronous.                      */
+int fire_sim_step(FireSim* sim, float dt, int n_steps, void* stream);
+/* Waits for all work the handle queued (FIRE.step's onSubmittedWorkDone, src/main.js:244).         */
+int fire_sim_sync(FireSim* sim);
+
+/* ---- parameters (FireSim.setParams, src/sim.js:601-604) ----------------------------------------- */
+/* Merges name/value pairs.  An unknown name fails with FIRE_ERR_BAD_PARAM and changes nothing.
+ * Setting hotR0, hotR1, hotY1 or bedRadius marks the geometry stale, as the reference does.         */
+int fire_sim_set_params(FireSim* sim, const char* const* names, const float* values, int n);
+int fire_sim_get_param(FireSim* sim, const char* name, float* value);
+/* Whole block in SIM_FIELDS order (64 floats); entries 0..11 are ignored on set.                   */
+int fire_sim_set_param_block(FireSim* sim, const float* block64);
+int fire_sim_get_param_block(FireSim* sim, float* block64);
+/* The block the next step would upload for time step dt (uniforms + extension, FIRE_BLOCK_FLOATS
+ * floats): what uploadUniforms writes (src/sim.js:620-624), before this step's event envelopes.     */
+#define FIRE_BLOCK_FLOATS 200
+int fire_sim_peek_block(FireSim* sim, float dt, float* out);
+/* SIM_FIELDS index of a name, or -1; and the name of an index (src/sim.js:14-23).                   */
+int fire_param_index(const char* name);
+const char* fire_param_name(int index);
+/* SIM_DEFAULTS in SIM_FIELDS order (src/sim.js:25-44); simulation-owned entries are 0.              */
+int fire_param_defaults(float* block64);
+
+/* Extensions with no counterpart in the reference (defaults reproduce the reference step):
+ * soot formation age gate smoothstep(age0, age1, age) (reference constants 0.015, 0.05 at
+ * src/sim.js:314) and a gain on the coal bed of the emitter geometry (1 = reference, 0 = no bed).   */
+int fire_sim_set_soot_age(FireSim* sim, float age0, float age1);
+int fire_sim_set_bed_gain(FireSim* sim, float gain);
+/* Gaussian pyrolysis spots: n records of (x, y, z, sigma_m, flux_g_per_s).  A spot adds a pyrolysis
+ * source of peak weight flux / ref_flux (ref_flux = 4 g/s) with a Gaussian profile of width sigma;
+ * it feeds the same source path as the log pyrolysis band (src/sim.js:246-284).                    */
+int fire_sim_set_spots(FireSim* sim, const float* spots, int n);
+
+/* ---- events (src/main.js:401-407, 456-461; src/timeline.js:126-157) ---------------------------- */
+/* inject: a burst puff (burstX/Y/Z, burstAmt; forces at src/sim.js:288-296) of `amount` lasting
+ * `duration` seconds of simulated time (the page holds burstAmt = 1 for 250 ms, src/main.js:404, 461). */
+int fire_sim_inject(FireSim* sim, float x, float y, float z, float amount, float duration);
+/* stoke: moves log `log_index` as applyLogs does (src/main.js:135-150) with the timeline's offsets
+ * scaled by s in [0, 1] (src/timeline.js:126-133: foot 2 cm out, top 1.2 cm out and 4 cm down), marks
+ * the geometry stale, and injects a 0.25 s burst at the log's foot.                                   */
+int fire_sim_stoke(FireSim* sim, int log_index, float s);
+/* gust: the page's wind envelope windX = -1.4 g, windZ = 0.5 g with g = sin(pi (1 - t_left / dur))
+ * (src/main.js:405, 459-461), advanced per step in simulated time and scaled by `strength`.          */
+int fire_sim_gust(FireSim* sim, float strength, float duration);
+
+/* ---- state ------------------------------------------------------------------------------------- */
+/* FireSim.reset (src/sim.js:606-618): zero every velocity/scalar/vorticity field and every pressure
+ * level; time = frame = 0.                                                                         */
+int fire_sim_reset(FireSim* sim);
+/* Rewrite the log buffer and mark the geometry stale (src/main.js:147-149).                          */
+int fire_sim_upload_logs(FireSim* sim, const float* logs, int n_logs);
+
+/* Zero-copy view of a field's device buffer (the reference binds sim.vel/S/S2 into the renderer and
+ * sparks, src/renderer.js:603-610, src/sparks.js:245).                                               */
+int fire_sim_field(FireSim* sim, int which, FireFieldDesc* out);
+/* Synchronous copies between a field and host memory (`bytes` must equal FireFieldDesc.bytes).
+ * Readback as FIRE.stats does it (src/main.js:268-294); upload sets state for tests and restarts.  */
+int fire_sim_download(FireSim* sim, int which, void* host, size_t bytes);
+int fire_sim_upload(FireSim* sim, int which, const void* host, size_t bytes);
+int fire_sim_info(FireSim* sim, FireInfo* out);
+const char* fire_sim_last_error(FireSim* sim);
+
+/* ---- stage-level access and profiling (src/sim.js:629-644 profileStages; src/gpu.js:128-171) -- */
+/* Runs one stage with the current parameter block and dt (no time advance).  FIRE_STAGE_VCYCLE runs
+ * one V(2,2) cycle.  Synchronous with respect to `stream`'s previous work only.                     */
+int fire_sim_run_stage(FireSim* sim, int stage, float dt, void* stream);
+/* Multigrid pieces on level `level` (1 = smooth colour `arg`, 2 = restrict level -> level+1,
+ * 3 = prolong level+1 -> level), for kernel-level parity tests.                                    */
+int fire_sim_run_mg(FireSim* sim, int op, int level, int arg, void* stream);
+/* Level arrays (which: 0 = p, 1 = b) of any multigrid level, as float32 host arrays.               */
+int fire_sim_level_io(FireSim* sim, int level, int which, void* host, size_t bytes, int to_device);
+int fire_sim_level_dims(FireSim* sim, int level, int dims3[3], float* h);
+/* Per-stage GPU milliseconds of the most recent profiled step: enable, then read FIRE_STAGE_COUNT
+ * floats (waits for that step).  Stage 3 (curl) is fused into stage 4 and reads 0.                 */
+int fire_sim_profile(FireSim* sim, int enable);
+int fire_sim_stage_times(FireSim* sim, float* ms, int n);
+/* Relative residual ||b - A p||_2 / ||b||_2 of multigrid level 0 (FP64 sums, fixed order).        */
+int fire_sim_residual(FireSim* sim, double* rel, void* stream);
+
+/* ---- diagnostics (FIRE.stats / FIRE.profile, src/main.js:268-355) ------------------------------ */
+/* Per-channel min, max, mean and non-finite count of a 4-channel field: out[16] = 4 x (min, max,
+ * mean, bad).  Deterministic device reduction; synchronous.                                        */
+int fire_sim_stats(FireSim* sim, int which, double* out16, void* stream);
+/* Heat release rate in kW: sum of 354800 q / T dV over cells with q > 0 (src/main.js:347-352).     */
+int fire_sim_hrr(FireSim* sim, double* q_kw, void* stream);
+/* Queue the stats of S and the heat release into a pinned host buffer without waiting:
+ * out[0..15] = S stats as in fire_sim_stats, out[16] = heat release (kW).  The values are valid once
+ * `stream` has reached this point (fire_sim_sync or a stream/event wait).                          */
+int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream);
+
+/* ---- scene helpers (src/scene.js) ------------------------------------------------------------- */
+/* buildCampfire(seed) + packLogs (src/scene.js:13-42, 92-98): writes max_logs*8 floats (8 real logs,
+ * zero-padded); returns the number of real logs.                                                    */
+int fire_build_campfire(uint32_t seed, float* out, int max_logs);
+/* Seeded floor spots for the spot emitter: n records (x, 0, z, sigma, flux) with positions uniform
+ * on a disc of `radius` around the origin and flux uniform in [flux_lo, flux_hi] g/s.  Uses the
+ * reference's pcg hash (src/shaders/lib.js:11-18).                                                 */
+int fire_make_spots(uint32_t seed, int n, float flux_lo, float flux_hi, float sigma, float radius, float* out);
+
+/* ---- library ----------------------------------------------------------------------------------- */
+/* 1 if the library's kernels were built for the current device's architecture, else 0.             */
+int fire_device_ok(int device);
+const char* fire_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FIRE_SIM_H */

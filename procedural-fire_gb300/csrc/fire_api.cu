@@ -1,0 +1,881 @@
+// Host runtime behind the C ABI (include/fire_sim.h): the GB300 counterpart of FireSim (src/sim.js:48-649)
+// and of the page-level event and diagnostics API (src/main.js).
+//
+// Design:
+//   * All fields and multigrid levels live in one device arena (dense float4 / float arrays).
+//   * The per-step parameter block (SIM_FIELDS + extension, 800 bytes) is staged in a pinned ring and
+//     copied to the device ahead of each step on the caller's stream, replacing queue.writeBuffer of the
+//     uniform buffer (src/gpu.js:70).  The step body reads it through a fixed device pointer, so the
+//     whole step is captured once as a CUDA graph and replayed every step.
+//   * The emitter geometry runs outside the graph, only when stale (src/sim.js:632).
+//   * The residual-driven multigrid mode loops V-cycles inside the graph with a conditional WHILE node;
+//     the loop condition is set on the device from the FP64 residual norm, so no host round trip.
+#include <cmath>
+#include <cstdio>
+#include <cstdarg>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <cuda_runtime.h>
+#include "../../include/fire_sim.h"
+#include "fire_internal.h"
+
+namespace fire {
+
+const char* const kParamNames[P_COUNT] = {
+  "nx", "ny", "nz", "dx", "dt", "time", "frame", "seed",
+  "ox", "oy", "oz", "nLogs",
+  "fuelSrc", "bedFuel", "srcTemp", "bedTemp", "srcVel", "srcFreq", "srcSpeed", "srcThresh",
+  "ignT", "kMix", "rs", "heatOut", "expansion", "sootForm", "sootOx", "radCool",
+  "coolRate", "sootDissip", "smokeDissip", "vitDecay", "fuelDissip", "buoyancy", "vortEps", "turbAmp",
+  "turbFreq", "turbRise", "turbEvolve", "windX", "windZ", "gust", "intensity", "velDissip",
+  "bedRadius", "logSrc", "burstX", "burstY", "burstZ", "burstAmt", "smolder", "sponge", "hotR0", "hotR1", "hotY1",
+  "visc", "lamAge", "anchorFreq", "srcFloor", "anchorGain",
+};
+
+// SIM_DEFAULTS (src/sim.js:25-44) in SIM_FIELDS order; simulation-owned entries are 0 (seed: `?? 0`).
+const float kParamDefaults[P_STRIDE] = {
+  0, 0, 0, 0, 0, 0, 0, 0,                       // nx ny nz dx dt time frame seed
+  0, 0, 0, 0,                                   // ox oy oz nLogs
+  0.13f, 0.16f, 0.75f, 0.82f, 0.25f, 35.0f, 0.06f, 0.0f,       // fuelSrc bedFuel srcTemp bedTemp srcVel srcFreq srcSpeed srcThresh
+  550.0f, 30.0f, 4.7f, 7700.0f, 0.7f, 25.0f, 30.0f, 0.25f,     // ignT kMix rs heatOut expansion sootForm sootOx radCool
+  3.0f, 0.4f, 0.3f, 1.5f, 0.3f, 26.8f, 8.0f, 0.8f,             // coolRate sootDissip smokeDissip vitDecay fuelDissip buoyancy vortEps turbAmp
+  1.5f, 1.5f, 0.6f, 0.0f, 0.0f, 0.0f, 1.0f, 0.05f,             // turbFreq turbRise turbEvolve windX windZ gust intensity velDissip
+  0.22f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.02f, 1.0f, 0.12f, 0.45f, 0.5f,   // bedRadius logSrc burstX..burstAmt smolder sponge hotR0 hotR1 hotY1
+  0.0f, 0.0f, 1.6f, 0.25f, 0.95f,                              // visc lamAge anchorFreq srcFloor anchorGain
+  0, 0, 0, 0,                                                   // padding to 64
+};
+
+// ---- kernels defined in other translation units that the runtime launches directly ----
+cudaError_t kernels_probe();
+void launch_mg_decide(const double* sums2, double tol, int max_cycles, int* counter, double* rel_out,
+                      cudaGraphConditionalHandle h, cudaStream_t st);
+void launch_mg_counter_reset(int* counter, cudaStream_t st);
+
+}  // namespace fire
+
+using namespace fire;
+
+namespace {
+constexpr int RING_SLOTS = 256;
+constexpr int SLOT_FLOATS = BLOCK_FLOATS + MAX_LOGS * 8;   // param block + log buffer (1312 bytes)
+constexpr size_t ALIGN = 256;
+size_t align_up(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
+}  // namespace
+
+struct FireSim {
+  int device = 0;
+  int res[3] = {0, 0, 0};
+  float size[3] = {0, 0, 0};
+  double dx = 0;
+  float origin[3] = {0, 0, 0};
+  int vcycles = 2;
+  int mg_max_cycles = 0;
+  double mg_tol = 0;
+  double time = 0;
+  long long frame = 0;
+  float params[P_STRIDE];
+  float ext[E_COUNT];
+  float logs[MAX_LOGS * 8];
+  int nLogs = 0;
+  bool geoReady = false;
+  bool logsDirty = true;
+
+  // device
+  void* arena = nullptr;
+  size_t arenaBytes = 0;
+  Fields f{};
+  Dims d{};
+  std::vector<MGLevel> levels;
+  int coarseIters = 8;
+  int tailFirst = 0;
+  uint2* noise = nullptr;
+  uint2* curl = nullptr;
+  float* dBlock = nullptr;
+  float* dLogs = nullptr;
+  double* dPartials = nullptr;
+  int partialsCount = 0;
+  double* dSmall = nullptr;     // [0..1] residual sums, [2..17] stats, [18] hrr, [19] rel residual
+  int* dCounter = nullptr;      // V-cycles run by the residual-driven loop
+
+  // host staging
+  float* hRing = nullptr;
+  cudaEvent_t ringEv[RING_SLOTS];
+  bool ringUsed[RING_SLOTS];
+  int ringPos = 0;
+  double* hSmall = nullptr;     // pinned mirror of dSmall
+  int* hCounter = nullptr;
+
+  cudaStream_t capStream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool graphProfiled = false;
+  bool profiling = false;
+  cudaEvent_t stageEv[FIRE_STAGE_COUNT + 1];
+  cudaEvent_t doneEv = nullptr;
+  bool profiledStepPending = false;
+
+  // events (src/main.js:401-407, 456-461)
+  double burstUntil = -1;
+  float burstAmt = 0;
+  bool burstActive = false;
+  double gustLeft = 0, gustDur = 2.4;
+  float gustStrength = 1;
+  bool gustActive = false;
+  float windBase[2] = {0, 0};
+
+  int lastCycles = 0;
+  double lastRel = -1;
+  long long stepsRun = 0;
+  std::string err;
+};
+
+namespace {
+
+int set_err(FireSim* s, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (s) s->err = buf;
+  return code;
+}
+#define CK(call)                                                                                    \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) return set_err(sim, FIRE_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+float* field_ptr4(FireSim* s, int which) {
+  switch (which) {
+    case FIRE_FIELD_VEL: return (float*)s->f.vel;
+    case FIRE_FIELD_VELX: return (float*)s->f.velX;
+    case FIRE_FIELD_VELY: return (float*)s->f.velY;
+    case FIRE_FIELD_S: return (float*)s->f.S;
+    case FIRE_FIELD_SX: return (float*)s->f.SX;
+    case FIRE_FIELD_SY: return (float*)s->f.SY;
+    case FIRE_FIELD_S2: return (float*)s->f.S2;
+    case FIRE_FIELD_S2X: return (float*)s->f.S2X;
+    case FIRE_FIELD_S2Y: return (float*)s->f.S2Y;
+    case FIRE_FIELD_VORT: return (float*)s->f.vort;
+    case FIRE_FIELD_GEO: return (float*)s->f.geo;
+    default: return nullptr;
+  }
+}
+
+// Fill the simulation-owned entries of the block, as uploadUniforms does (src/sim.js:620-624), and apply
+// the event envelopes for this step.
+void fill_block(FireSim* s, float dt, float* out) {
+  float* P = out;
+  std::memcpy(P, s->params, sizeof(float) * P_STRIDE);
+  P[P_nx] = (float)s->res[0]; P[P_ny] = (float)s->res[1]; P[P_nz] = (float)s->res[2];
+  P[P_dx] = (float)s->dx; P[P_dt] = dt; P[P_time] = (float)s->time; P[P_frame] = (float)s->frame;
+  P[P_ox] = s->origin[0]; P[P_oy] = s->origin[1]; P[P_oz] = s->origin[2];
+  P[P_nLogs] = (float)s->nLogs;
+  std::memcpy(P + P_STRIDE, s->ext, sizeof(float) * E_COUNT);
+}
+
+void advance_events(FireSim* s, float dt) {
+  // burst: burstAmt held while the simulated time is before burstUntil (src/main.js:404, 461)
+  if (s->burstActive) {
+    if (s->time < s->burstUntil) s->params[P_burstAmt] = s->burstAmt;
+    else { s->params[P_burstAmt] = 0.0f; s->burstActive = false; }
+  }
+  // gust: windT counts down before the envelope is evaluated (src/main.js:459-461)
+  if (s->gustActive) {
+    s->gustLeft = std::max(0.0, s->gustLeft - (double)dt);
+    double gw = s->gustLeft > 0 ? std::sin(3.141592653589793 * (1.0 - s->gustLeft / s->gustDur)) : 0.0;
+    s->params[P_windX] = (float)(s->windBase[0] + -1.4 * gw * s->gustStrength);
+    s->params[P_windZ] = (float)(s->windBase[1] + 0.5 * gw * s->gustStrength);
+    if (s->gustLeft <= 0) {
+      s->gustActive = false;
+      s->params[P_windX] = s->windBase[0];
+      s->params[P_windZ] = s->windBase[1];
+    }
+  }
+}
+
+// Stage a slot of the pinned ring (waiting if its previous copy has not run yet).
+int ring_slot(FireSim* sim, float** slot, cudaEvent_t* ev) {
+  int k = sim->ringPos;
+  sim->ringPos = (k + 1) % RING_SLOTS;
+  if (sim->ringUsed[k]) CK(cudaEventSynchronize(sim->ringEv[k]));
+  sim->ringUsed[k] = true;
+  *slot = sim->hRing + (size_t)k * SLOT_FLOATS;
+  *ev = sim->ringEv[k];
+  return FIRE_OK;
+}
+
+int upload_block(FireSim* sim, float dt, cudaStream_t st, bool with_logs) {
+  float* slot;
+  cudaEvent_t ev;
+  int rc = ring_slot(sim, &slot, &ev);
+  if (rc) return rc;
+  fill_block(sim, dt, slot);
+  CK(cudaMemcpyAsync(sim->dBlock, slot, sizeof(float) * BLOCK_FLOATS, cudaMemcpyHostToDevice, st));
+  if (with_logs) {
+    std::memcpy(slot + BLOCK_FLOATS, sim->logs, sizeof(float) * MAX_LOGS * 8);
+    CK(cudaMemcpyAsync(sim->dLogs, slot + BLOCK_FLOATS, sizeof(float) * MAX_LOGS * 8, cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaEventRecord(ev, st));
+  return FIRE_OK;
+}
+
+void record_smooth(FireSim* s, int l, int iters, cudaStream_t st) {
+  for (int k = 0; k < iters; ++k) { launch_smooth(s->levels[l], 0, st); launch_smooth(s->levels[l], 1, st); }
+}
+// One V(2,2) cycle (src/sim.js:588-599).  Levels [tailFirst, n) run inside one single-CTA kernel.
+void record_vcycle(FireSim* s, cudaStream_t st) {
+  const int n = (int)s->levels.size();
+  const int T = s->tailFirst;
+  const int top = std::min(T, n - 1);
+  for (int i = 0; i < top; ++i) { record_smooth(s, i, 2, st); launch_restrict(s->levels[i], s->levels[i + 1], st); }
+  if (T < n) launch_tail(s->levels.data(), T, n, 2, 2, s->coarseIters, st);
+  else record_smooth(s, n - 1, s->coarseIters, st);
+  for (int i = top - 1; i >= 0; --i) { launch_prolong(s->levels[i], s->levels[i + 1], st); record_smooth(s, i, 2, st); }
+}
+
+int record_ev(FireSim* sim, int idx, cudaStream_t st, bool prof) {
+  if (prof) CK(cudaEventRecordWithFlags(sim->stageEv[idx], st, cudaEventRecordExternal));
+  return FIRE_OK;
+}
+
+// Records the multigrid solve: a fixed number of cycles, or (residual-driven mode) a conditional
+// WHILE loop whose body is one cycle plus the FP64 residual norm and the device-side decision.
+int record_mg(FireSim* sim, cudaStream_t st) {
+  if (sim->mg_max_cycles <= 0) {
+    for (int c = 0; c < sim->vcycles; ++c) record_vcycle(sim, st);
+    return FIRE_OK;
+  }
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  const cudaGraphNode_t* deps;
+  size_t ndeps;
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+  if (cs != cudaStreamCaptureStatusActive) return set_err(sim, FIRE_ERR_STATE, "residual-driven solve needs graph capture");
+  launch_mg_counter_reset(sim->dCounter, st);
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  // capture the loop body on the side stream into the body graph
+  cudaStream_t bs = sim->capStream;
+  CK(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  record_vcycle(sim, bs);
+  launch_residual(sim->levels[0], sim->dPartials, sim->dSmall, bs);
+  launch_mg_decide(sim->dSmall, sim->mg_tol, sim->mg_max_cycles, sim->dCounter, sim->dSmall + 19, h, bs);
+  cudaGraph_t outg;
+  CK(cudaStreamEndCapture(bs, &outg));
+  return FIRE_OK;
+}
+
+// Records one step body (src/sim.js:633-644) on `st`: the parameter block must already be on the device.
+int record_step(FireSim* sim, cudaStream_t st, bool prof) {
+  int rc;
+  const Dims d = sim->d;
+  const float* P = sim->dBlock;
+  if ((rc = record_ev(sim, 0, st, prof))) return rc;
+  launch_adv1(P, sim->f, d, st);
+  if ((rc = record_ev(sim, 1, st, prof))) return rc;
+  launch_adv2(P, sim->f, d, st);
+  if ((rc = record_ev(sim, 2, st, prof))) return rc;
+  if ((rc = record_ev(sim, 3, st, prof))) return rc;    // curl is fused into forces
+  launch_forces(P, sim->f, sim->noise, sim->curl, d, st);
+  if ((rc = record_ev(sim, 4, st, prof))) return rc;
+  launch_div(P, sim->f, sim->levels[0].b, d, st);
+  if ((rc = record_ev(sim, 5, st, prof))) return rc;
+  if ((rc = record_mg(sim, st))) return rc;
+  if ((rc = record_ev(sim, 6, st, prof))) return rc;
+  launch_project(P, sim->f, sim->levels[0].p, d, st);
+  if ((rc = record_ev(sim, 7, st, prof))) return rc;
+  CK(cudaGetLastError());
+  return FIRE_OK;
+}
+
+void drop_graph(FireSim* s) {
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->exec = nullptr;
+  s->graph = nullptr;
+}
+
+int build_graph(FireSim* sim) {
+  drop_graph(sim);
+  // the main capture runs on a private stream; the residual loop body is captured on capStream
+  cudaStream_t st;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) { cudaStreamDestroy(st); return set_err(sim, FIRE_ERR_CUDA, "begin capture: %s", cudaGetErrorString(e)); }
+  int rc = record_step(sim, st, sim->profiling);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(st, &g);
+  cudaStreamDestroy(st);
+  if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+  if (e != cudaSuccess) return set_err(sim, FIRE_ERR_CUDA, "end capture: %s", cudaGetErrorString(e));
+  sim->graph = g;
+  e = cudaGraphInstantiate(&sim->exec, g, 0);
+  if (e != cudaSuccess) { drop_graph(sim); return set_err(sim, FIRE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+  sim->graphProfiled = sim->profiling;
+  return FIRE_OK;
+}
+
+int ensure_geo(FireSim* sim, cudaStream_t st) {
+  if (sim->geoReady && !sim->logsDirty) return FIRE_OK;
+  // geometry uses the current block (dx, origin, hot radii, nLogs) and the log buffer
+  launch_geo(sim->dBlock, sim->dLogs, sim->f.geo, sim->d, st);
+  CK(cudaGetLastError());
+  sim->geoReady = true;
+  sim->logsDirty = false;
+  return FIRE_OK;
+}
+
+}  // namespace
+
+// =====================================================================================================
+extern "C" {
+
+const char* fire_version(void) { return "procedural-fire-gb300 0.1 (sm_103a)"; }
+
+int fire_param_index(const char* name) {
+  if (!name) return -1;
+  for (int i = 0; i < P_COUNT; ++i)
+    if (std::strcmp(name, kParamNames[i]) == 0) return i;
+  return -1;
+}
+const char* fire_param_name(int index) { return (index >= 0 && index < P_COUNT) ? kParamNames[index] : nullptr; }
+int fire_param_defaults(float* block64) {
+  if (!block64) return FIRE_ERR_BAD_ARG;
+  std::memcpy(block64, kParamDefaults, sizeof(float) * P_STRIDE);
+  return FIRE_OK;
+}
+
+int fire_device_ok(int device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return 0;
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return 0;
+  if (p.major != 10 || p.minor != 3) return 0;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(device);
+  cudaError_t e = kernels_probe();
+  cudaSetDevice(prev);
+  return e == cudaSuccess ? 1 : 0;
+}
+
+int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSim** out) {
+  FireSim* sim = nullptr;
+  if (!cfg || !out) return FIRE_ERR_BAD_ARG;
+  *out = nullptr;
+  for (int i = 0; i < 3; ++i)
+    if (cfg->res[i] < 2 || cfg->size[i] <= 0.0f) return FIRE_ERR_BAD_ARG;
+  if (n_logs < 0 || n_logs > MAX_LOGS || (n_logs > 0 && !logs)) return FIRE_ERR_BAD_ARG;
+  if (cfg->vcycles < 0 || cfg->mg_max_cycles < 0) return FIRE_ERR_BAD_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return FIRE_ERR_NO_DEVICE;
+  if (cfg->device < 0 || cfg->device >= ndev) return FIRE_ERR_BAD_ARG;
+  if (!fire_device_ok(cfg->device)) return FIRE_ERR_NO_DEVICE;
+
+  sim = new FireSim();
+  sim->device = cfg->device;
+  if (cudaSetDevice(sim->device) != cudaSuccess) { delete sim; return FIRE_ERR_NO_DEVICE; }
+  for (int i = 0; i < 3; ++i) { sim->res[i] = cfg->res[i]; sim->size[i] = cfg->size[i]; }
+  sim->dx = (double)cfg->size[0] / (double)cfg->res[0];                        // src/sim.js:53
+  sim->origin[0] = -cfg->size[0] / 2; sim->origin[1] = 0; sim->origin[2] = -cfg->size[2] / 2;   // src/sim.js:54
+  sim->vcycles = cfg->vcycles;
+  sim->mg_max_cycles = cfg->mg_max_cycles;
+  sim->mg_tol = cfg->mg_tol;
+  std::memcpy(sim->params, kParamDefaults, sizeof sim->params);
+  std::memset(sim->ext, 0, sizeof sim->ext);
+  sim->ext[E_sootAge0] = 0.015f;
+  sim->ext[E_sootAge1] = 0.05f;
+  sim->ext[E_bedGain] = 1.0f;
+  sim->ext[E_spotRef] = 4.0f;
+  std::memset(sim->logs, 0, sizeof sim->logs);
+  if (n_logs > 0) std::memcpy(sim->logs, logs, sizeof(float) * 8 * n_logs);
+  sim->nLogs = n_logs;
+  sim->d = Dims{cfg->res[0], cfg->res[1], cfg->res[2]};
+
+  // multigrid hierarchy (src/sim.js:79-87): halve while every dim is even and the smallest > 6
+  {
+    int x = cfg->res[0], y = cfg->res[1], z = cfg->res[2];
+    double h = sim->dx;
+    while (true) {
+      MGLevel L{x, y, z, (float)h, nullptr, nullptr};
+      sim->levels.push_back(L);
+      if (x % 2 || y % 2 || z % 2 || std::min(x, std::min(y, z)) <= 6) break;
+      x /= 2; y /= 2; z /= 2; h *= 2;
+    }
+    const MGLevel& C = sim->levels.back();
+    const double PI = 3.14159265358979323846;
+    double mu = (std::cos(PI / C.nx) + std::cos(PI / (2.0 * C.ny)) + std::cos(PI / C.nz)) / 3.0;   // src/sim.js:91-92
+    sim->coarseIters = (int)std::max(8.0, std::min(64.0, std::ceil(std::log(0.05) / std::log(mu * mu))));
+    const int n = (int)sim->levels.size();
+    sim->tailFirst = n;
+    for (int l = n - 1; l >= 0; --l) {
+      if (tail_smem_bytes(sim->levels.data(), l, n) <= TAIL_SMEM_BUDGET) sim->tailFirst = l;
+      else break;
+    }
+  }
+
+  // device arena
+  const size_t cells = (size_t)cfg->res[0] * cfg->res[1] * cfg->res[2];
+  size_t off = 0;
+  std::vector<size_t> fieldOff(11);
+  for (int i = 0; i < 11; ++i) { fieldOff[i] = off; off = align_up(off + cells * sizeof(float4)); }
+  std::vector<size_t> pOff(sim->levels.size()), bOff(sim->levels.size());
+  for (size_t l = 0; l < sim->levels.size(); ++l) {
+    size_t c = (size_t)sim->levels[l].nx * sim->levels[l].ny * sim->levels[l].nz;
+    pOff[l] = off; off = align_up(off + c * sizeof(float));
+    bOff[l] = off; off = align_up(off + c * sizeof(float));
+  }
+  const size_t tabBytes = (size_t)TABLE_N * TABLE_N * TABLE_N * sizeof(uint2);
+  size_t noiseOff = off; off = align_up(off + tabBytes);
+  size_t curlOff = off; off = align_up(off + tabBytes);
+  size_t blockOff = off; off = align_up(off + sizeof(float) * BLOCK_FLOATS);
+  size_t logsOff = off; off = align_up(off + sizeof(float) * MAX_LOGS * 8);
+  sim->partialsCount = std::max(stats_partials_count(sim->d), residual_partials_count(sim->levels[0]));
+  size_t partOff = off; off = align_up(off + sizeof(double) * 16 * (size_t)sim->partialsCount);
+  size_t smallOff = off; off = align_up(off + sizeof(double) * 32);
+  size_t cntOff = off; off = align_up(off + sizeof(int) * 4);
+  sim->arenaBytes = off;
+  cudaError_t e = cudaMalloc(&sim->arena, off);
+  if (e != cudaSuccess) { delete sim; return FIRE_ERR_OOM; }
+  char* A = (char*)sim->arena;
+  float4** fp[11] = {&sim->f.vel, &sim->f.velX, &sim->f.velY, &sim->f.S, &sim->f.SX, &sim->f.SY,
+                     &sim->f.S2, &sim->f.S2X, &sim->f.S2Y, &sim->f.vort, &sim->f.geo};
+  for (int i = 0; i < 11; ++i) *fp[i] = (float4*)(A + fieldOff[i]);
+  for (size_t l = 0; l < sim->levels.size(); ++l) { sim->levels[l].p = (float*)(A + pOff[l]); sim->levels[l].b = (float*)(A + bOff[l]); }
+  sim->noise = (uint2*)(A + noiseOff);
+  sim->curl = (uint2*)(A + curlOff);
+  sim->dBlock = (float*)(A + blockOff);
+  sim->dLogs = (float*)(A + logsOff);
+  sim->dPartials = (double*)(A + partOff);
+  sim->dSmall = (double*)(A + smallOff);
+  sim->dCounter = (int*)(A + cntOff);
+
+  auto fail = [&](int code) { fire_sim_destroy(sim); return code; };
+  if (cudaHostAlloc((void**)&sim->hRing, sizeof(float) * SLOT_FLOATS * RING_SLOTS, cudaHostAllocDefault) != cudaSuccess) return fail(FIRE_ERR_OOM);
+  if (cudaHostAlloc((void**)&sim->hSmall, sizeof(double) * 32, cudaHostAllocDefault) != cudaSuccess) return fail(FIRE_ERR_OOM);
+  if (cudaHostAlloc((void**)&sim->hCounter, sizeof(int) * 4, cudaHostAllocDefault) != cudaSuccess) return fail(FIRE_ERR_OOM);
+  for (int k = 0; k < RING_SLOTS; ++k) {
+    sim->ringUsed[k] = false;
+    if (cudaEventCreateWithFlags(&sim->ringEv[k], cudaEventDisableTiming) != cudaSuccess) return fail(FIRE_ERR_CUDA);
+  }
+  for (int k = 0; k <= FIRE_STAGE_COUNT; ++k)
+    if (cudaEventCreate(&sim->stageEv[k]) != cudaSuccess) return fail(FIRE_ERR_CUDA);
+  if (cudaEventCreateWithFlags(&sim->doneEv, cudaEventDisableTiming) != cudaSuccess) return fail(FIRE_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&sim->capStream, cudaStreamNonBlocking) != cudaSuccess) return fail(FIRE_ERR_CUDA);
+  if (mg_configure(TAIL_SMEM_BUDGET) != cudaSuccess) return fail(set_err(sim, FIRE_ERR_CUDA, "tail kernel smem opt-in failed"));
+
+  // zero state (reset semantics), bake the tables (src/noise.js), upload logs
+  cudaStream_t st = sim->capStream;
+  if (cudaMemsetAsync(sim->arena, 0, sim->arenaBytes, st) != cudaSuccess) return fail(FIRE_ERR_CUDA);
+  launch_noise_table(sim->noise, TABLE_N, cfg->noise_seed, st);
+  launch_curl_table(sim->noise, sim->curl, TABLE_N, st);
+  if (cudaGetLastError() != cudaSuccess) return fail(FIRE_ERR_CUDA);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_err(sim, FIRE_ERR_CUDA, "table bake failed"));
+  sim->geoReady = false;
+  sim->logsDirty = true;
+  *out = sim;
+  return FIRE_OK;
+}
+
+int fire_sim_destroy(FireSim* sim) {
+  if (!sim) return FIRE_ERR_BAD_ARG;
+  cudaSetDevice(sim->device);
+  cudaDeviceSynchronize();
+  drop_graph(sim);
+  for (int k = 0; k < RING_SLOTS; ++k) if (sim->ringEv[k]) cudaEventDestroy(sim->ringEv[k]);
+  for (int k = 0; k <= FIRE_STAGE_COUNT; ++k) if (sim->stageEv[k]) cudaEventDestroy(sim->stageEv[k]);
+  if (sim->doneEv) cudaEventDestroy(sim->doneEv);
+  if (sim->capStream) cudaStreamDestroy(sim->capStream);
+  if (sim->hRing) cudaFreeHost(sim->hRing);
+  if (sim->hSmall) cudaFreeHost(sim->hSmall);
+  if (sim->hCounter) cudaFreeHost(sim->hCounter);
+  if (sim->arena) cudaFree(sim->arena);
+  delete sim;
+  return FIRE_OK;
+}
+
+int fire_sim_step(FireSim* sim, float dt, int n_steps, void* stream) {
+  if (!sim || n_steps < 0 || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
+  CK(cudaSetDevice(sim->device));
+  cudaStream_t st = as_stream(stream);
+  if (!sim->exec || sim->graphProfiled != sim->profiling) {
+    int rc = build_graph(sim);
+    if (rc) return rc;
+  }
+  for (int s = 0; s < n_steps; ++s) {
+    advance_events(sim, dt);
+    const bool geo = !sim->geoReady || sim->logsDirty;
+    int rc = upload_block(sim, dt, st, geo);
+    if (rc) return rc;
+    if (geo && (rc = ensure_geo(sim, st))) return rc;
+    CK(cudaGraphLaunch(sim->exec, st));
+    sim->time += dt;                                                          // src/sim.js:646-647
+    sim->frame += 1;
+    sim->stepsRun += 1;
+  }
+  if (sim->profiling) { CK(cudaEventRecord(sim->doneEv, st)); sim->profiledStepPending = n_steps > 0; }
+  return FIRE_OK;
+}
+
+int fire_sim_sync(FireSim* sim) {
+  if (!sim) return FIRE_ERR_BAD_ARG;
+  CK(cudaSetDevice(sim->device));
+  CK(cudaDeviceSynchronize());
+  return FIRE_OK;
+}
+
+int fire_sim_set_params(FireSim* sim, const char* const* names, const float* values, int n) {
+  if (!sim || n < 0 || (n > 0 && (!names || !values))) return FIRE_ERR_BAD_ARG;
+  int idx[P_COUNT * 4];
+  if (n > (int)(sizeof idx / sizeof idx[0])) return set_err(sim, FIRE_ERR_BAD_ARG, "too many parameters");
+  for (int i = 0; i < n; ++i) {
+    idx[i] = fire_param_index(names[i]);
+    if (idx[i] < 0) return set_err(sim, FIRE_ERR_BAD_PARAM, "unknown uniform SimParams.%s", names[i] ? names[i] : "(null)");
+  }
+  for (int i = 0; i < n; ++i) {
+    const int k = idx[i];
+    if (k == P_hotR0 || k == P_hotR1 || k == P_hotY1 || k == P_bedRadius) sim->geoReady = false;   // src/sim.js:602
+    sim->params[k] = values[i];
+    if (k == P_windX && !sim->gustActive) sim->windBase[0] = values[i];
+    if (k == P_windZ && !sim->gustActive) sim->windBase[1] = values[i];
+    if (k == P_burstAmt) sim->burstActive = false;   // an explicit burstAmt overrides a pending inject
+  }
+  return FIRE_OK;
+}
+int fire_sim_get_param(FireSim* sim, const char* name, float* value) {
+  if (!sim || !value) return FIRE_ERR_BAD_ARG;
+  int k = fire_param_index(name);
+  if (k < 0) return set_err(sim, FIRE_ERR_BAD_PARAM, "unknown uniform SimParams.%s", name ? name : "(null)");
+  *value = sim->params[k];
+  return FIRE_OK;
+}
+int fire_sim_set_param_block(FireSim* sim, const float* block64) {
+  if (!sim || !block64) return FIRE_ERR_BAD_ARG;
+  const char* names[P_COUNT];
+  float vals[P_COUNT];
+  int n = 0;
+  for (int k = P_seed; k < P_COUNT; ++k) {
+    if (k >= P_ox && k <= P_nLogs) continue;
+    names[n] = kParamNames[k];
+    vals[n++] = block64[k];
+  }
+  // only mark the geometry stale when a geometry parameter actually changes
+  bool geoChange = block64[P_hotR0] != sim->params[P_hotR0] || block64[P_hotR1] != sim->params[P_hotR1] ||
+                   block64[P_hotY1] != sim->params[P_hotY1] || block64[P_bedRadius] != sim->params[P_bedRadius];
+  bool was = sim->geoReady;
+  int rc = fire_sim_set_params(sim, names, vals, n);
+  if (rc == FIRE_OK && !geoChange) sim->geoReady = was;
+  return rc;
+}
+int fire_sim_get_param_block(FireSim* sim, float* block64) {
+  if (!sim || !block64) return FIRE_ERR_BAD_ARG;
+  std::memcpy(block64, sim->params, sizeof(float) * P_STRIDE);
+  return FIRE_OK;
+}
+int fire_sim_peek_block(FireSim* sim, float dt, float* out) {
+  if (!sim || !out) return FIRE_ERR_BAD_ARG;
+  static_assert(BLOCK_FLOATS == FIRE_BLOCK_FLOATS, "block size mismatch");
+  fill_block(sim, dt, out);
+  return FIRE_OK;
+}
+int fire_sim_set_soot_age(FireSim* sim, float age0, float age1) {
+  if (!sim || !(age1 > age0)) return FIRE_ERR_BAD_ARG;
+  sim->ext[E_sootAge0] = age0;
+  sim->ext[E_sootAge1] = age1;
+  return FIRE_OK;
+}
+int fire_sim_set_bed_gain(FireSim* sim, float gain) {
+  if (!sim || gain < 0.0f) return FIRE_ERR_BAD_ARG;
+  sim->ext[E_bedGain] = gain;
+  sim->geoReady = false;
+  return FIRE_OK;
+}
+int fire_sim_set_spots(FireSim* sim, const float* spots, int n) {
+  if (!sim || n < 0 || n > MAX_SPOTS || (n > 0 && !spots)) return FIRE_ERR_BAD_ARG;
+  for (int i = 0; i < n; ++i)
+    if (!(spots[5 * i + 3] > 0.0f) || spots[5 * i + 4] < 0.0f) return set_err(sim, FIRE_ERR_BAD_ARG, "spot %d: sigma must be > 0 and flux >= 0", i);
+  std::memset(sim->ext + E_SPOTS, 0, sizeof(float) * MAX_SPOTS * SPOT_STRIDE);
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 5; ++c) sim->ext[E_SPOTS + SPOT_STRIDE * i + c] = spots[5 * i + c];
+  sim->ext[E_nSpots] = (float)n;
+  return FIRE_OK;
+}
+
+int fire_sim_inject(FireSim* sim, float x, float y, float z, float amount, float duration) {
+  if (!sim || amount < 0.0f || duration < 0.0f) return FIRE_ERR_BAD_ARG;
+  sim->params[P_burstX] = x; sim->params[P_burstY] = y; sim->params[P_burstZ] = z;
+  sim->burstAmt = amount;
+  sim->burstUntil = sim->time + duration;
+  sim->burstActive = true;
+  return FIRE_OK;
+}
+int fire_sim_stoke(FireSim* sim, int log_index, float s) {
+  if (!sim || log_index < 0 || log_index >= sim->nLogs || s < 0.0f || s > 1.0f) return FIRE_ERR_BAD_ARG;
+  // applyLogs (src/main.js:135-150) with logOffsetsAt's offsets (src/timeline.js:126-133)
+  const float footOut = 0.02f, topDrop = 0.04f, topOut = 0.012f;
+  float* a = sim->logs + 8 * log_index;
+  float ox = a[0], oz = a[2];
+  float l = std::hypot(ox, oz);
+  if (l == 0.0f) l = 1.0f;
+  float dxn = ox / l, dzn = oz / l;
+  a[0] += dxn * footOut * s; a[2] += dzn * footOut * s; a[1] -= 0.004f * s;
+  a[4] += dxn * topOut * s; a[6] += dzn * topOut * s; a[5] -= topDrop * s;
+  sim->logsDirty = true;
+  return fire_sim_inject(sim, a[0], 0.08f, a[2], 1.0f, 0.25f);   // the log-shift burst (src/main.js:404)
+}
+int fire_sim_gust(FireSim* sim, float strength, float duration) {
+  if (!sim || !(duration > 0.0f)) return FIRE_ERR_BAD_ARG;
+  if (!sim->gustActive) { sim->windBase[0] = sim->params[P_windX]; sim->windBase[1] = sim->params[P_windZ]; }
+  sim->gustActive = true;
+  sim->gustLeft = duration;
+  sim->gustDur = duration;
+  sim->gustStrength = strength;
+  return FIRE_OK;
+}
+
+int fire_sim_reset(FireSim* sim) {
+  if (!sim) return FIRE_ERR_BAD_ARG;
+  CK(cudaSetDevice(sim->device));
+  CK(cudaDeviceSynchronize());
+  const size_t cells = (size_t)sim->res[0] * sim->res[1] * sim->res[2];
+  for (int w = FIRE_FIELD_VEL; w <= FIRE_FIELD_VORT; ++w) CK(cudaMemset(field_ptr4(sim, w), 0, cells * sizeof(float4)));
+  for (auto& L : sim->levels) CK(cudaMemset(L.p, 0, sizeof(float) * (size_t)L.nx * L.ny * L.nz));
+  sim->time = 0;
+  sim->frame = 0;
+  return FIRE_OK;
+}
+
+int fire_sim_upload_logs(FireSim* sim, const float* logs, int n_logs) {
+  if (!sim || n_logs < 0 || n_logs > MAX_LOGS || (n_logs > 0 && !logs)) return FIRE_ERR_BAD_ARG;
+  std::memset(sim->logs, 0, sizeof sim->logs);
+  if (n_logs > 0) std::memcpy(sim->logs, logs, sizeof(float) * 8 * n_logs);
+  sim->nLogs = n_logs;
+  sim->logsDirty = true;
+  return FIRE_OK;
+}
+
+int fire_sim_field(FireSim* sim, int which, FireFieldDesc* out) {
+  if (!sim || !out) return FIRE_ERR_BAD_ARG;
+  std::memset(out, 0, sizeof *out);
+  if (which >= FIRE_FIELD_VEL && which <= FIRE_FIELD_GEO) {
+    out->data = field_ptr4(sim, which);
+    for (int i = 0; i < 3; ++i) out->dims[i] = sim->res[i];
+    out->channels = 4; out->elem_bytes = 4;
+  } else if (which == FIRE_FIELD_P || which == FIRE_FIELD_B) {
+    out->data = which == FIRE_FIELD_P ? sim->levels[0].p : sim->levels[0].b;
+    for (int i = 0; i < 3; ++i) out->dims[i] = sim->res[i];
+    out->channels = 1; out->elem_bytes = 4;
+  } else if (which == FIRE_FIELD_NOISE || which == FIRE_FIELD_CURL) {
+    out->data = which == FIRE_FIELD_NOISE ? (void*)sim->noise : (void*)sim->curl;
+    for (int i = 0; i < 3; ++i) out->dims[i] = TABLE_N;
+    out->channels = 4; out->elem_bytes = 2;
+  } else {
+    return set_err(sim, FIRE_ERR_BAD_ARG, "unknown field %d", which);
+  }
+  out->strides[0] = (size_t)out->channels * out->elem_bytes;
+  out->strides[1] = out->strides[0] * out->dims[0];
+  out->strides[2] = out->strides[1] * out->dims[1];
+  out->bytes = out->strides[2] * out->dims[2];
+  return FIRE_OK;
+}
+
+int fire_sim_download(FireSim* sim, int which, void* host, size_t bytes) {
+  FireFieldDesc d;
+  int rc = fire_sim_field(sim, which, &d);
+  if (rc) return rc;
+  if (!host || bytes != d.bytes) return set_err(sim, FIRE_ERR_BAD_ARG, "download: need %zu bytes, got %zu", d.bytes, bytes);
+  CK(cudaSetDevice(sim->device));
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(host, d.data, bytes, cudaMemcpyDeviceToHost));
+  return FIRE_OK;
+}
+int fire_sim_upload(FireSim* sim, int which, const void* host, size_t bytes) {
+  FireFieldDesc d;
+  int rc = fire_sim_field(sim, which, &d);
+  if (rc) return rc;
+  if (!host || bytes != d.bytes) return set_err(sim, FIRE_ERR_BAD_ARG, "upload: need %zu bytes, got %zu", d.bytes, bytes);
+  CK(cudaSetDevice(sim->device));
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(d.data, host, bytes, cudaMemcpyHostToDevice));
+  if (which == FIRE_FIELD_GEO) { sim->geoReady = true; sim->logsDirty = false; }   // caller-provided geometry
+  return FIRE_OK;
+}
+
+int fire_sim_info(FireSim* sim, FireInfo* out) {
+  if (!sim || !out) return FIRE_ERR_BAD_ARG;
+  std::memset(out, 0, sizeof *out);
+  for (int i = 0; i < 3; ++i) { out->res[i] = sim->res[i]; out->size[i] = sim->size[i]; out->origin[i] = sim->origin[i]; }
+  out->dx = (float)sim->dx;
+  out->time = sim->time;
+  out->frame = sim->frame;
+  out->n_levels = (int)sim->levels.size();
+  out->coarse_iters = sim->coarseIters;
+  out->vcycles = sim->vcycles;
+  if (sim->mg_max_cycles > 0) {
+    cudaSetDevice(sim->device);
+    cudaDeviceSynchronize();
+    int cnt[2] = {0, 0};
+    double rel = -1;
+    cudaMemcpy(cnt, sim->dCounter, 2 * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(&rel, sim->dSmall + 19, sizeof(double), cudaMemcpyDeviceToHost);
+    sim->lastCycles = cnt[0];
+    sim->lastRel = rel;
+    out->total_cycles = cnt[1];
+  } else {
+    sim->lastCycles = sim->vcycles;
+    out->total_cycles = (long long)sim->stepsRun * sim->vcycles;
+  }
+  out->last_cycles = sim->lastCycles;
+  out->last_rel_residual = sim->lastRel;
+  return FIRE_OK;
+}
+
+const char* fire_sim_last_error(FireSim* sim) { return sim ? sim->err.c_str() : "null handle"; }
+
+int fire_sim_run_stage(FireSim* sim, int stage, float dt, void* stream) {
+  if (!sim || stage < 0 || stage >= FIRE_STAGE_COUNT) return FIRE_ERR_BAD_ARG;
+  CK(cudaSetDevice(sim->device));
+  cudaStream_t st = as_stream(stream);
+  int rc = upload_block(sim, dt, st, stage == FIRE_STAGE_GEO);
+  if (rc) return rc;
+  const float* P = sim->dBlock;
+  switch (stage) {
+    case FIRE_STAGE_GEO: sim->geoReady = false; rc = ensure_geo(sim, st); if (rc) return rc; break;
+    case FIRE_STAGE_ADV1: launch_adv1(P, sim->f, sim->d, st); break;
+    case FIRE_STAGE_ADV2: launch_adv2(P, sim->f, sim->d, st); break;
+    case FIRE_STAGE_CURL: launch_curl(sim->f, sim->d, st); break;
+    case FIRE_STAGE_FORCES: launch_forces(P, sim->f, sim->noise, sim->curl, sim->d, st); break;
+    case FIRE_STAGE_DIV: launch_div(P, sim->f, sim->levels[0].b, sim->d, st); break;
+    case FIRE_STAGE_VCYCLE: record_vcycle(sim, st); break;
+    case FIRE_STAGE_PROJECT: launch_project(P, sim->f, sim->levels[0].p, sim->d, st); break;
+  }
+  CK(cudaGetLastError());
+  return FIRE_OK;
+}
+
+int fire_sim_run_mg(FireSim* sim, int op, int level, int arg, void* stream) {
+  if (!sim || level < 0 || level >= (int)sim->levels.size()) return FIRE_ERR_BAD_ARG;
+  CK(cudaSetDevice(sim->device));
+  cudaStream_t st = as_stream(stream);
+  const int n = (int)sim->levels.size();
+  switch (op) {
+    case 1: if (arg != 0 && arg != 1) return FIRE_ERR_BAD_ARG; launch_smooth(sim->levels[level], arg, st); break;
+    case 2: if (level >= n - 1) return FIRE_ERR_BAD_ARG; launch_restrict(sim->levels[level], sim->levels[level + 1], st); break;
+    case 3: if (level >= n - 1) return FIRE_ERR_BAD_ARG; launch_prolong(sim->levels[level], sim->levels[level + 1], st); break;
+    case 4: launch_tail(sim->levels.data(), level, n, 2, 2, sim->coarseIters, st); break;   // tail from `level`
+    default: return FIRE_ERR_BAD_ARG;
+  }
+  if (op == 4 && tail_smem_bytes(sim->levels.data(), level, n) > TAIL_SMEM_BUDGET) return FIRE_ERR_BAD_ARG;
+  CK(cudaGetLastError());
+  return FIRE_OK;
+}
+
+int fire_sim_level_dims(FireSim* sim, int level, int dims3[3], float* h) {
+  if (!sim || !dims3 || level < 0 || level >= (int)sim->levels.size()) return FIRE_ERR_BAD_ARG;
+  dims3[0] = sim->levels[level].nx; dims3[1] = sim->levels[level].ny; dims3[2] = sim->levels[level].nz;
+  if (h) *h = sim->levels[level].h;
+  return FIRE_OK;
+}
+
+int fire_sim_level_io(FireSim* sim, int level, int which, void* host, size_t bytes, int to_device) {
+  if (!sim || !host || level < 0 || level >= (int)sim->levels.size() || (which != 0 && which != 1)) return FIRE_ERR_BAD_ARG;
+  const MGLevel& L = sim->levels[level];
+  size_t need = sizeof(float) * (size_t)L.nx * L.ny * L.nz;
+  if (bytes != need) return set_err(sim, FIRE_ERR_BAD_ARG, "level io: need %zu bytes", need);
+  CK(cudaSetDevice(sim->device));
+  CK(cudaDeviceSynchronize());
+  float* dptr = which ? L.b : L.p;
+  if (to_device) CK(cudaMemcpy(dptr, host, bytes, cudaMemcpyHostToDevice));
+  else CK(cudaMemcpy(host, dptr, bytes, cudaMemcpyDeviceToHost));
+  return FIRE_OK;
+}
+
+int fire_sim_profile(FireSim* sim, int enable) {
+  if (!sim) return FIRE_ERR_BAD_ARG;
+  sim->profiling = enable != 0;
+  return FIRE_OK;
+}
+int fire_sim_stage_times(FireSim* sim, float* ms, int n) {
+  if (!sim || !ms || n < FIRE_STAGE_COUNT) return FIRE_ERR_BAD_ARG;
+  if (!sim->graphProfiled || !sim->profiledStepPending) return set_err(sim, FIRE_ERR_STATE, "no profiled step has run");
+  CK(cudaSetDevice(sim->device));
+  CK(cudaEventSynchronize(sim->doneEv));
+  // event k marks the start of stage slot k: 0 adv1, 1 adv2, 2 (curl, fused), 3 forces, 4 div, 5 mg, 6 project, 7 end
+  float t[FIRE_STAGE_COUNT];
+  for (int k = 0; k < 7; ++k) CK(cudaEventElapsedTime(&t[k], sim->stageEv[k], sim->stageEv[k + 1]));
+  ms[FIRE_STAGE_GEO] = 0.0f;
+  ms[FIRE_STAGE_ADV1] = t[0];
+  ms[FIRE_STAGE_ADV2] = t[1];
+  ms[FIRE_STAGE_CURL] = t[2];
+  ms[FIRE_STAGE_FORCES] = t[3];
+  ms[FIRE_STAGE_DIV] = t[4];
+  ms[FIRE_STAGE_VCYCLE] = t[5];
+  ms[FIRE_STAGE_PROJECT] = t[6];
+  for (int k = FIRE_STAGE_COUNT; k < n; ++k) ms[k] = 0.0f;
+  return FIRE_OK;
+}
+
+int fire_sim_residual(FireSim* sim, double* rel, void* stream) {
+  if (!sim || !rel) return FIRE_ERR_BAD_ARG;
+  CK(cudaSetDevice(sim->device));
+  cudaStream_t st = as_stream(stream);
+  launch_residual(sim->levels[0], sim->dPartials, sim->dSmall, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(sim->hSmall, sim->dSmall, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *rel = sim->hSmall[1] > 0 ? std::sqrt(sim->hSmall[0] / sim->hSmall[1]) : 0.0;
+  return FIRE_OK;
+}
+
+int fire_sim_stats(FireSim* sim, int which, double* out16, void* stream) {
+  if (!sim || !out16) return FIRE_ERR_BAD_ARG;
+  float* f = field_ptr4(sim, which);
+  if (!f) return set_err(sim, FIRE_ERR_BAD_ARG, "stats: field %d is not a 4-channel grid field", which);
+  CK(cudaSetDevice(sim->device));
+  cudaStream_t st = as_stream(stream);
+  launch_stats((const float4*)f, sim->d, sim->dPartials, sim->dSmall + 2, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(sim->hSmall + 2, sim->dSmall + 2, 16 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::memcpy(out16, sim->hSmall + 2, 16 * sizeof(double));
+  return FIRE_OK;
+}
+int fire_sim_hrr(FireSim* sim, double* q_kw, void* stream) {
+  if (!sim || !q_kw) return FIRE_ERR_BAD_ARG;
+  CK(cudaSetDevice(sim->device));
+  cudaStream_t st = as_stream(stream);
+  launch_hrr(sim->f.S, sim->d, (float)sim->dx, sim->dPartials, sim->dSmall + 18, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(sim->hSmall + 18, sim->dSmall + 18, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *q_kw = sim->hSmall[18];
+  return FIRE_OK;
+}
+int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream) {
+  if (!sim || !pinned_out17) return FIRE_ERR_BAD_ARG;
+  CK(cudaSetDevice(sim->device));
+  cudaStream_t st = as_stream(stream);
+  launch_stats(sim->f.S, sim->d, sim->dPartials, sim->dSmall + 2, st);
+  launch_hrr(sim->f.S, sim->d, (float)sim->dx, sim->dPartials, sim->dSmall + 18, st);   // reuses the partials after stats
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(pinned_out17, sim->dSmall + 2, 17 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  return FIRE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+// Device helpers for the fire simulation kernels: WGSL builtin semantics, hashing and trilinear sampling.
+//
+// The semantics match the CPU oracle exactly (same expression order):
+//   clamp(x, lo, hi) = fminf(fmaxf(x, lo), hi)   (NaN -> lo)
+//   mix(a, b, t)     = a * (1 - t) + b * t
+//   smoothstep       = t * t * (3 - 2 t), t = clamp((x - e0) / (e1 - e0), 0, 1)
+//   textureSampleLevel(linear) = trilinear in cell units (texel i's centre at i + 0.5), exact weights.
+#pragma once
+#include <cuda_fp16.h>
+#include <cstdint>
+#include "fire_internal.h"
+
+namespace fire {
+
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+__device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+__device__ __forceinline__ float sstep(float e0, float e1, float x) {
+  float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }
+__device__ __forceinline__ f3 xyz(const float4& v) { return mk3(v.x, v.y, v.z); }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float len3(f3 a) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ f3 cross3(f3 a, f3 b) { return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+__device__ __forceinline__ f3 fmin3(f3 a, f3 b) { return mk3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)); }
+__device__ __forceinline__ f3 fmax3(f3 a, f3 b) { return mk3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)); }
+__device__ __forceinline__ float4 fmin4(float4 a, float4 b) { return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), fminf(a.w, b.w)); }
+__device__ __forceinline__ float4 fmax4(float4 a, float4 b) { return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), fmaxf(a.w, b.w)); }
+__device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float4 sub4(float4 a, float4 b) { return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+__device__ __forceinline__ float4 mul4(float4 a, float s) { return make_float4(a.x * s, a.y * s, a.z * s, a.w * s); }
+
+__device__ __forceinline__ size_t cell(int x, int y, int z, int nx, int ny) {
+  return (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * (size_t)z);
+}
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+// textureLoad with clamped coordinates (`ld`, src/sim.js:114)
+__device__ __forceinline__ float4 ldc(const float4* __restrict__ f, int x, int y, int z, Dims d) {
+  x = min(max(x, 0), d.nx - 1); y = min(max(y, 0), d.ny - 1); z = min(max(z, 0), d.nz - 1);
+  return __ldg(f + cell(x, y, z, d.nx, d.ny));
+}
+
+// ---- hashes (src/shaders/lib.js:3-18) ----
+__device__ __forceinline__ uint3 pcg3d(uint3 v) {
+  v.x = v.x * 1664525u + 1013904223u; v.y = v.y * 1664525u + 1013904223u; v.z = v.z * 1664525u + 1013904223u;
+  v.x += v.y * v.z; v.y += v.z * v.x; v.z += v.x * v.y;
+  v.x ^= v.x >> 16; v.y ^= v.y >> 16; v.z ^= v.z >> 16;
+  v.x += v.y * v.z; v.y += v.z * v.x; v.z += v.x * v.y;
+  return v;
+}
+constexpr float kInvU32 = 2.3283064365386963e-10f;   // f32(1 / 4294967295) == 2^-32
+__device__ __forceinline__ f3 hash3f(int x, int y, int z) {
+  uint3 h = pcg3d(make_uint3((unsigned)x, (unsigned)y, (unsigned)z));
+  return mk3(__uint2float_rn(h.x) * kInvU32, __uint2float_rn(h.y) * kInvU32, __uint2float_rn(h.z) * kInvU32);
+}
+
+// ---- trilinear sampling, clamp-to-edge, in cell units ----
+struct Tap {
+  int x0, x1, y0, y1, z0, z1;
+  float fx, fy, fz;
+};
+__device__ __forceinline__ void axis_clamp(float c, int n, int& i0, int& i1, float& f) {
+  float u = clampf(c - 0.5f, -1.0f, (float)n);   // clamping u to [-1, n] does not change a clamp-to-edge sample
+  float fl = floorf(u);
+  int i = (int)fl;
+  f = u - fl;
+  i0 = min(max(i, 0), n - 1);
+  i1 = min(max(i + 1, 0), n - 1);
+}
+__device__ __forceinline__ Tap make_tap(f3 c, Dims d) {
+  Tap t;
+  axis_clamp(c.x, d.nx, t.x0, t.x1, t.fx);
+  axis_clamp(c.y, d.ny, t.y0, t.y1, t.fy);
+  axis_clamp(c.z, d.nz, t.z0, t.z1, t.fz);
+  return t;
+}
+__device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {
+  float s = 1.0f - t;
+  return make_float4(a.x * s + b.x * t, a.y * s + b.y * t, a.z * s + b.z * t, a.w * s + b.w * t);
+}
+__device__ __forceinline__ float4 sample(const float4* __restrict__ f, const Tap& t, Dims d) {
+  const size_t sy = (size_t)d.nx, sz = (size_t)d.nx * d.ny;
+  const size_t r00 = (size_t)t.y0 * sy + (size_t)t.z0 * sz, r10 = (size_t)t.y1 * sy + (size_t)t.z0 * sz;
+  const size_t r01 = (size_t)t.y0 * sy + (size_t)t.z1 * sz, r11 = (size_t)t.y1 * sy + (size_t)t.z1 * sz;
+  float4 c00 = lerp4(__ldg(f + r00 + t.x0), __ldg(f + r00 + t.x1), t.fx);
+  float4 c10 = lerp4(__ldg(f + r10 + t.x0), __ldg(f + r10 + t.x1), t.fx);
+  float4 c01 = lerp4(__ldg(f + r01 + t.x0), __ldg(f + r01 + t.x1), t.fx);
+  float4 c11 = lerp4(__ldg(f + r11 + t.x0), __ldg(f + r11 + t.x1), t.fx);
+  return lerp4(lerp4(c00, c10, t.fy), lerp4(c01, c11, t.fy), t.fz);
+}
+
+// ---- repeat-addressed sampling of a 128^3 half4 table in normalised coordinates ----
+__device__ __forceinline__ float4 h4(uint2 v) {
+  __half2 a = *reinterpret_cast<__half2*>(&v.x);
+  __half2 b = *reinterpret_cast<__half2*>(&v.y);
+  float2 fa = __half22float2(a), fb = __half22float2(b);
+  return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+__device__ __forceinline__ int wrapN(long long i) { long long m = i % TABLE_N; return (int)(m < 0 ? m + TABLE_N : m); }
+__device__ __forceinline__ float4 sample_table(const uint2* __restrict__ tab, f3 q) {
+  const float N = (float)TABLE_N;
+  float ux = q.x * N - 0.5f, uy = q.y * N - 0.5f, uz = q.z * N - 0.5f;
+  float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
+  float fx = ux - flx, fy = uy - fly, fz = uz - flz;
+  long long ix = (long long)flx, iy = (long long)fly, iz = (long long)flz;
+  int x0 = wrapN(ix), x1 = wrapN(ix + 1), y0 = wrapN(iy), y1 = wrapN(iy + 1), z0 = wrapN(iz), z1 = wrapN(iz + 1);
+  auto T = [&](int x, int y, int z) { return h4(__ldg(tab + x + TABLE_N * (y + TABLE_N * z))); };
+  float4 c00 = lerp4(T(x0, y0, z0), T(x1, y0, z0), fx);
+  float4 c10 = lerp4(T(x0, y1, z0), T(x1, y1, z0), fx);
+  float4 c01 = lerp4(T(x0, y0, z1), T(x1, y0, z1), fx);
+  float4 c11 = lerp4(T(x0, y1, z1), T(x1, y1, z1), fx);
+  return lerp4(lerp4(c00, c10, fy), lerp4(c01, c11, fy), fz);
+}
+
+}  // namespace fire

@@ -1,0 +1,84 @@
+// Internal declarations shared by the host runtime and the CUDA kernels of the fire simulation step.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fire {
+
+// SIM_FIELDS order (src/sim.js:14-23): the index of every scalar in the 64-float parameter block.
+enum ParamIndex {
+  P_nx, P_ny, P_nz, P_dx, P_dt, P_time, P_frame, P_seed, P_ox, P_oy, P_oz, P_nLogs,
+  P_fuelSrc, P_bedFuel, P_srcTemp, P_bedTemp, P_srcVel, P_srcFreq, P_srcSpeed, P_srcThresh,
+  P_ignT, P_kMix, P_rs, P_heatOut, P_expansion, P_sootForm, P_sootOx, P_radCool,
+  P_coolRate, P_sootDissip, P_smokeDissip, P_vitDecay, P_fuelDissip, P_buoyancy, P_vortEps, P_turbAmp,
+  P_turbFreq, P_turbRise, P_turbEvolve, P_windX, P_windZ, P_gust, P_intensity, P_velDissip,
+  P_bedRadius, P_logSrc, P_burstX, P_burstY, P_burstZ, P_burstAmt, P_smolder, P_sponge, P_hotR0, P_hotR1, P_hotY1,
+  P_visc, P_lamAge, P_anchorFreq, P_srcFloor, P_anchorGain, P_COUNT
+};
+static_assert(P_COUNT == 60, "SIM_FIELDS has 60 entries");
+constexpr int P_STRIDE = 64;
+
+// Extension block appended after the 64-float parameter block (no counterpart in the reference).
+enum ExtIndex { E_sootAge0 = 0, E_sootAge1, E_bedGain, E_nSpots, E_spotRef, E_SPOTS = 8 };
+constexpr int MAX_SPOTS = 16;
+constexpr int SPOT_STRIDE = 8;
+constexpr int E_COUNT = E_SPOTS + MAX_SPOTS * SPOT_STRIDE;   // 136
+constexpr int BLOCK_FLOATS = P_STRIDE + E_COUNT;            // 200 floats uploaded per step
+
+constexpr int TABLE_N = 128;          // noise / curl tables: 128^3 (src/main.js:36-37)
+constexpr int MAX_LOGS = 16;          // packLogs max (src/scene.js:92)
+
+extern const char* const kParamNames[P_COUNT];
+extern const float kParamDefaults[P_STRIDE];
+
+// Device view of the simulation buffers.  All rgba fields are float4, x fastest.
+struct Fields {
+  float4* vel; float4* velX; float4* velY;
+  float4* S; float4* SX; float4* SY;
+  float4* S2; float4* S2X; float4* S2Y;
+  float4* vort; float4* geo;
+};
+struct Dims { int nx, ny, nz; };
+
+struct MGLevel {
+  int nx, ny, nz;
+  float h;
+  float* p;
+  float* b;
+};
+
+// ---- kernel launchers (fire_tables.cu) ----
+void launch_noise_table(uint2* noise, int N, int seed, cudaStream_t st);
+void launch_curl_table(const uint2* noise, uint2* curl, int N, cudaStream_t st);
+void launch_geo(const float* P, const float* logs, float4* geo, Dims d, cudaStream_t st);
+
+// ---- kernel launchers (fire_step.cu) ----
+void launch_adv1(const float* P, Fields f, Dims d, cudaStream_t st);
+void launch_adv2(const float* P, Fields f, Dims d, cudaStream_t st);
+void launch_curl(Fields f, Dims d, cudaStream_t st);
+void launch_forces(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
+void launch_forces_unfused(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
+void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st);
+void launch_project(const float* P, Fields f, const float* p0, Dims d, cudaStream_t st);
+
+// ---- kernel launchers (fire_mg.cu) ----
+void launch_smooth(const MGLevel& L, int color, cudaStream_t st);
+void launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st);
+void launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st);
+// Single-CTA V-cycle over levels [first, n): all level arrays staged in shared memory.
+size_t tail_smem_bytes(const MGLevel* levels, int first, int n);
+void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, cudaStream_t st);
+// Opts the tail kernel into `max_tail_smem` bytes of dynamic shared memory on the current device.
+cudaError_t mg_configure(size_t max_tail_smem);
+constexpr size_t TAIL_SMEM_BUDGET = 200 * 1024;
+// Residual / RHS sums of squares on a level: partial sums per CTA then a fixed-order final sum.
+int residual_partials_count(const MGLevel& L);
+void launch_residual(const MGLevel& L, double* partials, double* out2, cudaStream_t st);
+
+// ---- diagnostics (fire_stats.cu) ----
+int stats_partials_count(Dims d);
+void launch_stats(const float4* f, Dims d, double* partials, double* out16, cudaStream_t st);
+void launch_hrr(const float4* S, Dims d, float dx, double* partials, double* out1, cudaStream_t st);
+
+}  // namespace fire

@@ -1,0 +1,384 @@
+// Per-step stencil kernels of the fire simulation: MacCormack advection, curl + forces (fused),
+// divergence and projection.  Each kernel restates one WGSL compute shader of src/sim.js; the line
+// ranges are given per kernel.  One thread per cell; CTAs cover 32 x 4 x 2 bricks so the gathers of
+// the semi-Lagrangian back-trace and the 7-point stencils hit L1.  Fields are dense float4 arrays,
+// x fastest, so every warp reads and writes 512 contiguous bytes per field.
+#include "fire_device.cuh"
+
+namespace fire {
+
+constexpr int BX = 32, BY = 4, BZ = 2;
+
+struct CellId { int i, j, k; bool ok; };
+__device__ __forceinline__ CellId cell_id(Dims d) {
+  CellId c;
+  c.i = blockIdx.x * BX + threadIdx.x;
+  c.j = blockIdx.y * BY + threadIdx.y;
+  c.k = blockIdx.z * BZ + threadIdx.z;
+  c.ok = c.i < d.nx && c.j < d.ny && c.k < d.nz;
+  return c;
+}
+static dim3 grid_for(Dims d) { return dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, (d.nz + BZ - 1) / BZ); }
+static dim3 block_shape() { return dim3(BX, BY, BZ); }
+
+// Scalars entering from outside the domain are ambient (src/sim.js:137-140)
+__device__ __forceinline__ float outside_fade(f3 c, Dims d) {
+  float lo = fminf(c.x, c.z);
+  float hi = fmaxf(c.x - (float)d.nx, fmaxf(c.y - (float)d.ny, c.z - (float)d.nz));
+  return clampf(1.0f - fmaxf(-lo, hi), 0.0f, 1.0f);
+}
+// RK2 midpoint back-trace in cells (src/sim.js:129-135).  The first velocity sample sits exactly on the
+// cell centre, where the trilinear weights are (1, 0) on every axis, so it equals the cell's own value.
+__device__ __forceinline__ f3 backtrace(const float4* __restrict__ vel, f3 c, f3 v0, float dt, float dx, Dims d) {
+  f3 mid = c - v0 * (0.5f * dt) / dx;
+  f3 v1 = xyz(sample(vel, make_tap(mid, d), d));
+  return c - v1 * dt / dx;
+}
+
+// ---------------- adv1 (src/sim.js:142-157) ----------------
+__global__ void __launch_bounds__(256) k_adv1(const float* __restrict__ P, Fields f, Dims d) {
+  CellId id = cell_id(d);
+  if (!id.ok) return;
+  const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx);
+  const size_t ci = cell(id.i, id.j, id.k, d.nx, d.ny);
+  f3 c = mk3((float)id.i + 0.5f, (float)id.j + 0.5f, (float)id.k + 0.5f);
+  f3 b = backtrace(f.vel, c, xyz(__ldg(f.vel + ci)), dt, dx, d);
+  float fade = outside_fade(b, d);
+  float ws = sstep(0.03f, 0.4f, b.y * dx);
+  f3 wind = mk3(__ldg(P + P_windX) * ws, 0.0f * ws, __ldg(P + P_windZ) * ws);
+  Tap t = make_tap(b, d);
+  f3 sv = xyz(sample(f.vel, t, d));
+  f.velX[ci] = make_float4(mixf(wind.x, sv.x, fade), mixf(wind.y, sv.y, fade), mixf(wind.z, sv.z, fade), 0.0f);
+  f.SX[ci] = mul4(sample(f.S, t, d), fade);
+  f.S2X[ci] = mul4(sample(f.S2, t, d), fade);
+}
+
+// ---------------- adv2 (src/sim.js:159-197) ----------------
+__global__ void __launch_bounds__(256) k_adv2(const float* __restrict__ P, Fields f, Dims d) {
+  CellId id = cell_id(d);
+  if (!id.ok) return;
+  const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx);
+  const size_t ci = cell(id.i, id.j, id.k, d.nx, d.ny);
+  f3 c = mk3((float)id.i + 0.5f, (float)id.j + 0.5f, (float)id.k + 0.5f);
+  f3 v = xyz(__ldg(f.vel + ci));
+  // reverse advection of the forward result
+  f3 fw = c + v * dt / dx;
+  f3 vH = xyz(__ldg(f.velX + ci));
+  float4 sH = __ldg(f.SX + ci);
+  float4 s2H = __ldg(f.S2X + ci);
+  Tap tf = make_tap(fw, d);
+  f3 vN = vH + (v - xyz(sample(f.velX, tf, d))) * 0.5f;
+  float4 sN = add4(sH, mul4(sub4(__ldg(f.S + ci), sample(f.SX, tf, d)), 0.5f));
+  float4 s2N = add4(s2H, mul4(sub4(__ldg(f.S2 + ci), sample(f.S2X, tf, d)), 0.5f));
+  // clamp to the range of the source stencil at the back-traced point (Selle et al. 2008)
+  f3 bt = backtrace(f.vel, c, v, dt, dx, d);
+  f3 b = mk3(bt.x - 0.5f, bt.y - 0.5f, bt.z - 0.5f);
+  int b0x = (int)floorf(clampf(b.x, -2.0f, (float)(d.nx + 1)));
+  int b0y = (int)floorf(clampf(b.y, -2.0f, (float)(d.ny + 1)));
+  int b0z = (int)floorf(clampf(b.z, -2.0f, (float)(d.nz + 1)));
+  f3 vmn = mk3(1e9f, 1e9f, 1e9f), vmx = mk3(-1e9f, -1e9f, -1e9f);
+  float4 smn = make_float4(1e9f, 1e9f, 1e9f, 1e9f), smx = make_float4(-1e9f, -1e9f, -1e9f, -1e9f);
+  float4 tmn = smn, tmx = smx;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    int qx = b0x + (q & 1), qy = b0y + ((q >> 1) & 1), qz = b0z + ((q >> 2) & 1);
+    f3 vv = xyz(ldc(f.vel, qx, qy, qz, d));
+    float4 ss = ldc(f.S, qx, qy, qz, d);
+    float4 tt = ldc(f.S2, qx, qy, qz, d);
+    vmn = fmin3(vmn, vv); vmx = fmax3(vmx, vv);
+    smn = fmin4(smn, ss); smx = fmax4(smx, ss);
+    tmn = fmin4(tmn, tt); tmx = fmax4(tmx, tt);
+  }
+  if (outside_fade(mk3(b.x + 0.5f, b.y + 0.5f, b.z + 0.5f), d) < 1.0f) { vN = vH; sN = sH; s2N = s2H; }
+  vN = fmin3(fmax3(vN, fmin3(vmn, vH)), fmax3(vmx, vH));
+  sN = fmin4(fmax4(sN, fmin4(smn, sH)), fmax4(smx, sH));
+  s2N = fmin4(fmax4(s2N, fmin4(tmn, s2H)), fmax4(tmx, s2H));
+  const float4 z0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  f.velY[ci] = make_float4(vN.x, vN.y, vN.z, 0.0f);
+  f.SY[ci] = fmax4(sN, z0);
+  f.S2Y[ci] = fmax4(s2N, z0);
+}
+
+// ---------------- curl (src/sim.js:200-211) ----------------
+// Vorticity at cell (x, y, z) (already inside the domain), from clamped velY neighbours.
+__device__ __forceinline__ float4 curl_at(const float4* __restrict__ v, int x, int y, int z, Dims d) {
+  f3 L = xyz(ldc(v, x - 1, y, z, d)), R = xyz(ldc(v, x + 1, y, z, d));
+  f3 B = xyz(ldc(v, x, y - 1, z, d)), T = xyz(ldc(v, x, y + 1, z, d));
+  f3 K = xyz(ldc(v, x, y, z - 1, d)), F = xyz(ldc(v, x, y, z + 1, d));
+  f3 w = mk3((T.z - B.z) - (F.y - K.y), (F.x - K.x) - (R.z - L.z), (R.y - L.y) - (T.x - B.x)) * 0.5f;
+  return make_float4(w.x, w.y, w.z, len3(w));
+}
+__global__ void __launch_bounds__(256) k_curl(Fields f, Dims d) {
+  CellId id = cell_id(d);
+  if (!id.ok) return;
+  f.vort[cell(id.i, id.j, id.k, d.nx, d.ny)] = curl_at(f.velY, id.i, id.j, id.k, d);
+}
+
+// ---------------- forces (src/sim.js:214-396), with the curl recomputed in place ----------------
+// The reference runs a separate curl dispatch into a vorticity texture and reads 7 taps of it here.
+// This kernel computes those 7 vorticity values from velY directly (the taps are clamped to the
+// domain exactly as `ld` clamps them), so the vorticity field never round-trips through HBM.
+__device__ __forceinline__ float4 noise4(const uint2* __restrict__ tab, f3 q) {    // src/sim.js:228
+  float4 t = sample_table(tab, q);
+  return make_float4(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f, t.w * 2.0f - 1.0f);
+}
+template <bool kFusedCurl>
+__global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fields f, const uint2* __restrict__ noiseT,
+                                                const uint2* __restrict__ curlT, Dims d) {
+  CellId id = cell_id(d);
+  if (!id.ok) return;
+  const int i = id.i, j = id.j, k = id.k;
+  const size_t ci = cell(i, j, k, d.nx, d.ny);
+  const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx), I = __ldg(P + P_intensity);
+  const float seed = __ldg(P + P_seed), time = __ldg(P + P_time);
+  const float* E = P + P_STRIDE;
+  f3 p = mk3(__ldg(P + P_ox), __ldg(P + P_oy), __ldg(P + P_oz)) + mk3((float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f) * dx;
+  float4 v4 = __ldg(f.velY + ci);
+  f3 v = xyz(v4);
+  float4 s = __ldg(f.SY + ci);
+  float4 s2 = __ldg(f.S2Y + ci);
+  float4 geo = __ldg(f.geo + ci);
+
+  // ---- sources: pyrolysis on the hot log surfaces + the coal bed (src/sim.js:246-284)
+  float src = 0.0f, anchor = 0.0f;
+  if (geo.x > 0.001f) {
+    f3 qa = p * __ldg(P + P_anchorFreq) + mk3(seed * 0.37f, 0.0f, 0.11f);
+    anchor = sstep(-0.05f, 0.25f, noise4(noiseT, qa).z);
+    f3 qn = p * (__ldg(P + P_srcFreq) * 0.06f) + mk3(seed * 0.131f, 0.0f, time * __ldg(P + P_srcSpeed));
+    const float th = __ldg(P + P_srcThresh);
+    float pulse = sstep(th - 0.25f, th + 0.25f, noise4(noiseT, qn).x);
+    src = clampf(geo.x * __ldg(P + P_logSrc) * (__ldg(P + P_srcFloor) + __ldg(P + P_anchorGain) * anchor) * mixf(0.55f, 1.0f, pulse) * 1.2f,
+                 0.0f, 1.0f) * I;
+    src *= 1.0f - geo.z;
+  }
+  // Gaussian pyrolysis spots (build-defined extension; none by default)
+  const int nSpots = (int)__ldg(E + E_nSpots);
+  if (nSpots > 0) {
+    const float spotRef = __ldg(E + E_spotRef);
+    float acc = 0.0f;
+    for (int q = 0; q < nSpots; ++q) {
+      const float* sp = E + E_SPOTS + SPOT_STRIDE * q;
+      f3 dd = p - mk3(__ldg(sp + 0), __ldg(sp + 1), __ldg(sp + 2));
+      float sg = __ldg(sp + 3);
+      float d2 = dot3(dd, dd);
+      if (d2 < 16.0f * sg * sg) acc += (__ldg(sp + 4) / spotRef) * expf(-d2 / (2.0f * sg * sg));
+    }
+    src = fmaxf(src, clampf(acc, 0.0f, 1.0f) * I);
+  }
+  const float srcW = fminf(src, 1.0f);
+  const float bedHot = geo.y;
+  float bed = geo.y * clampf(I * 1.4f, 0.3f, 1.0f);
+  if (bed > 0.001f) {
+    f3 qb = p * 2.4f + mk3(0.17f, -time * 0.12f, time * 0.05f);
+    bed *= sstep(0.0f, 0.3f, noise4(noiseT, qb).y);
+  }
+  s.y = fmaxf(s.y, src * __ldg(P + P_fuelSrc));
+  s.y = fmaxf(s.y, bed * __ldg(P + P_bedFuel));
+  s.x = fmaxf(s.x, src * __ldg(P + P_srcTemp));
+  s.x = fmaxf(s.x, bedHot * __ldg(P + P_bedTemp));
+  const float srcAll = fmaxf(srcW, bed);
+  s2.w = mixf(s2.w, 1.0f, bed * (1.0f - srcW));
+  s2.w = mixf(s2.w, 0.0f, srcW);
+  s2.y = s2.y * (1.0f - srcAll);
+  s2.x = fmaxf(s2.x, (1.0f - s.y) * srcW);
+  s2.x = fmaxf(s2.x, (1.0f - s.y) * bed * 0.6f);
+  float wsrc = 1.0f - powf(1.0f - clampf(srcW + bed * 0.4f, 0.0f, 1.0f) * 0.5f, dt * 90.0f);
+  v.y = mixf(v.y, fmaxf(v.y, __ldg(P + P_srcVel)), wsrc);
+  s2.z += geo.x * (1.0f - anchor) * __ldg(P + P_smolder) * dt * I;
+
+  // ---- burst (src/sim.js:288-296)
+  const float burstAmt = __ldg(P + P_burstAmt);
+  if (burstAmt > 0.0f) {
+    float bd = len3(p - mk3(__ldg(P + P_burstX), __ldg(P + P_burstY), __ldg(P + P_burstZ)));
+    float bw = clampf(expf(-bd * bd / 0.006f) * burstAmt, 0.0f, 1.0f);
+    s.y = fmaxf(s.y, 0.17f * bw);
+    s.x = fmaxf(s.x, 0.9f * bw);
+    s2.x *= 1.0f - bw;
+    s2.w *= 1.0f - bw;
+    s2.y = fmaxf(s2.y, 0.05f * bw * clampf(s.y + s2.x, 0.0f, 1.0f));
+  }
+  float ageF = s2.y / fmaxf(s.y + s2.x, 1e-4f);
+
+  // ---- mixing-limited combustion (src/sim.js:299-309)
+  const float T0 = 293.0f + 1000.0f * s.x;
+  const float o = clampf(1.0f - s.y - s2.x, 0.0f, 1.0f);
+  const float ignT = __ldg(P + P_ignT), rs = __ldg(P + P_rs);
+  const float ign = sstep(ignT - 50.0f, ignT + 50.0f, T0);
+  const float b = fminf(s.y, o / rs) * (1.0f - expf(-__ldg(P + P_kMix) * ign * dt));
+  s.y -= b;
+  s2.x = fminf(s2.x + (1.0f + rs) * b, 1.0f);
+  const float dT = fminf(__ldg(P + P_heatOut) * b, fmaxf(2100.0f - T0, 0.0f));
+  float T = T0 + dT;
+  const float q = dT / dt;
+  const float phi = geo.z > 0.5f ? 0.0f : fminf(__ldg(P + P_expansion) * q / T, 60.0f);
+
+  // ---- soot (src/sim.js:312-318); the age gate bounds come from the extension block
+  const float sootOx = __ldg(P + P_sootOx);
+  ageF = fminf(ageF + dt, 4.0f);
+  s.z += __ldg(P + P_sootForm) * b * sstep(__ldg(E + E_sootAge0), __ldg(E + E_sootAge1), ageF) * sstep(1000.0f, 1400.0f, T) * (1.0f - s2.w);
+  s.z *= expf(-sootOx * (0.25f + o) * sstep(1100.0f, 1400.0f, T) * dt);
+  s.z *= expf(-sootOx * 0.5f * o * sstep(850.0f, 1100.0f, T) * (1.0f - sstep(1100.0f, 1300.0f, T)) * dt);
+  s.z *= expf(-__ldg(P + P_sootDissip) * dt);
+
+  // ---- cooling (src/sim.js:321-330)
+  const float th = T * 0.001f;
+  T -= fminf(__ldg(P + P_radCool) * 970.0f * s.z * th * th * (th * th * th * th - 0.00737f), 6000.0f) * dt;
+  const float notBurning = 1.0f - sstep(500.0f, 5000.0f, q);
+  T = 293.0f + fmaxf(T - 293.0f, 0.0f) * expf(-__ldg(P + P_coolRate) * notBurning * dt);
+  s.x = (T - 293.0f) * 0.001f;
+  s.w = q * 1e-4f;
+  s.y *= expf(-__ldg(P + P_fuelDissip) * dt);
+  s2.x *= expf(-__ldg(P + P_vitDecay) * dt);
+  s2.z *= expf(-__ldg(P + P_smokeDissip) * dt);
+  s2.y = ageF * clampf(s.y + s2.x, 0.0f, 1.0f);
+
+  // ---- buoyancy (src/sim.js:333)
+  v.y += __ldg(P + P_buoyancy) * s.x * dt;
+
+  // ---- hot-gas viscosity (src/sim.js:339-346)
+  const float visc = __ldg(P + P_visc);
+  if (visc > 0.0f) {
+    f3 lapV = xyz(ldc(f.velY, i + 1, j, k, d)) + xyz(ldc(f.velY, i - 1, j, k, d));
+    lapV = lapV + xyz(ldc(f.velY, i, j + 1, k, d));
+    lapV = lapV + xyz(ldc(f.velY, i, j - 1, k, d));
+    lapV = lapV + xyz(ldc(f.velY, i, j, k + 1, d));
+    lapV = lapV + xyz(ldc(f.velY, i, j, k - 1, d));
+    lapV = lapV - xyz(v4) * 6.0f;
+    float nu = visc * 1.5e-5f * powf(fmaxf(T, 293.0f) / 293.0f, 1.7f);
+    v = v + lapV * fminf(nu * dt / (dx * dx), 0.15f);
+  }
+  // ---- laminar flame base (src/sim.js:350)
+  const float lamAge = __ldg(P + P_lamAge);
+  const float lam = lamAge > 0.0f ? sstep(0.5f * lamAge, fmaxf(lamAge, 1e-3f), ageF) : 1.0f;
+
+  // ---- vorticity confinement (src/sim.js:353-361)
+  float4 wc;
+  f3 g;
+  if (kFusedCurl) {
+    wc = curl_at(f.velY, i, j, k, d);
+    g = mk3(curl_at(f.velY, min(i + 1, d.nx - 1), j, k, d).w - curl_at(f.velY, max(i - 1, 0), j, k, d).w,
+            curl_at(f.velY, i, min(j + 1, d.ny - 1), k, d).w - curl_at(f.velY, i, max(j - 1, 0), k, d).w,
+            curl_at(f.velY, i, j, min(k + 1, d.nz - 1), d).w - curl_at(f.velY, i, j, max(k - 1, 0), d).w);
+  } else {
+    wc = __ldg(f.vort + ci);
+    g = mk3(ldc(f.vort, i + 1, j, k, d).w - ldc(f.vort, i - 1, j, k, d).w,
+            ldc(f.vort, i, j + 1, k, d).w - ldc(f.vort, i, j - 1, k, d).w,
+            ldc(f.vort, i, j, k + 1, d).w - ldc(f.vort, i, j, k - 1, d).w);
+  }
+  const float gl = len3(g);
+  if (gl > 1e-6f) {
+    float gate = sstep(450.0f, 900.0f, T) * (1.0f - srcAll) * sstep(0.02f, 0.08f, p.y) * lam;
+    v = v + cross3(g / gl, xyz(wc)) * (__ldg(P + P_vortEps) * gate) * dt;
+  }
+
+  // ---- sub-grid turbulence: rising, evolving curl noise (src/sim.js:364-368)
+  f3 tq = (p - mk3(0.0f, time * __ldg(P + P_turbRise), 0.0f)) * __ldg(P + P_turbFreq) + mk3(0.0f, 0.0f, time * __ldg(P + P_turbEvolve));
+  f3 cn = xyz(sample_table(curlT, tq));
+  float tgate = fmaxf(sstep(500.0f, 1100.0f, T), sstep(0.0f, 3.0f, s.w)) * (1.0f - srcAll) *
+                mixf(0.6f, 1.8f, sstep(0.2f, 0.75f, p.y)) * lam;
+  v = v + cn * (__ldg(P + P_turbAmp) / 12.0f) * tgate * dt * 10.0f;
+
+  // ---- wind above the logs (src/sim.js:372-375)
+  const float windX = __ldg(P + P_windX), windZ = __ldg(P + P_windZ);
+  const float windK = sstep(0.05f, 0.5f, p.y) * (1.0f + __ldg(P + P_gust));
+  v.x += (windX * windK - v.x) * dt * 0.35f * windK;
+  v.z += (windZ * windK - v.z) * dt * 0.35f * windK;
+  v = v * expf(-__ldg(P + P_velDissip) * dt);
+
+  // ---- solids & sponge layers (src/sim.js:378-388)
+  if (geo.z > 0.5f) { v = mk3(0.0f, 0.0f, 0.0f); s.y = 0.0f; s2.y = 0.0f; }
+  f3 fp = mk3((float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f);
+  float side = fminf(fminf(fp.x, (float)d.nx - fp.x), fminf(fp.z, (float)d.nz - fp.z));
+  float sp = (1.0f - sstep(0.0f, 5.0f, side)) * __ldg(P + P_sponge);
+  float wsy = sstep(0.03f, 0.4f, p.y);
+  float wSx = windX * wsy, wSz = windZ * wsy;
+  float ks = 1.0f - powf(1.0f - 0.15f * clampf(sp, 0.0f, 1.0f), dt * 90.0f);
+  v.x = mixf(v.x, wSx, ks);
+  v.z = mixf(v.z, wSz, ks);
+  float top = sstep((float)d.ny - 10.0f, (float)d.ny, fp.y);
+  float kt = powf(1.0f - 0.1f * top, dt * 90.0f);
+  s.z *= kt;
+  s2.z *= kt;
+
+  float vl = len3(v);
+  if (vl > 15.0f) v = v * (15.0f / vl);
+  bool bad = isnan(s.x) || isnan(s.y) || isnan(s.z) || isnan(s.w) || isnan(s2.x) || isnan(s2.y) || isnan(s2.z) ||
+             isnan(s2.w) || isnan(v.x) || isnan(v.y) || isnan(v.z);
+  if (bad) {
+    s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    s2 = s;
+    v = mk3(0.0f, 0.0f, 0.0f);
+  }
+  f.velX[ci] = make_float4(v.x, v.y, v.z, phi);
+  f.S[ci] = s;
+  f.S2[ci] = s2;
+}
+
+// ---------------- divergence minus the expansion target (src/sim.js:399-413) ----------------
+__global__ void __launch_bounds__(256) k_div(const float* __restrict__ P, const float4* __restrict__ velX,
+                                             float* __restrict__ b0, Dims d) {
+  CellId id = cell_id(d);
+  if (!id.ok) return;
+  const int i = id.i, j = id.j, k = id.k;
+  const size_t ci = cell(i, j, k, d.nx, d.ny);
+  const float dx = __ldg(P + P_dx);
+  float4 me = __ldg(velX + ci);
+  float L = ldc(velX, i - 1, j, k, d).x, R = ldc(velX, i + 1, j, k, d).x;
+  float B = ldc(velX, i, j - 1, k, d).y, T = ldc(velX, i, j + 1, k, d).y;
+  float K = ldc(velX, i, j, k - 1, d).z, F = ldc(velX, i, j, k + 1, d).z;
+  if (j == 0) B = -me.y;   // solid floor
+  b0[ci] = ((R - L) + (T - B) + (F - K)) / (2.0f * dx) - me.w;
+}
+
+// ---------------- projection (src/sim.js:526-550) ----------------
+__device__ __forceinline__ float pr(const float* __restrict__ p, int x, int y, int z, Dims d, float me) {
+  if (x < 0 || z < 0 || x >= d.nx || z >= d.nz || y >= d.ny) return -me;   // open sides/top: p = 0 on the face
+  if (y < 0) return me;                                                    // floor: Neumann
+  return __ldg(p + cell(x, y, z, d.nx, d.ny));
+}
+__global__ void __launch_bounds__(256) k_project(const float* __restrict__ P, const float4* __restrict__ velX,
+                                                 const float* __restrict__ p0, const float4* __restrict__ geo,
+                                                 float4* __restrict__ vel, Dims d) {
+  CellId id = cell_id(d);
+  if (!id.ok) return;
+  const int i = id.i, j = id.j, k = id.k;
+  const size_t ci = cell(i, j, k, d.nx, d.ny);
+  const float dx = __ldg(P + P_dx);
+  float me = __ldg(p0 + ci);
+  f3 g = mk3(pr(p0, i + 1, j, k, d, me) - pr(p0, i - 1, j, k, d, me),
+             pr(p0, i, j + 1, k, d, me) - pr(p0, i, j - 1, k, d, me),
+             pr(p0, i, j, k + 1, d, me) - pr(p0, i, j, k - 1, d, me)) / (2.0f * dx);
+  f3 v = xyz(__ldg(velX + ci)) - g;
+  if (__ldg(&geo[ci].z) > 0.5f) v = mk3(0.0f, 0.0f, 0.0f);
+  if (j == 0) v.y = fmaxf(v.y, 0.0f);
+  float vl = len3(v);
+  if (vl > 20.0f || isnan(vl)) v = isnan(vl) ? mk3(0.0f, 0.0f, 0.0f) : v * 20.0f / vl;
+  vel[ci] = make_float4(v.x, v.y, v.z, 0.0f);
+}
+
+// ---------------- launchers ----------------
+void launch_adv1(const float* P, Fields f, Dims d, cudaStream_t st) { k_adv1<<<grid_for(d), block_shape(), 0, st>>>(P, f, d); }
+void launch_adv2(const float* P, Fields f, Dims d, cudaStream_t st) { k_adv2<<<grid_for(d), block_shape(), 0, st>>>(P, f, d); }
+void launch_curl(Fields f, Dims d, cudaStream_t st) { k_curl<<<grid_for(d), block_shape(), 0, st>>>(f, d); }
+void launch_forces(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
+  k_forces<true><<<grid_for(d), block_shape(), 0, st>>>(P, f, noise, curl, d);
+}
+void launch_forces_unfused(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
+  k_forces<false><<<grid_for(d), block_shape(), 0, st>>>(P, f, noise, curl, d);
+}
+void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st) {
+  k_div<<<grid_for(d), block_shape(), 0, st>>>(P, f.velX, b0, d);
+}
+void launch_project(const float* P, Fields f, const float* p0, Dims d, cudaStream_t st) {
+  k_project<<<grid_for(d), block_shape(), 0, st>>>(P, f.velX, p0, f.geo, f.vel, d);
+}
+
+}  // namespace fire
+
+namespace fire {
+// Verifies that this library carries a kernel image for the current device.
+cudaError_t kernels_probe() {
+  cudaFuncAttributes a;
+  return cudaFuncGetAttributes(&a, k_div);
+}
+}  // namespace fire

@@ -1,0 +1,382 @@
+"""Python host mirror of the reference's FireSim (src/sim.js) over the C ABI in include/fire_sim.h.
+
+The reference drives its simulation from JavaScript: ``new FireSim(device, {res, size, logs, vcycles})``,
+``sim.step(enc, dt)``, ``sim.setParams({...})``, ``sim.reset()``, and the page API's events and
+diagnostics (src/main.js ``window.FIRE``).  This module exposes the same surface with the same names,
+argument meanings and error behaviour, backed by the CUDA sm_103a library ``libfiresim.so``.
+
+There is no CPU fallback: constructing a FireSim without the built library or without a GB300-class
+device raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+from typing import Dict, Iterable, Optional, Sequence
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libfiresim.so"
+
+# SIM_FIELDS (src/sim.js:14-23)
+SIM_FIELDS = [
+    "nx", "ny", "nz", "dx", "dt", "time", "frame", "seed",
+    "ox", "oy", "oz", "nLogs",
+    "fuelSrc", "bedFuel", "srcTemp", "bedTemp", "srcVel", "srcFreq", "srcSpeed", "srcThresh",
+    "ignT", "kMix", "rs", "heatOut", "expansion", "sootForm", "sootOx", "radCool",
+    "coolRate", "sootDissip", "smokeDissip", "vitDecay", "fuelDissip", "buoyancy", "vortEps", "turbAmp",
+    "turbFreq", "turbRise", "turbEvolve", "windX", "windZ", "gust", "intensity", "velDissip",
+    "bedRadius", "logSrc", "burstX", "burstY", "burstZ", "burstAmt", "smolder", "sponge", "hotR0", "hotR1", "hotY1",
+    "visc", "lamAge", "anchorFreq", "srcFloor", "anchorGain",
+]
+# Fields (src/sim.js:71-76 texture names; p/b = multigrid level 0)
+FIELDS = {"vel": 0, "velX": 1, "velY": 2, "S": 3, "SX": 4, "SY": 5, "S2": 6, "S2X": 7, "S2Y": 8,
+          "vort": 9, "geo": 10, "p": 11, "b": 12, "noise": 13, "curl": 14}
+STAGES = {"geo": 0, "adv1": 1, "adv2": 2, "curl": 3, "forces": 4, "div": 5, "vcycle": 6, "project": 7}
+ERRORS = {1: "bad argument", 2: "unknown parameter", 3: "CUDA error", 4: "no sm_103 device", 5: "out of memory",
+          6: "bad state"}
+
+
+class FireError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+class FireConfig(ctypes.Structure):
+    _fields_ = [("res", ctypes.c_int * 3), ("size", ctypes.c_float * 3), ("vcycles", ctypes.c_int),
+                ("device", ctypes.c_int), ("noise_seed", ctypes.c_int), ("mg_max_cycles", ctypes.c_int),
+                ("mg_tol", ctypes.c_double)]
+
+
+class FireFieldDesc(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("dims", ctypes.c_int * 3), ("channels", ctypes.c_int),
+                ("elem_bytes", ctypes.c_int), ("strides", ctypes.c_size_t * 3), ("bytes", ctypes.c_size_t)]
+
+
+class FireInfo(ctypes.Structure):
+    _fields_ = [("res", ctypes.c_int * 3), ("size", ctypes.c_float * 3), ("dx", ctypes.c_float),
+                ("origin", ctypes.c_float * 3), ("time", ctypes.c_double), ("frame", ctypes.c_longlong),
+                ("n_levels", ctypes.c_int), ("coarse_iters", ctypes.c_int), ("vcycles", ctypes.c_int),
+                ("last_cycles", ctypes.c_int), ("last_rel_residual", ctypes.c_double),
+                ("total_cycles", ctypes.c_longlong)]
+
+
+# Every exported entry point and its ctypes signature (mirrors include/fire_sim.h).
+_vp, _ip, _fp, _dp, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_size_t
+_SIGS = {
+    "fire_sim_create": (_ip, [ctypes.POINTER(FireConfig), _vp, _ip, ctypes.POINTER(_vp)]),
+    "fire_sim_destroy": (_ip, [_vp]),
+    "fire_sim_step": (_ip, [_vp, _fp, _ip, _vp]),
+    "fire_sim_sync": (_ip, [_vp]),
+    "fire_sim_set_params": (_ip, [_vp, ctypes.POINTER(ctypes.c_char_p), _vp, _ip]),
+    "fire_sim_get_param": (_ip, [_vp, ctypes.c_char_p, ctypes.POINTER(_fp)]),
+    "fire_sim_set_param_block": (_ip, [_vp, _vp]),
+    "fire_sim_get_param_block": (_ip, [_vp, _vp]),
+    "fire_sim_peek_block": (_ip, [_vp, _fp, _vp]),
+    "fire_param_index": (_ip, [ctypes.c_char_p]),
+    "fire_param_name": (ctypes.c_char_p, [_ip]),
+    "fire_param_defaults": (_ip, [_vp]),
+    "fire_sim_set_soot_age": (_ip, [_vp, _fp, _fp]),
+    "fire_sim_set_bed_gain": (_ip, [_vp, _fp]),
+    "fire_sim_set_spots": (_ip, [_vp, _vp, _ip]),
+    "fire_sim_inject": (_ip, [_vp, _fp, _fp, _fp, _fp, _fp]),
+    "fire_sim_stoke": (_ip, [_vp, _ip, _fp]),
+    "fire_sim_gust": (_ip, [_vp, _fp, _fp]),
+    "fire_sim_reset": (_ip, [_vp]),
+    "fire_sim_upload_logs": (_ip, [_vp, _vp, _ip]),
+    "fire_sim_field": (_ip, [_vp, _ip, ctypes.POINTER(FireFieldDesc)]),
+    "fire_sim_download": (_ip, [_vp, _ip, _vp, _sz]),
+    "fire_sim_upload": (_ip, [_vp, _ip, _vp, _sz]),
+    "fire_sim_info": (_ip, [_vp, ctypes.POINTER(FireInfo)]),
+    "fire_sim_last_error": (ctypes.c_char_p, [_vp]),
+    "fire_sim_run_stage": (_ip, [_vp, _ip, _fp, _vp]),
+    "fire_sim_run_mg": (_ip, [_vp, _ip, _ip, _ip, _vp]),
+    "fire_sim_level_io": (_ip, [_vp, _ip, _ip, _vp, _sz, _ip]),
+    "fire_sim_level_dims": (_ip, [_vp, _ip, ctypes.POINTER(_ip), ctypes.POINTER(_fp)]),
+    "fire_sim_profile": (_ip, [_vp, _ip]),
+    "fire_sim_stage_times": (_ip, [_vp, _vp, _ip]),
+    "fire_sim_residual": (_ip, [_vp, ctypes.POINTER(_dp), _vp]),
+    "fire_sim_stats": (_ip, [_vp, _ip, _vp, _vp]),
+    "fire_sim_hrr": (_ip, [_vp, ctypes.POINTER(_dp), _vp]),
+    "fire_sim_stats_async": (_ip, [_vp, _vp, _vp]),
+    "fire_build_campfire": (_ip, [ctypes.c_uint32, _vp, _ip]),
+    "fire_make_spots": (_ip, [ctypes.c_uint32, _ip, _fp, _fp, _fp, _fp, _vp]),
+    "fire_device_ok": (_ip, [_ip]),
+    "fire_version": (ctypes.c_char_p, []),
+}
+EXPORTS = tuple(_SIGS)
+
+_lib = None
+
+
+def load_library(path: Optional[os.PathLike] = None):
+    """Loads libfiresim.so; raises if it was not built (there is no fallback)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FireError(3, f"{p} is missing: build it with procedural-fire_gb300/fire_build.py")
+    L = ctypes.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def param_defaults() -> np.ndarray:
+    """SIM_DEFAULTS (src/sim.js:25-44) as the 64-float block."""
+    out = np.zeros(64, np.float32)
+    load_library().fire_param_defaults(_ptr(out))
+    return out
+
+
+SIM_DEFAULTS_NAMES = SIM_FIELDS[12:]
+
+
+def build_campfire(seed: int = 7, max_logs: int = 16) -> np.ndarray:
+    """buildCampfire(seed) + packLogs (src/scene.js:21-98): max_logs * 8 floats."""
+    out = np.zeros(max_logs * 8, np.float32)
+    n = load_library().fire_build_campfire(seed, _ptr(out), max_logs)
+    if n < 0:
+        raise FireError(1, "build_campfire")
+    return out
+
+
+def make_spots(seed: int, n: int, flux_lo: float = 1.0, flux_hi: float = 4.0, sigma: float = 0.02,
+               radius: float = 0.15) -> np.ndarray:
+    out = np.zeros((max(n, 1), 5), np.float32)
+    rc = load_library().fire_make_spots(seed, n, flux_lo, flux_hi, sigma, radius, _ptr(out))
+    if rc:
+        raise FireError(rc, "make_spots")
+    return out[:n]
+
+
+def device_ok(device: int = 0) -> bool:
+    return bool(load_library().fire_device_ok(device))
+
+
+def _stream_handle(stream) -> Optional[int]:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream", stream))   # torch.cuda.Stream
+
+
+class FireSim:
+    """GPU fire simulation with the reference FireSim's interface (src/sim.js:48-649)."""
+
+    def __init__(self, res: Sequence[int] = (80, 120, 80), size: Sequence[float] = (1.2, 1.8, 1.2),
+                 logs: Optional[np.ndarray] = None, vcycles: int = 2, device: int = 0, noise_seed: int = 1,
+                 mg_max_cycles: int = 0, mg_tol: float = 0.0):
+        self._lib = load_library()
+        self._h = None
+        cfg = FireConfig()
+        cfg.res[:] = [int(r) for r in res]
+        cfg.size[:] = [float(s) for s in size]
+        cfg.vcycles = int(vcycles)
+        cfg.device = int(device)
+        cfg.noise_seed = int(noise_seed)
+        cfg.mg_max_cycles = int(mg_max_cycles)
+        cfg.mg_tol = float(mg_tol)
+        if logs is None:
+            logs = np.zeros(0, np.float32)
+        lg = np.ascontiguousarray(logs, np.float32).reshape(-1)
+        if lg.size % 8:
+            raise FireError(1, "logs must hold 8 floats per log")
+        h = ctypes.c_void_p()
+        rc = self._lib.fire_sim_create(ctypes.byref(cfg), _ptr(lg) if lg.size else None, lg.size // 8, ctypes.byref(h))
+        if rc:
+            raise FireError(rc, "fire_sim_create")
+        self._h = h
+        self.res = tuple(int(r) for r in res)
+        self.size = tuple(float(s) for s in size)
+        info = self.info()
+        self.dx = info.dx
+        self.origin = tuple(info.origin)
+        self.coarse_iters = info.coarse_iters
+        self.levels = []
+        for l in range(info.n_levels):
+            d = (ctypes.c_int * 3)()
+            hh = ctypes.c_float()
+            self._lib.fire_sim_level_dims(self._h, l, d, ctypes.byref(hh))
+            self.levels.append({"dims": tuple(d), "h": hh.value})
+        self._pinned = None
+
+    # ---- lifetime ----
+    def close(self):
+        if self._h is not None:
+            self._lib.fire_sim_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            msg = self._lib.fire_sim_last_error(self._h)
+            raise FireError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    # ---- stepping ----
+    def step(self, dt: float, n: int = 1, stream=None):
+        """FireSim.step (src/sim.js:627-648), n times, asynchronously on `stream`."""
+        self._check(self._lib.fire_sim_step(self._h, float(dt), int(n), _stream_handle(stream)), "step")
+
+    def sync(self):
+        self._check(self._lib.fire_sim_sync(self._h), "sync")
+
+    # ---- parameters ----
+    def set_params(self, p: Dict[str, float]):
+        """FireSim.setParams (src/sim.js:601-604); unknown names raise, as UniformStruct.set does."""
+        if not p:
+            return
+        names = (ctypes.c_char_p * len(p))(*[k.encode() for k in p])
+        vals = np.asarray(list(p.values()), np.float32)
+        self._check(self._lib.fire_sim_set_params(self._h, names, _ptr(vals), len(p)), "set_params")
+
+    setParams = set_params
+
+    @property
+    def params(self) -> Dict[str, float]:
+        blk = np.zeros(64, np.float32)
+        self._check(self._lib.fire_sim_get_param_block(self._h, _ptr(blk)), "params")
+        return {k: float(blk[i]) for i, k in enumerate(SIM_FIELDS)}
+
+    def peek_block(self, dt: float) -> np.ndarray:
+        """The 200-float block (SIM_FIELDS uniforms + extension) the next step uploads."""
+        out = np.zeros(200, np.float32)
+        self._check(self._lib.fire_sim_peek_block(self._h, float(dt), _ptr(out)), "peek_block")
+        return out
+
+    def set_soot_age(self, age0: float, age1: float):
+        self._check(self._lib.fire_sim_set_soot_age(self._h, age0, age1), "set_soot_age")
+
+    def set_bed_gain(self, gain: float):
+        self._check(self._lib.fire_sim_set_bed_gain(self._h, gain), "set_bed_gain")
+
+    def set_spots(self, spots: np.ndarray):
+        s = np.ascontiguousarray(spots, np.float32).reshape(-1, 5)
+        self._check(self._lib.fire_sim_set_spots(self._h, _ptr(s) if len(s) else None, len(s)), "set_spots")
+
+    # ---- events ----
+    def inject(self, pos: Sequence[float], amount: float = 1.0, duration: float = 0.25):
+        self._check(self._lib.fire_sim_inject(self._h, *[float(v) for v in pos], float(amount), float(duration)), "inject")
+
+    def stoke(self, log_index: int = 3, s: float = 1.0):
+        self._check(self._lib.fire_sim_stoke(self._h, int(log_index), float(s)), "stoke")
+
+    def gust(self, strength: float = 1.0, duration: float = 2.4):
+        self._check(self._lib.fire_sim_gust(self._h, float(strength), float(duration)), "gust")
+
+    # ---- state ----
+    def reset(self):
+        """FireSim.reset (src/sim.js:606-618)."""
+        self._check(self._lib.fire_sim_reset(self._h), "reset")
+
+    def upload_logs(self, logs: np.ndarray):
+        lg = np.ascontiguousarray(logs, np.float32).reshape(-1)
+        self._check(self._lib.fire_sim_upload_logs(self._h, _ptr(lg) if lg.size else None, lg.size // 8), "upload_logs")
+
+    def info(self) -> FireInfo:
+        out = FireInfo()
+        self._check(self._lib.fire_sim_info(self._h, ctypes.byref(out)), "info")
+        return out
+
+    @property
+    def time(self) -> float:
+        return self.info().time
+
+    @property
+    def frame(self) -> int:
+        return self.info().frame
+
+    def field(self, name: str) -> FireFieldDesc:
+        d = FireFieldDesc()
+        self._check(self._lib.fire_sim_field(self._h, FIELDS[name], ctypes.byref(d)), f"field {name}")
+        return d
+
+    def _shape(self, d: FireFieldDesc):
+        shape = (d.dims[2], d.dims[1], d.dims[0]) + ((d.channels,) if d.channels > 1 else ())
+        return shape, (np.float16 if d.elem_bytes == 2 else np.float32)
+
+    def download(self, name: str) -> np.ndarray:
+        d = self.field(name)
+        shape, dt = self._shape(d)
+        out = np.empty(shape, dt)
+        self._check(self._lib.fire_sim_download(self._h, FIELDS[name], _ptr(out), out.nbytes), f"download {name}")
+        return out
+
+    def upload(self, name: str, arr: np.ndarray):
+        d = self.field(name)
+        shape, dt = self._shape(d)
+        a = np.ascontiguousarray(arr, dt)
+        if a.size != int(np.prod(shape)):
+            raise FireError(1, f"upload {name}: expected shape {shape}")
+        self._check(self._lib.fire_sim_upload(self._h, FIELDS[name], _ptr(a), a.nbytes), f"upload {name}")
+
+    # ---- stage-level ----
+    def run_stage(self, name: str, dt: float, stream=None):
+        self._check(self._lib.fire_sim_run_stage(self._h, STAGES[name], float(dt), _stream_handle(stream)), f"stage {name}")
+
+    def run_mg(self, op: str, level: int, arg: int = 0, stream=None):
+        code = {"smooth": 1, "restrict": 2, "prolong": 3, "tail": 4}[op]
+        self._check(self._lib.fire_sim_run_mg(self._h, code, level, arg, _stream_handle(stream)), f"mg {op}")
+
+    def level(self, l: int, which: str) -> np.ndarray:
+        nx, ny, nz = self.levels[l]["dims"]
+        out = np.empty((nz, ny, nx), np.float32)
+        self._check(self._lib.fire_sim_level_io(self._h, l, 0 if which == "p" else 1, _ptr(out), out.nbytes, 0), "level")
+        return out
+
+    def set_level(self, l: int, which: str, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, np.float32)
+        self._check(self._lib.fire_sim_level_io(self._h, l, 0 if which == "p" else 1, _ptr(a), a.nbytes, 1), "set_level")
+
+    def profile(self, enable: bool = True):
+        self._check(self._lib.fire_sim_profile(self._h, int(enable)), "profile")
+
+    def stage_times(self) -> Dict[str, float]:
+        ms = np.zeros(8, np.float32)
+        self._check(self._lib.fire_sim_stage_times(self._h, _ptr(ms), 8), "stage_times")
+        return {k: float(ms[v]) for k, v in STAGES.items()}
+
+    def residual(self, stream=None) -> float:
+        r = ctypes.c_double()
+        self._check(self._lib.fire_sim_residual(self._h, ctypes.byref(r), _stream_handle(stream)), "residual")
+        return r.value
+
+    # ---- diagnostics (FIRE.stats / FIRE.profile) ----
+    def stats(self, name: str = "S", stream=None):
+        out = np.zeros(16, np.float64)
+        self._check(self._lib.fire_sim_stats(self._h, FIELDS[name], _ptr(out), _stream_handle(stream)), "stats")
+        return [{"min": out[4 * c], "max": out[4 * c + 1], "mean": out[4 * c + 2], "bad": int(out[4 * c + 3])}
+                for c in range(4)]
+
+    def hrr(self, stream=None) -> float:
+        q = ctypes.c_double()
+        self._check(self._lib.fire_sim_hrr(self._h, ctypes.byref(q), _stream_handle(stream)), "hrr")
+        return q.value
+
+    def stats_async(self, out_ptr: int, stream=None):
+        """Queues S stats + heat release into a pinned host buffer of 17 doubles (no wait)."""
+        self._check(self._lib.fire_sim_stats_async(self._h, ctypes.c_void_p(out_ptr), _stream_handle(stream)), "stats_async")

@@ -1,0 +1,169 @@
+"""Step-level parity, determinism and API semantics of the CUDA simulation step.
+
+Tolerances (FP32 GPU vs FP32 oracle, which restates the WGSL step line by line):
+  * one step from a mid-burn state: per channel |gpu - oracle| <= 1e-3 |oracle| + 1e-4 max|oracle|, at most
+    0.5 % of cells beyond (a step chains ~20 kernels plus 4 V-cycles; FMA contraction differs);
+  * 60 steps from reset (48x96x48, dt = 1/120, 4 V-cycles): relative L2 error per field <= 2e-2 against the
+    FP32 oracle and <= 5e-2 against the FP64 oracle (the flow is chaotic, so errors grow with steps; the
+    measured values are printed).
+"""
+import numpy as np
+import pytest
+
+import fire_cases as FC
+import fire_sim as F
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def campfire():
+    return F.build_campfire(7)
+
+
+def _fields(sim_or_orc, gpu):
+    out = {}
+    for k in ("vel", "S", "S2", "velX"):
+        out[k] = sim_or_orc.download(k) if gpu else sim_or_orc.get(k)
+    out["p"] = sim_or_orc.level(0, "p") if gpu else sim_or_orc.get_level(0, "p")
+    return out
+
+
+def test_one_step_from_state(campfire):
+    sim, orc = FC.make_pair(FC.C1, logs=campfire, params={"windX": 0.3})
+    dt = FC.C1["dt"]
+    FC.put_state(sim, orc, FC.random_state(FC.C1["res"], 21))
+    FC.sync_block(sim, orc, dt)
+    sim.step(dt, 1)
+    sim.sync()
+    orc.step_raw(True, FC.C1["vcycles"])
+    g, o = _fields(sim, True), _fields(orc, False)
+    for k in ("vel", "S", "S2", "velX"):
+        for c in range(4):
+            FC.compare(g[k][..., c], o[k][..., c], 1e-3, 1e-4, 5e-3, what=f"step:{k}[{c}]")
+    FC.compare(g["p"], o["p"], 1e-3, 1e-4, 5e-3, what="step:p")
+
+
+def _run(cfg, logs, spots, nsteps, dbl):
+    sim, orc = FC.make_pair(cfg, logs=logs, dbl=dbl, spots=spots, bed_gain=0.0 if spots is not None else None)
+    dt = cfg["dt"]
+    for s in range(nsteps):
+        FC.sync_block(sim, orc, dt)
+        sim.step(dt, 1)
+        orc.step_raw(s == 0, cfg["vcycles"])
+    sim.sync()
+    return _fields(sim, True), _fields(orc, False), sim
+
+
+def _derived(f):
+    """Compared quantities: u, v, w, T, fuel, soot, age, p."""
+    S, S2, v = f["S"].astype(np.float64), f["S2"].astype(np.float64), f["vel"].astype(np.float64)
+    return {"u": v[..., 0], "v": v[..., 1], "w": v[..., 2], "T": 293.0 + 1000.0 * S[..., 0], "fuel": S[..., 1],
+            "soot": S[..., 2], "age": S2[..., 1] / np.maximum(S[..., 1] + S2[..., 0], 1e-4), "p": f["p"]}
+
+
+@pytest.mark.parametrize("emitter", ["campfire", "spots"])
+def test_sixty_steps_vs_oracles(campfire, emitter):
+    logs = campfire if emitter == "campfire" else None
+    spots = F.make_spots(1, 3, 2.0, 2.0, 0.02, 0.15) if emitter == "spots" else None
+    g32, o32, sim = _run(FC.C1, logs, spots, 60, False)
+    _, o64, _ = _run(FC.C1, logs, spots, 60, True)
+    dg, d32, d64 = _derived(g32), _derived(o32), _derived(o64)
+    report = {}
+    for k in dg:
+        e32, e64 = FC.rel_l2(dg[k], d32[k]), FC.rel_l2(dg[k], d64[k])
+        report[k] = (e32, e64)
+        assert np.isfinite(dg[k]).all()
+    print(f"\n60-step rel L2 errors ({emitter}): " + ", ".join(f"{k}: {a:.2e}/{b:.2e}" for k, (a, b) in report.items()))
+    for k, (e32, e64) in report.items():
+        assert e32 <= 2e-2, (k, e32)
+        assert e64 <= 5e-2, (k, e64)
+    # the fire must actually be burning: heat release and hot gas present
+    assert sim.hrr() > 0.1
+    assert dg["T"].max() > 900.0
+
+
+def test_determinism(campfire):
+    outs = []
+    for _ in range(2):
+        sim = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=4)
+        sim.step(FC.C1["dt"], 20)
+        sim.sync()
+        outs.append([sim.download(k) for k in ("vel", "S", "S2")] + [sim.level(0, "p")])
+        sim.close()
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_reset_and_time(campfire):
+    sim = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=2)
+    sim.step(FC.C1["dt"], 5)
+    sim.sync()
+    assert sim.frame == 5 and sim.time == pytest.approx(5 / 120)
+    assert np.abs(sim.download("S")).max() > 0
+    sim.reset()
+    assert sim.frame == 0 and sim.time == 0
+    for k in ("vel", "velX", "velY", "S", "SX", "SY", "S2", "S2X", "S2Y", "vort"):
+        assert not sim.download(k).any(), k
+    assert not sim.level(0, "p").any()
+
+
+def test_params_api(campfire):
+    sim = F.FireSim(res=(32, 48, 32), size=(0.4, 0.6, 0.4), logs=campfire)
+    d = sim.params
+    assert d["buoyancy"] == pytest.approx(26.8) and d["vortEps"] == 8 and d["anchorGain"] == pytest.approx(0.95)
+    sim.set_params({"vortEps": 0.3, "turbAmp": 0.2})
+    assert sim.params["vortEps"] == pytest.approx(0.3)
+    with pytest.raises(F.FireError) as ei:
+        sim.set_params({"vortEps": 1.0, "notAParam": 2.0})
+    assert ei.value.code == 2
+    assert sim.params["vortEps"] == pytest.approx(0.3)   # nothing applied on error
+    blk = sim.peek_block(0.01)
+    assert blk[0] == 32 and blk[3] == pytest.approx(0.4 / 32) and blk[4] == pytest.approx(0.01)
+    assert blk[8] == pytest.approx(-0.2) and blk[11] == 16
+
+
+def test_events(campfire):
+    sim = F.FireSim(res=(32, 48, 32), size=(0.4, 0.6, 0.4), logs=campfire)
+    dt = 1 / 100
+    sim.inject((0.0, 0.08, 0.0), 1.0, 0.05)
+    sim.step(dt, 1)
+    assert sim.params["burstAmt"] == 1.0
+    sim.step(dt, 5)
+    assert sim.params["burstAmt"] == 0.0
+    sim.gust(1.0, 0.2)
+    sim.step(dt, 10)
+    wx = sim.params["windX"]
+    assert wx < -1.0    # mid-gust: -1.4 sin(pi/2)
+    sim.step(dt, 15)
+    assert sim.params["windX"] == 0.0
+    before = sim.download("geo")
+    sim.stoke(3, 1.0)
+    sim.step(dt, 1)
+    sim.sync()
+    assert not np.array_equal(before, sim.download("geo"))
+
+
+def test_stats_and_hrr_match_numpy(campfire):
+    sim = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=2)
+    sim.step(FC.C1["dt"], 30)
+    S = sim.download("S").astype(np.float64).reshape(-1, 4)
+    st = sim.stats("S")
+    for c in range(4):
+        assert st[c]["min"] == S[:, c].min() and st[c]["max"] == S[:, c].max()
+        assert st[c]["mean"] == pytest.approx(S[:, c].mean(), rel=1e-12, abs=1e-15)
+        assert st[c]["bad"] == 0
+    q = S[:, 3] * 1e4
+    T = 293.0 + 1000.0 * S[:, 0]
+    want = (354800.0 * q[q > 0] / T[q > 0] * (sim.dx ** 3)).sum() / 1000.0
+    assert sim.hrr() == pytest.approx(want, rel=1e-9)
+
+
+def test_residual_driven_solve(campfire):
+    sim = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=4, mg_max_cycles=12, mg_tol=1e-4)
+    sim.step(FC.C1["dt"], 10)
+    sim.sync()
+    info = sim.info()
+    assert 1 <= info.last_cycles <= 12
+    assert info.last_rel_residual <= 1e-4 or info.last_cycles == 12
+    assert sim.residual() == pytest.approx(info.last_rel_residual, rel=1e-6)
