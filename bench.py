@@ -244,7 +244,7 @@ def run_ours(args):
     sh = stream.cuda_stream
     dt = W["dt"]
 
-    sim.step(dt, W["preroll"] + args.warmup, stream=sh)
+    sim.step(dt, args.preroll + args.warmup, stream=sh)
     torch.cuda.synchronize(dev)
     info0 = sim.info()
 
@@ -393,6 +393,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--preroll", type=int, default=WORKLOAD["preroll"], help="untimed steps that develop the fire")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     out = run_reference(args) if args.impl == "reference" else run_ours(args)

@@ -3,9 +3,9 @@
 Tolerances (FP32 GPU vs FP32 oracle, which restates the WGSL step line by line):
   * one step from a mid-burn state: per channel |gpu - oracle| <= 1e-3 |oracle| + 1e-4 max|oracle|, at most
     0.5 % of cells beyond (a step chains ~20 kernels plus 4 V-cycles; FMA contraction differs);
-  * 60 steps from reset (48x96x48, dt = 1/120, 4 V-cycles): relative L2 error per field <= 2e-2 against the
-    FP32 oracle and <= 5e-2 against the FP64 oracle (the flow is chaotic, so errors grow with steps; the
-    measured values are printed).
+  * 60 steps from reset (48x96x48, dt = 1/120, 4 V-cycles): relative L2 error per field <= 1e-2 against the
+    FP32 oracle; against the FP64 oracle within 1.5x (+1e-2) of the FP32 oracle's own FP64 error (the flow
+    is chaotic, so FP32 and FP64 trajectories separate; the measured values are printed).
 """
 import numpy as np
 import pytest
@@ -64,20 +64,27 @@ def _derived(f):
 
 @pytest.mark.parametrize("emitter", ["campfire", "spots"])
 def test_sixty_steps_vs_oracles(campfire, emitter):
+    """60 steps from rest.  Against the FP32 oracle: rel L2 <= 1e-2 per field.  Against the FP64 oracle the
+    FP32 flow itself diverges (the plume is chaotic and the model is full of smoothstep thresholds), so the
+    bound is relative to the FP32 oracle's own FP64 error: the GPU must be as accurate as a faithful FP32
+    restatement of the WGSL (within 1.5x + 1e-2).  Age is compared where fuel + products > 1e-2."""
     logs = campfire if emitter == "campfire" else None
     spots = F.make_spots(1, 3, 2.0, 2.0, 0.02, 0.15) if emitter == "spots" else None
     g32, o32, sim = _run(FC.C1, logs, spots, 60, False)
     _, o64, _ = _run(FC.C1, logs, spots, 60, True)
     dg, d32, d64 = _derived(g32), _derived(o32), _derived(o64)
+    z = (o64["S"][..., 1].astype(np.float64) + o64["S2"][..., 0]) > 1e-2
+    for d in (dg, d32, d64):
+        d["age"] = d["age"][z]
     report = {}
     for k in dg:
-        e32, e64 = FC.rel_l2(dg[k], d32[k]), FC.rel_l2(dg[k], d64[k])
-        report[k] = (e32, e64)
         assert np.isfinite(dg[k]).all()
-    print(f"\n60-step rel L2 errors ({emitter}): " + ", ".join(f"{k}: {a:.2e}/{b:.2e}" for k, (a, b) in report.items()))
-    for k, (e32, e64) in report.items():
-        assert e32 <= 2e-2, (k, e32)
-        assert e64 <= 5e-2, (k, e64)
+        report[k] = (FC.rel_l2(dg[k], d32[k]), FC.rel_l2(dg[k], d64[k]), FC.rel_l2(d32[k], d64[k]))
+    print(f"\n60-step rel L2 errors ({emitter}) gpu-vs-f32 / gpu-vs-f64 / f32oracle-vs-f64: " +
+          ", ".join(f"{k}: {a:.2e}/{b:.2e}/{c:.2e}" for k, (a, b, c) in report.items()))
+    for k, (e32, e64, o3264) in report.items():
+        assert e32 <= 1e-2, (k, e32)
+        assert e64 <= 1.5 * o3264 + 1e-2, (k, e64, o3264)
     # the fire must actually be burning: heat release and hot gas present
     assert sim.hrr() > 0.1
     assert dg["T"].max() > 900.0
@@ -129,7 +136,9 @@ def test_events(campfire):
     sim.inject((0.0, 0.08, 0.0), 1.0, 0.05)
     sim.step(dt, 1)
     assert sim.params["burstAmt"] == 1.0
-    sim.step(dt, 5)
+    sim.step(dt, 3)
+    assert sim.params["burstAmt"] == 1.0   # still inside the 0.05 s window
+    sim.step(dt, 4)
     assert sim.params["burstAmt"] == 0.0
     sim.gust(1.0, 0.2)
     sim.step(dt, 10)
