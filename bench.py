@@ -157,10 +157,12 @@ def ncu_traffic(kernel_stage: str):
         return None
 
 
-def make_sim(F, device: int):
+def make_sim(F, device: int, mg_fixed: int = 0):
+    """The workload's simulation.  mg_fixed > 0 replaces the residual-driven solve by that many fixed
+    V-cycles (same kernels, no conditional graph node), which ncu needs to profile graph kernel nodes."""
     W = WORKLOAD
-    sim = F.FireSim(res=W["res"], size=W["size"], logs=None, vcycles=4, device=device,
-                    mg_max_cycles=W["mg_max_cycles"], mg_tol=W["mg_tol"])
+    sim = F.FireSim(res=W["res"], size=W["size"], logs=None, vcycles=mg_fixed or 4, device=device,
+                    mg_max_cycles=0 if mg_fixed else W["mg_max_cycles"], mg_tol=W["mg_tol"])
     sim.set_params({"vortEps": W["vortEps"], "turbAmp": W["turbAmp"]})
     sim.set_soot_age(*W["soot_age"])
     sim.set_bed_gain(0.0)
@@ -170,7 +172,8 @@ def make_sim(F, device: int):
 
 def launches_per_step(sim, cycles_per_step: float) -> float:
     """Kernels launched per step by the captured graph: 5 stencil kernels, the counter reset, and per
-    V-cycle 10 per level above the shared-memory tail, the tail kernel, 2 residual kernels and the decision."""
+    V-cycle 6 per level above the shared-memory tail (2 + 2 sweeps, restrict, prolong), the tail kernel,
+    2 residual kernels and the decision."""
     n = len(sim.levels)
     cells = [l["dims"][0] * l["dims"][1] * l["dims"][2] for l in sim.levels]
     T = n
@@ -179,7 +182,7 @@ def launches_per_step(sim, cycles_per_step: float) -> float:
             T = l
         else:
             break
-    per_cycle = 10 * min(T, n - 1) + (1 if T < n else 2 * sim.coarse_iters) + 3
+    per_cycle = 6 * min(T, n - 1) + (1 if T < n else sim.coarse_iters) + 3
     return 6 + per_cycle * cycles_per_step
 
 
@@ -239,7 +242,7 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     W = WORKLOAD
     cells = W["res"][0] * W["res"][1] * W["res"][2]
-    sim = make_sim(F, dev)
+    sim = make_sim(F, dev, args.mg_fixed)
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
     dt = W["dt"]
@@ -394,6 +397,8 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--preroll", type=int, default=WORKLOAD["preroll"], help="untimed steps that develop the fire")
+    ap.add_argument("--mg-fixed", type=int, default=0,
+                    help="profiling aid: N fixed V-cycles per step instead of the residual-driven solve")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     out = run_reference(args) if args.impl == "reference" else run_ours(args)

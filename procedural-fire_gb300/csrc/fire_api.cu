@@ -225,6 +225,7 @@ int upload_block(FireSim* sim, float dt, cudaStream_t st, bool with_logs) {
   return FIRE_OK;
 }
 
+// `iters` red-black sweeps of level l (src/sim.js:576-586): colour 0 then colour 1, one launch each.
 void record_smooth(FireSim* s, int l, int iters, cudaStream_t st) {
   for (int k = 0; k < iters; ++k) { launch_smooth(s->levels[l], 0, st); launch_smooth(s->levels[l], 1, st); }
 }
@@ -334,7 +335,7 @@ int build_graph(FireSim* sim) {
 int ensure_geo(FireSim* sim, cudaStream_t st) {
   if (sim->geoReady && !sim->logsDirty) return FIRE_OK;
   // geometry uses the current block (dx, origin, hot radii, nLogs) and the log buffer
-  launch_geo(sim->dBlock, sim->dLogs, sim->f.geo, sim->d, st);
+  launch_geo(sim->dBlock, sim->dLogs, sim->f.geo, sim->f.solid, sim->d, st);
   CK(cudaGetLastError());
   sim->geoReady = true;
   sim->logsDirty = false;
@@ -442,6 +443,7 @@ int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSi
     bOff[l] = off; off = align_up(off + c * sizeof(float));
   }
   const size_t tabBytes = (size_t)TABLE_N * TABLE_N * TABLE_N * sizeof(uint2);
+  size_t solidOff = off; off = align_up(off + cells);
   size_t noiseOff = off; off = align_up(off + tabBytes);
   size_t curlOff = off; off = align_up(off + tabBytes);
   size_t blockOff = off; off = align_up(off + sizeof(float) * BLOCK_FLOATS);
@@ -457,9 +459,13 @@ int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSi
   float4** fp[11] = {&sim->f.vel, &sim->f.velX, &sim->f.velY, &sim->f.S, &sim->f.SX, &sim->f.SY,
                      &sim->f.S2, &sim->f.S2X, &sim->f.S2Y, &sim->f.vort, &sim->f.geo};
   for (int i = 0; i < 11; ++i) *fp[i] = (float4*)(A + fieldOff[i]);
-  for (size_t l = 0; l < sim->levels.size(); ++l) { sim->levels[l].p = (float*)(A + pOff[l]); sim->levels[l].b = (float*)(A + bOff[l]); }
+  for (size_t l = 0; l < sim->levels.size(); ++l) {
+    sim->levels[l].p = (float*)(A + pOff[l]);
+    sim->levels[l].b = (float*)(A + bOff[l]);
+  }
   sim->noise = (uint2*)(A + noiseOff);
   sim->curl = (uint2*)(A + curlOff);
+  sim->f.solid = (unsigned char*)(A + solidOff);
   sim->dBlock = (float*)(A + blockOff);
   sim->dLogs = (float*)(A + logsOff);
   sim->dPartials = (double*)(A + partOff);
@@ -479,6 +485,7 @@ int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSi
   if (cudaEventCreateWithFlags(&sim->doneEv, cudaEventDisableTiming) != cudaSuccess) return fail(FIRE_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&sim->capStream, cudaStreamNonBlocking) != cudaSuccess) return fail(FIRE_ERR_CUDA);
   if (mg_configure(TAIL_SMEM_BUDGET) != cudaSuccess) return fail(set_err(sim, FIRE_ERR_CUDA, "tail kernel smem opt-in failed"));
+  if (step_configure() != cudaSuccess) return fail(set_err(sim, FIRE_ERR_CUDA, "forces kernel smem opt-in failed"));
 
   // zero state (reset semantics), bake the tables (src/noise.js), upload logs
   cudaStream_t st = sim->capStream;
@@ -713,7 +720,13 @@ int fire_sim_upload(FireSim* sim, int which, const void* host, size_t bytes) {
   CK(cudaSetDevice(sim->device));
   CK(cudaDeviceSynchronize());
   CK(cudaMemcpy(d.data, host, bytes, cudaMemcpyHostToDevice));
-  if (which == FIRE_FIELD_GEO) { sim->geoReady = true; sim->logsDirty = false; }   // caller-provided geometry
+  if (which == FIRE_FIELD_GEO) {   // caller-provided geometry: derive the solid mask, skip the rebuild
+    launch_solid_mask(sim->f.geo, sim->f.solid, sim->d, nullptr);
+    CK(cudaGetLastError());
+    CK(cudaDeviceSynchronize());
+    sim->geoReady = true;
+    sim->logsDirty = false;
+  }
   return FIRE_OK;
 }
 
@@ -778,10 +791,16 @@ int fire_sim_run_mg(FireSim* sim, int op, int level, int arg, void* stream) {
     case 1: if (arg != 0 && arg != 1) return FIRE_ERR_BAD_ARG; launch_smooth(sim->levels[level], arg, st); break;
     case 2: if (level >= n - 1) return FIRE_ERR_BAD_ARG; launch_restrict(sim->levels[level], sim->levels[level + 1], st); break;
     case 3: if (level >= n - 1) return FIRE_ERR_BAD_ARG; launch_prolong(sim->levels[level], sim->levels[level + 1], st); break;
-    case 4: launch_tail(sim->levels.data(), level, n, 2, 2, sim->coarseIters, st); break;   // tail from `level`
+    case 5:   // `arg` red-black sweeps (each = colour 0 then colour 1), as the V-cycle runs them
+      if (arg < 1) return FIRE_ERR_BAD_ARG;
+      record_smooth(sim, level, arg, st);
+      break;
+    case 4:   // the shared-memory V-cycle from `level` down, if it fits
+      if (tail_smem_bytes(sim->levels.data(), level, n) > TAIL_SMEM_BUDGET) return FIRE_ERR_BAD_ARG;
+      launch_tail(sim->levels.data(), level, n, 2, 2, sim->coarseIters, st);
+      break;
     default: return FIRE_ERR_BAD_ARG;
   }
-  if (op == 4 && tail_smem_bytes(sim->levels.data(), level, n) > TAIL_SMEM_BUDGET) return FIRE_ERR_BAD_ARG;
   CK(cudaGetLastError());
   return FIRE_OK;
 }

@@ -38,6 +38,7 @@ struct Fields {
   float4* S; float4* SX; float4* SY;
   float4* S2; float4* S2X; float4* S2Y;
   float4* vort; float4* geo;
+  unsigned char* solid;   // geo.b > 0.5 as one byte per cell (what projection reads)
 };
 struct Dims { int nx, ny, nz; };
 
@@ -51,7 +52,9 @@ struct MGLevel {
 // ---- kernel launchers (fire_tables.cu) ----
 void launch_noise_table(uint2* noise, int N, int seed, cudaStream_t st);
 void launch_curl_table(const uint2* noise, uint2* curl, int N, cudaStream_t st);
-void launch_geo(const float* P, const float* logs, float4* geo, Dims d, cudaStream_t st);
+void launch_geo(const float* P, const float* logs, float4* geo, unsigned char* solid, Dims d, cudaStream_t st);
+// Rebuilds the solid mask from a caller-provided geometry field.
+void launch_solid_mask(const float4* geo, unsigned char* solid, Dims d, cudaStream_t st);
 
 // ---- kernel launchers (fire_step.cu) ----
 void launch_adv1(const float* P, Fields f, Dims d, cudaStream_t st);
@@ -59,6 +62,9 @@ void launch_adv2(const float* P, Fields f, Dims d, cudaStream_t st);
 void launch_curl(Fields f, Dims d, cudaStream_t st);
 void launch_forces(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
 void launch_forces_unfused(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
+void launch_forces_recompute(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
+// Opts the shared-memory kernels of fire_step.cu into their dynamic shared memory on the current device.
+cudaError_t step_configure();
 void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st);
 void launch_project(const float* P, Fields f, const float* p0, Dims d, cudaStream_t st);
 

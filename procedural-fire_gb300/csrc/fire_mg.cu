@@ -5,21 +5,26 @@
 // sum_nb(p) - 6 p = h^2 b with the ghost rules folded into the diagonal of the red-black Gauss-Seidel
 // update, exactly as mgSmooth does.
 //
-// GB300 mapping: the fine levels run as one launch per colour sweep (the grid is large enough to fill
-// 152 SMs); every level small enough to fit, with all coarser ones, in one CTA's shared memory is
-// solved by a single-CTA kernel that runs the rest of the V-cycle (smoothing, restriction, the coarse
-// sweeps and prolongation) out of shared memory with __syncthreads between colours.  At 128x256x128
-// this replaces the 3 coarsest levels' ~40 launches per cycle with one.
+// GB300 mapping:
+//  * the fine levels run one launch per colour sweep, restriction and prolongation on 3D grids of
+//    32 x 4 x 2 CTAs (32-bit index arithmetic, no integer division); at 128x256x128 the level-0 arrays
+//    (p and b, 33.5 MB) stay resident in the 129 MB L2 across the cycle;
+//  * every level small enough to fit, with all coarser ones, in one CTA's shared memory is solved by a
+//    single-CTA kernel that runs the rest of the V-cycle out of shared memory; levels of <= 1024 cells
+//    inside it run on one warp with __syncwarp, so the coarse sweeps cost no CTA-wide barriers;
+//  * every kernel uses programmatic dependent launch (fire_launch.cuh) so consecutive launches overlap.
 #include "fire_device.cuh"
+#include "fire_launch.cuh"
 
 namespace fire {
 
-constexpr int MB = 256;
+constexpr int GX = 32, GY = 4, GZ = 2;   // CTA shape of the level kernels (256 threads)
 
-// ---------------- red-black Gauss-Seidel sweep, one colour (src/sim.js:417-437) ----------------
+// ---------------- red-black Gauss-Seidel update of one cell (src/sim.js:417-437) ----------------
+// Neighbours in the order mgSmooth sums them: x-, x+, z-, z+, y-, y+.
 __device__ __forceinline__ float rb_update(const float* p, const float* b, int x, int y, int z, int nx, int ny, int nz, float h2) {
-  const size_t c = (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z);
-  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  const int sy = nx, sz = nx * ny;
+  const int c = x + y * sy + z * sz;
   float sum = 0.0f, diag = 6.0f;
   if (x > 0) sum += p[c - 1]; else diag += 1.0f;
   if (x < nx - 1) sum += p[c + 1]; else diag += 1.0f;
@@ -29,48 +34,46 @@ __device__ __forceinline__ float rb_update(const float* p, const float* b, int x
   if (y < ny - 1) sum += p[c + sy]; else diag += 1.0f;
   return (sum - h2 * b[c]) / diag;
 }
-__global__ void __launch_bounds__(MB) k_smooth(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
-                                               float h, int color) {
-  const int hx = (nx + 1) >> 1;
-  const long long t = (long long)blockIdx.x * MB + threadIdx.x;
-  const long long total = (long long)hx * ny * nz;
-  if (t >= total) return;
-  const int gx = (int)(t % hx);
-  const long long r = t / hx;
-  const int y = (int)(r % ny), z = (int)(r / ny);
+__global__ void __launch_bounds__(GX * GY * GZ) k_smooth(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
+                                                         float h, int color) {
+  pdl_wait();
+  pdl_trigger();
+  const int gx = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y, z = blockIdx.z * GZ + threadIdx.z;
+  if (y >= ny || z >= nz) return;
   const int x = gx * 2 + ((y + z + color) & 1);
   if (x >= nx) return;
-  p[(size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)] = rb_update(p, b, x, y, z, nx, ny, nz, h * h);
+  p[x + nx * (y + ny * z)] = rb_update(p, b, x, y, z, nx, ny, nz, h * h);
 }
 
 // ---------------- fused residual + restriction (src/sim.js:439-466) ----------------
 __device__ __forceinline__ float pghost(const float* p, int x, int y, int z, int nx, int ny, int nz, float me) {
   if (x < 0 || z < 0 || x >= nx || z >= nz || y >= ny) return -me;
   if (y < 0) return me;
-  return p[(size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)];
+  return p[x + nx * (y + ny * z)];
 }
 __device__ __forceinline__ float restrict_cell(const float* p, const float* b, int cx, int cy, int cz, int nx, int ny, int nz, float ih2) {
   float acc = 0.0f;
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const int x = 2 * cx + (q & 1), y = 2 * cy + ((q >> 1) & 1), z = 2 * cz + ((q >> 2) & 1);
-    const float me = p[(size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)];
+    const int c = x + nx * (y + ny * z);
+    const float me = p[c];
     const float lap = (pghost(p, x - 1, y, z, nx, ny, nz, me) + pghost(p, x + 1, y, z, nx, ny, nz, me) +
                        pghost(p, x, y - 1, z, nx, ny, nz, me) + pghost(p, x, y + 1, z, nx, ny, nz, me) +
                        pghost(p, x, y, z - 1, nx, ny, nz, me) + pghost(p, x, y, z + 1, nx, ny, nz, me) - 6.0f * me) * ih2;
-    acc += b[(size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)] - lap;
+    acc += b[c] - lap;
   }
   return acc * 0.125f;
 }
-__global__ void __launch_bounds__(MB) k_restrict(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
-                                                 float h, float* __restrict__ bc, float* __restrict__ pc) {
+__global__ void __launch_bounds__(GX * GY * GZ) k_restrict(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
+                                                           float h, float* __restrict__ bc, float* __restrict__ pc) {
+  pdl_wait();
+  pdl_trigger();
   const int cnx = nx / 2, cny = ny / 2, cnz = nz / 2;
-  const long long t = (long long)blockIdx.x * MB + threadIdx.x;
-  if (t >= (long long)cnx * cny * cnz) return;
-  const int cx = (int)(t % cnx);
-  const long long r = t / cnx;
-  const int cy = (int)(r % cny), cz = (int)(r / cny);
+  const int cx = blockIdx.x * GX + threadIdx.x, cy = blockIdx.y * GY + threadIdx.y, cz = blockIdx.z * GZ + threadIdx.z;
+  if (cx >= cnx || cy >= cny || cz >= cnz) return;
   const float ih2 = 1.0f / (h * h);
+  const int t = cx + cnx * (cy + cny * cz);
   bc[t] = restrict_cell(p, b, cx, cy, cz, nx, ny, nz, ih2);
   pc[t] = 0.0f;
 }
@@ -85,7 +88,7 @@ __device__ __forceinline__ float prolong_cell(const float* pc, int x, int y, int
   for (int q = 0; q < 8; ++q) {
     const int ox = q & 1, oy = (q >> 1) & 1, oz = (q >> 2) & 1;
     const int qx = g0x + ox, qy = g0y + oy, qz = g0z + oz;
-    float val = pc[(size_t)min(max(qx, 0), ncx - 1) + (size_t)ncx * ((size_t)min(max(qy, 0), ncy - 1) + (size_t)ncy * min(max(qz, 0), ncz - 1))];
+    float val = pc[min(max(qx, 0), ncx - 1) + ncx * (min(max(qy, 0), ncy - 1) + ncy * min(max(qz, 0), ncz - 1))];
     // odd mirror (Dirichlet) on sides/top, even (Neumann) at the floor; one flip per axis outside
     if (qx < 0 || qx >= ncx) val = -val;
     if (qz < 0 || qz >= ncz) val = -val;
@@ -95,146 +98,259 @@ __device__ __forceinline__ float prolong_cell(const float* pc, int x, int y, int
   }
   return acc;
 }
-__global__ void __launch_bounds__(MB) k_prolong(float* __restrict__ p, const float* __restrict__ pc, int nx, int ny, int nz) {
-  const long long t = (long long)blockIdx.x * MB + threadIdx.x;
-  if (t >= (long long)nx * ny * nz) return;
-  const int x = (int)(t % nx);
-  const long long r = t / nx;
-  const int y = (int)(r % ny), z = (int)(r / ny);
-  p[t] = p[t] + prolong_cell(pc, x, y, z, nx / 2, ny / 2, nz / 2);
+// One thread per coarse cell: the 3x3x3 coarse neighbourhood (with the mirror signs of prolong_cell) is
+// loaded once and the 8 fine children are formed from it.  For fine index c = 2 cc + d the trilinear base is
+// g0 = cc - 1 + d with fraction 0.75 (d = 0) or 0.25 (d = 1), so child d reads coarse offsets d-1 and d;
+// each child's sum runs in prolong_cell's order, so the result is identical.
+__global__ void __launch_bounds__(GX * GY * GZ) k_prolong(float* __restrict__ p, const float* __restrict__ pc, int nx, int ny, int nz) {
+  pdl_wait();
+  pdl_trigger();
+  const int ncx = nx / 2, ncy = ny / 2, ncz = nz / 2;
+  const int cx = blockIdx.x * GX + threadIdx.x, cy = blockIdx.y * GY + threadIdx.y, cz = blockIdx.z * GZ + threadIdx.z;
+  if (cx >= ncx || cy >= ncy || cz >= ncz) return;
+  float v[3][3][3];   // [dz][dy][dx] for offsets -1..1
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int qx = cx + c - 1, qy = cy + bb - 1, qz = cz + a - 1;
+        float val = __ldg(pc + min(max(qx, 0), ncx - 1) + ncx * (min(max(qy, 0), ncy - 1) + ncy * min(max(qz, 0), ncz - 1)));
+        if (qx < 0 || qx >= ncx) val = -val;
+        if (qz < 0 || qz >= ncz) val = -val;
+        if (qy >= ncy) val = -val;
+        v[a][bb][c] = val;
+      }
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const float fx = dx ? 0.25f : 0.75f, fy = dy ? 0.25f : 0.75f, fz = dz ? 0.25f : 0.75f;
+        float acc = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int ox = q & 1, oy = (q >> 1) & 1, oz = (q >> 2) & 1;
+          const float wx = ox ? fx : 1.0f - fx, wy = oy ? fy : 1.0f - fy, wz = oz ? fz : 1.0f - fz;
+          acc += v[dz + oz][dy + oy][dx + ox] * wx * wy * wz;
+        }
+        const int t = (2 * cx + dx) + nx * ((2 * cy + dy) + ny * (2 * cz + dz));
+        p[t] = p[t] + acc;
+      }
 }
 
 // ---------------- single-CTA tail V-cycle out of shared memory ----------------
+// Cells are visited as a flat index split into (x, y, z) with a float-reciprocal quotient and a one-step
+// correction (exact for indices below 2^24), several times cheaper than integer division.  Levels with
+// at most TAIL_WARP_CELLS cells run on warp 0 alone, synchronised with __syncwarp.
 constexpr int TAIL_THREADS = 1024;
+constexpr int TAIL_WARP_CELLS = 1024;
 constexpr int TAIL_MAX_LEVELS = 12;
 struct TailLevels {
   int n;                       // number of levels in the tail
+  int small;                   // first tail level with <= TAIL_WARP_CELLS cells (n if none)
   int nx[TAIL_MAX_LEVELS], ny[TAIL_MAX_LEVELS], nz[TAIL_MAX_LEVELS];
   float h[TAIL_MAX_LEVELS];
   int off[TAIL_MAX_LEVELS];    // float offset of level l's p in shared memory (b follows p)
   float* gp[TAIL_MAX_LEVELS];  // global copies (written back at the end)
   float* gb[TAIL_MAX_LEVELS];
 };
-__device__ void tail_smooth(float* p, const float* b, int nx, int ny, int nz, float h, int iters) {
+struct FastDiv {
+  int d;
+  float r;
+  __device__ FastDiv(int dd) : d(dd), r(1.0f / (float)dd) {}
+  __device__ __forceinline__ int div(int t) const {
+    int q = __float2int_rz((float)t * r);
+    const int rem = t - q * d;
+    if (rem < 0) --q;
+    else if (rem >= d) ++q;
+    return q;
+  }
+};
+// A group of threads working on one level: the whole CTA (barrier = __syncthreads) or warp 0 (__syncwarp).
+template <bool kWarp>
+struct Team {
+  int rank;
+  static constexpr int size = kWarp ? 32 : TAIL_THREADS;
+  __device__ __forceinline__ void sync() const { if (kWarp) __syncwarp(); else __syncthreads(); }
+};
+template <bool kWarp>
+__device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters) {
   const int hx = (nx + 1) >> 1;
   const int total = hx * ny * nz;
   const float h2 = h * h;
+  const FastDiv dhx(hx), dny(ny);
   for (int it = 0; it < iters; ++it)
     for (int color = 0; color < 2; ++color) {
-      for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int gx = t % hx, r = t / hx, y = r % ny, z = r / ny;
+      for (int t = tm.rank; t < total; t += tm.size) {
+        const int r = dhx.div(t), gx = t - r * hx;
+        const int z = dny.div(r), y = r - z * ny;
         const int x = gx * 2 + ((y + z + color) & 1);
         if (x < nx) p[x + nx * (y + ny * z)] = rb_update(p, b, x, y, z, nx, ny, nz, h2);
       }
-      __syncthreads();
+      tm.sync();
     }
+}
+template <bool kWarp>
+__device__ void tail_restrict(const Team<kWarp>& tm, const TailLevels& T, float* sm, int l) {
+  const int nx = T.nx[l], ny = T.ny[l], nz = T.nz[l];
+  const float* p = sm + T.off[l];
+  const float* b = p + nx * ny * nz;
+  const int cnx = T.nx[l + 1], cny = T.ny[l + 1], cnz = T.nz[l + 1];
+  float* pc = sm + T.off[l + 1];
+  float* bc = pc + cnx * cny * cnz;
+  const float ih2 = 1.0f / (T.h[l] * T.h[l]);
+  const FastDiv dcx(cnx), dcy(cny);
+  for (int t = tm.rank; t < cnx * cny * cnz; t += tm.size) {
+    const int r = dcx.div(t), cx = t - r * cnx;
+    const int cz = dcy.div(r), cy = r - cz * cny;
+    bc[t] = restrict_cell(p, b, cx, cy, cz, nx, ny, nz, ih2);
+    pc[t] = 0.0f;
+  }
+  tm.sync();
+}
+template <bool kWarp>
+__device__ void tail_prolong(const Team<kWarp>& tm, const TailLevels& T, float* sm, int l) {
+  const int nx = T.nx[l], ny = T.ny[l], nz = T.nz[l];
+  float* p = sm + T.off[l];
+  const float* pc = sm + T.off[l + 1];
+  const FastDiv dx_(nx), dy_(ny);
+  for (int t = tm.rank; t < nx * ny * nz; t += tm.size) {
+    const int r = dx_.div(t), x = t - r * nx;
+    const int z = dy_.div(r), y = r - z * ny;
+    p[t] = p[t] + prolong_cell(pc, x, y, z, nx / 2, ny / 2, nz / 2);
+  }
+  tm.sync();
+}
+// V-cycle over tail levels [from, n) with one team (src/sim.js:588-599 restricted to these levels).
+template <bool kWarp>
+__device__ void tail_vcycle(const Team<kWarp>& tm, const TailLevels& T, float* sm, int from, int pre, int post, int coarse) {
+  const int n = T.n;
+  for (int l = from; l < n - 1; ++l) {
+    float* p = sm + T.off[l];
+    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
+    tail_restrict(tm, T, sm, l);
+  }
+  {
+    float* p = sm + T.off[n - 1];
+    tail_smooth(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse);
+  }
+  for (int l = n - 2; l >= from; --l) {
+    tail_prolong(tm, T, sm, l);
+    float* p = sm + T.off[l];
+    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
+  }
 }
 __global__ void __launch_bounds__(TAIL_THREADS, 1) k_tail(TailLevels T, int pre, int post, int coarse) {
   extern __shared__ float sm[];
-  // stage the first tail level's p and b (restriction already wrote them)
-  {
+  pdl_wait();
+  pdl_trigger();
+  const int tid = threadIdx.x;
+  {  // stage the first tail level's p and b (restriction already wrote them)
     const int n0 = T.nx[0] * T.ny[0] * T.nz[0];
     float* p = sm + T.off[0];
     float* b = p + n0;
-    for (int t = threadIdx.x; t < n0; t += blockDim.x) { p[t] = T.gp[0][t]; b[t] = T.gb[0][t]; }
+    for (int t = tid; t < n0; t += TAIL_THREADS) { p[t] = T.gp[0][t]; b[t] = T.gb[0][t]; }
     __syncthreads();
   }
-  const int n = T.n;
-  for (int l = 0; l < n - 1; ++l) {
-    const int nl = T.nx[l] * T.ny[l] * T.nz[l];
-    float* p = sm + T.off[l];
-    float* b = p + nl;
-    tail_smooth(p, b, T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
-    const int cnx = T.nx[l + 1], cny = T.ny[l + 1], cnz = T.nz[l + 1];
-    const int nc = cnx * cny * cnz;
-    float* pc = sm + T.off[l + 1];
-    float* bc = pc + nc;
-    const float ih2 = 1.0f / (T.h[l] * T.h[l]);
-    for (int t = threadIdx.x; t < nc; t += blockDim.x) {
-      const int cx = t % cnx, r = t / cnx, cy = r % cny, cz = r / cny;
-      bc[t] = restrict_cell(p, b, cx, cy, cz, T.nx[l], T.ny[l], T.nz[l], ih2);
-      pc[t] = 0.0f;
+  const Team<false> cta{tid};
+  const int S = T.small;
+  if (S == 0) {
+    if (tid < 32) tail_vcycle(Team<true>{tid}, T, sm, 0, pre, post, coarse);
+    __syncthreads();
+  } else if (S >= T.n) {
+    tail_vcycle(cta, T, sm, 0, pre, post, coarse);
+  } else {
+    // large levels [0, S) with the whole CTA; the V-cycle below S (levels S..n-1) on warp 0
+    for (int l = 0; l < S; ++l) {
+      float* p = sm + T.off[l];
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
+      tail_restrict(cta, T, sm, l);
     }
+    if (tid < 32) tail_vcycle(Team<true>{tid}, T, sm, S, pre, post, coarse);
     __syncthreads();
-  }
-  {
-    const int l = n - 1;
-    const int nl = T.nx[l] * T.ny[l] * T.nz[l];
-    float* p = sm + T.off[l];
-    tail_smooth(p, p + nl, T.nx[l], T.ny[l], T.nz[l], T.h[l], coarse);
-  }
-  for (int l = n - 2; l >= 0; --l) {
-    const int nl = T.nx[l] * T.ny[l] * T.nz[l];
-    float* p = sm + T.off[l];
-    float* b = p + nl;
-    const float* pc = sm + T.off[l + 1];
-    const int nx = T.nx[l], ny = T.ny[l], nz = T.nz[l];
-    for (int t = threadIdx.x; t < nl; t += blockDim.x) {
-      const int x = t % nx, r = t / nx, y = r % ny, z = r / ny;
-      p[t] = p[t] + prolong_cell(pc, x, y, z, nx / 2, ny / 2, nz / 2);
+    for (int l = S - 1; l >= 0; --l) {
+      tail_prolong(cta, T, sm, l);
+      float* p = sm + T.off[l];
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
     }
-    __syncthreads();
-    tail_smooth(p, b, nx, ny, nz, T.h[l], post);
   }
   // write every tail level back (level 0 of the tail feeds the next prolongation)
-  for (int l = 0; l < n; ++l) {
+  for (int l = 0; l < T.n; ++l) {
     const int nl = T.nx[l] * T.ny[l] * T.nz[l];
     const float* p = sm + T.off[l];
-    for (int t = threadIdx.x; t < nl; t += blockDim.x) { T.gp[l][t] = p[t]; T.gb[l][t] = p[nl + t]; }
+    for (int t = tid; t < nl; t += TAIL_THREADS) { T.gp[l][t] = p[t]; T.gb[l][t] = p[nl + t]; }
   }
 }
 
-// ---------------- residual norms ||b - A p||^2 and ||b||^2 (FP64, fixed order) ----------------
-constexpr int RB = 256;
+// ---------------- residual norms ||b - A p||^2 and ||b||^2 (FP64 above the thread, fixed order) ----------------
+constexpr int RB = GX * GY * GZ;
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
+// One partial pair per CTA (3D grid over the level, RZ planes per thread); the CTA index is its slot.
+// The per-cell residual and its square are FP32 (GB300's FP64 rate is a small fraction of FP32; the
+// convergence test needs ~2 digits of the norm); each thread's RZ-cell sum is widened to FP64 and every
+// reduction above the thread is FP64 in a fixed order, so the result is deterministic.
+constexpr int RZ = 4;
 __global__ void __launch_bounds__(RB) k_residual(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
-                                                 float h, double* __restrict__ partials) {
+                                                 float ih2, double* __restrict__ partials) {
   __shared__ double sr[RB / 32], sb[RB / 32];
-  const long long total = (long long)nx * ny * nz;
-  const double ih2 = 1.0 / ((double)h * (double)h);
-  double rr = 0.0, bb = 0.0;
-  for (long long t = (long long)blockIdx.x * RB + threadIdx.x; t < total; t += (long long)gridDim.x * RB) {
-    const int x = (int)(t % nx);
-    const long long r = t / nx;
-    const int y = (int)(r % ny), z = (int)(r / ny);
-    const float me = __ldg(p + t);
-    const double lap = ((double)pghost(p, x - 1, y, z, nx, ny, nz, me) + (double)pghost(p, x + 1, y, z, nx, ny, nz, me) +
-                        (double)pghost(p, x, y - 1, z, nx, ny, nz, me) + (double)pghost(p, x, y + 1, z, nx, ny, nz, me) +
-                        (double)pghost(p, x, y, z - 1, nx, ny, nz, me) + (double)pghost(p, x, y, z + 1, nx, ny, nz, me) -
-                        6.0 * (double)me) * ih2;
-    const double bv = (double)__ldg(b + t);
-    const double res = bv - lap;
-    rr += res * res;
-    bb += bv * bv;
+  pdl_wait();
+  pdl_trigger();
+  const int x = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y;
+  const int tid = threadIdx.x + GX * (threadIdx.y + GY * threadIdx.z);
+  float rrf = 0.0f, bbf = 0.0f;
+  if (x < nx && y < ny) {
+    for (int k = 0; k < RZ; ++k) {
+      const int z = (blockIdx.z * GZ + threadIdx.z) * RZ + k;
+      if (z >= nz) break;
+      const int t = x + nx * (y + ny * z);
+      const float me = __ldg(p + t);
+      const float lap = (pghost(p, x - 1, y, z, nx, ny, nz, me) + pghost(p, x + 1, y, z, nx, ny, nz, me) +
+                         pghost(p, x, y - 1, z, nx, ny, nz, me) + pghost(p, x, y + 1, z, nx, ny, nz, me) +
+                         pghost(p, x, y, z - 1, nx, ny, nz, me) + pghost(p, x, y, z + 1, nx, ny, nz, me) - 6.0f * me) * ih2;
+      const float bv = __ldg(b + t);
+      const float res = bv - lap;
+      rrf += res * res;
+      bbf += bv * bv;
+    }
   }
-  rr = warp_sum(rr);
-  bb = warp_sum(bb);
-  if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = rr; sb[threadIdx.x >> 5] = bb; }
+  double rr = warp_sum((double)rrf);
+  double bb = warp_sum((double)bbf);
+  if ((tid & 31) == 0) { sr[tid >> 5] = rr; sb[tid >> 5] = bb; }
   __syncthreads();
-  if (threadIdx.x < 32) {
-    rr = threadIdx.x < RB / 32 ? sr[threadIdx.x] : 0.0;
-    bb = threadIdx.x < RB / 32 ? sb[threadIdx.x] : 0.0;
+  if (tid < 32) {
+    rr = tid < RB / 32 ? sr[tid] : 0.0;
+    bb = tid < RB / 32 ? sb[tid] : 0.0;
     rr = warp_sum(rr);
     bb = warp_sum(bb);
-    if (threadIdx.x == 0) { partials[2 * blockIdx.x] = rr; partials[2 * blockIdx.x + 1] = bb; }
+    if (tid == 0) {
+      const int slot = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+      partials[2 * slot] = rr;
+      partials[2 * slot + 1] = bb;
+    }
   }
 }
-// Sums `count` pairs of partials in a fixed order: thread t takes pairs t, t+256, ...; then a tree.
-__global__ void __launch_bounds__(RB) k_sum_pairs(const double* __restrict__ partials, int count, double* __restrict__ out2) {
-  __shared__ double sa[RB / 32], sb[RB / 32];
+// Sums `count` pairs of partials in a fixed order: thread t takes pairs t, t+1024, ...; then a tree.
+constexpr int SUMT = 1024;
+__global__ void __launch_bounds__(SUMT) k_sum_pairs(const double* __restrict__ partials, int count, double* __restrict__ out2) {
+  __shared__ double sa[SUMT / 32], sb[SUMT / 32];
+  pdl_wait();
+  pdl_trigger();
   double a = 0.0, b = 0.0;
-  for (int i = threadIdx.x; i < count; i += RB) { a += partials[2 * i]; b += partials[2 * i + 1]; }
+  for (int i = threadIdx.x; i < count; i += SUMT) { a += partials[2 * i]; b += partials[2 * i + 1]; }
   a = warp_sum(a);
   b = warp_sum(b);
   if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
   __syncthreads();
   if (threadIdx.x < 32) {
-    a = threadIdx.x < RB / 32 ? sa[threadIdx.x] : 0.0;
-    b = threadIdx.x < RB / 32 ? sb[threadIdx.x] : 0.0;
+    a = sa[threadIdx.x];
+    b = sb[threadIdx.x];
     a = warp_sum(a);
     b = warp_sum(b);
     if (threadIdx.x == 0) { out2[0] = a; out2[1] = b; }
@@ -242,19 +358,17 @@ __global__ void __launch_bounds__(RB) k_sum_pairs(const double* __restrict__ par
 }
 
 // ---------------- launchers ----------------
-static inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+static dim3 grid3(int x, int y, int z) { return dim3((x + GX - 1) / GX, (y + GY - 1) / GY, (z + GZ - 1) / GZ); }
+static const dim3 kBlock(GX, GY, GZ);
 
 void launch_smooth(const MGLevel& L, int color, cudaStream_t st) {
-  long long n = (long long)((L.nx + 1) >> 1) * L.ny * L.nz;
-  k_smooth<<<blocks_for(n, MB), MB, 0, st>>>(L.p, L.b, L.nx, L.ny, L.nz, L.h, color);
+  launch_pdl(k_smooth, grid3((L.nx + 1) >> 1, L.ny, L.nz), kBlock, 0, st, L.p, (const float*)L.b, L.nx, L.ny, L.nz, L.h, color);
 }
 void launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
-  long long n = (long long)C.nx * C.ny * C.nz;
-  k_restrict<<<blocks_for(n, MB), MB, 0, st>>>(F.p, F.b, F.nx, F.ny, F.nz, F.h, C.b, C.p);
+  launch_pdl(k_restrict, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (const float*)F.p, (const float*)F.b, F.nx, F.ny, F.nz, F.h, C.b, C.p);
 }
 void launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
-  long long n = (long long)F.nx * F.ny * F.nz;
-  k_prolong<<<blocks_for(n, MB), MB, 0, st>>>(F.p, C.p, F.nx, F.ny, F.nz);
+  launch_pdl(k_prolong, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, F.p, (const float*)C.p, F.nx, F.ny, F.nz);
 }
 size_t tail_smem_bytes(const MGLevel* levels, int first, int n) {
   size_t cells = 0;
@@ -264,6 +378,7 @@ size_t tail_smem_bytes(const MGLevel* levels, int first, int n) {
 void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, cudaStream_t st) {
   TailLevels T;
   T.n = n - first;
+  T.small = T.n;
   int off = 0;
   for (int l = 0; l < T.n; ++l) {
     const MGLevel& L = levels[first + l];
@@ -271,22 +386,22 @@ void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int
     T.off[l] = off;
     off += 2 * L.nx * L.ny * L.nz;
     T.gp[l] = L.p; T.gb[l] = L.b;
+    if (T.small == T.n && L.nx * L.ny * L.nz <= TAIL_WARP_CELLS) T.small = l;
   }
-  size_t smem = (size_t)off * sizeof(float);
-  k_tail<<<1, TAIL_THREADS, smem, st>>>(T, pre, post, coarse);
+  launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), (size_t)off * sizeof(float), st, T, pre, post, coarse);
 }
 cudaError_t mg_configure(size_t max_tail_smem) {
   return cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_tail_smem);
 }
+static dim3 residual_grid(const MGLevel& L) { return grid3(L.nx, L.ny, (L.nz + RZ - 1) / RZ); }
 int residual_partials_count(const MGLevel& L) {
-  long long n = (long long)L.nx * L.ny * L.nz;
-  long long b = (n + RB - 1) / RB;
-  return (int)(b < 1216 ? b : 1216);   // 8 CTAs per SM on 152 SMs
+  dim3 g = residual_grid(L);
+  return (int)(g.x * g.y * g.z);
 }
 void launch_residual(const MGLevel& L, double* partials, double* out2, cudaStream_t st) {
-  int nb = residual_partials_count(L);
-  k_residual<<<nb, RB, 0, st>>>(L.p, L.b, L.nx, L.ny, L.nz, L.h, partials);
-  k_sum_pairs<<<1, RB, 0, st>>>(partials, nb, out2);
+  launch_pdl(k_residual, residual_grid(L), kBlock, 0, st, (const float*)L.p, (const float*)L.b, L.nx, L.ny, L.nz,
+             1.0f / (L.h * L.h), partials);
+  launch_pdl(k_sum_pairs, dim3(1), dim3(SUMT), 0, st, (const double*)partials, residual_partials_count(L), out2);
 }
 
 }  // namespace fire
@@ -297,6 +412,7 @@ namespace fire {
 // residual is above `tol` and fewer than `max_cycles` cycles have run.
 __global__ void k_mg_decide(const double* __restrict__ sums2, double tol, int max_cycles, int* __restrict__ counter,
                             double* __restrict__ rel_out, cudaGraphConditionalHandle h) {
+  pdl_wait();
   if (threadIdx.x != 0) return;
   const int c = counter[0] + 1;
   counter[0] = c;
@@ -308,7 +424,7 @@ __global__ void k_mg_decide(const double* __restrict__ sums2, double tol, int ma
 __global__ void k_mg_counter_reset(int* counter) { if (threadIdx.x == 0) counter[0] = 0; }
 void launch_mg_decide(const double* sums2, double tol, int max_cycles, int* counter, double* rel_out,
                       cudaGraphConditionalHandle h, cudaStream_t st) {
-  k_mg_decide<<<1, 32, 0, st>>>(sums2, tol, max_cycles, counter, rel_out, h);
+  launch_pdl(k_mg_decide, dim3(1), dim3(32), 0, st, sums2, tol, max_cycles, counter, rel_out, h);
 }
 void launch_mg_counter_reset(int* counter, cudaStream_t st) { k_mg_counter_reset<<<1, 32, 0, st>>>(counter); }
 }  // namespace fire

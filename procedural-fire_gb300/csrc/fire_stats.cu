@@ -14,25 +14,28 @@ __device__ __forceinline__ double wsum(double v) { for (int o = 16; o > 0; o >>=
 
 // partial layout per CTA: 4 channels x (min, max, sum, bad)
 __global__ void __launch_bounds__(SB) k_stats(const float4* __restrict__ f, long long n, double* __restrict__ partials) {
+  // Per-cell work is FP32 (min/max are exact in FP32; a thread sums ~a dozen cells), everything above the
+  // thread is FP64 in a fixed order: GB300's FP64 rate is a small fraction of its FP32 rate.
   __shared__ double sh[SB / 32][16];
-  double mn[4], mx[4], sm[4], bd[4];
+  float mn[4], mx[4], sm[4];
+  int bd[4];
 #pragma unroll
-  for (int c = 0; c < 4; ++c) { mn[c] = INFINITY; mx[c] = -INFINITY; sm[c] = 0.0; bd[c] = 0.0; }
+  for (int c = 0; c < 4; ++c) { mn[c] = INFINITY; mx[c] = -INFINITY; sm[c] = 0.0f; bd[c] = 0; }
   for (long long t = (long long)blockIdx.x * SB + threadIdx.x; t < n; t += (long long)gridDim.x * SB) {
     float4 v = __ldg(f + t);
     float a[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      if (!isfinite(a[c])) { bd[c] += 1.0; continue; }
-      mn[c] = fmin(mn[c], (double)a[c]);
-      mx[c] = fmax(mx[c], (double)a[c]);
-      sm[c] += (double)a[c];
+      if (!isfinite(a[c])) { bd[c] += 1; continue; }
+      mn[c] = fminf(mn[c], a[c]);
+      mx[c] = fmaxf(mx[c], a[c]);
+      sm[c] += a[c];
     }
   }
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    double a = wmin(mn[c]), b = wmax(mx[c]), s = wsum(sm[c]), z = wsum(bd[c]);
+    double a = wmin((double)mn[c]), b = wmax((double)mx[c]), s = wsum((double)sm[c]), z = wsum((double)bd[c]);
     if (l == 0) { sh[w][4 * c] = a; sh[w][4 * c + 1] = b; sh[w][4 * c + 2] = s; sh[w][4 * c + 3] = z; }
   }
   __syncthreads();
@@ -62,16 +65,13 @@ __global__ void k_stats_final(const double* __restrict__ partials, int count, lo
 // Heat release rate: Q = sum over cells with q > 0 of 354800 q / T * dx^3 (W), q = S.w * 1e4, T = 293 + 1000 S.x.
 __global__ void __launch_bounds__(SB) k_hrr(const float4* __restrict__ S, long long n, double vol, double* __restrict__ partials) {
   __shared__ double sh[SB / 32];
-  double acc = 0.0;
+  float accf = 0.0f;   // sum of q / T over this thread's cells (FP32); scaled and widened below
   for (long long t = (long long)blockIdx.x * SB + threadIdx.x; t < n; t += (long long)gridDim.x * SB) {
     float4 s = __ldg(S + t);
-    double q = (double)s.w * 1e4;
-    if (q > 0.0) {
-      double T = 293.0 + 1000.0 * (double)s.x;
-      acc += 354800.0 * q / T * vol;
-    }
+    float q = s.w * 1e4f;
+    if (q > 0.0f) accf += q / (293.0f + 1000.0f * s.x);
   }
-  acc = wsum(acc);
+  double acc = wsum((double)accf * 354800.0 * vol);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {

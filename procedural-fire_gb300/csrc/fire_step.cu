@@ -4,13 +4,18 @@
 // the semi-Lagrangian back-trace and the 7-point stencils hit L1.  Fields are dense float4 arrays,
 // x fastest, so every warp reads and writes 512 contiguous bytes per field.
 #include "fire_device.cuh"
+#include "fire_launch.cuh"
 
 namespace fire {
 
 constexpr int BX = 32, BY = 4, BZ = 2;
 
 struct CellId { int i, j, k; bool ok; };
+// Every stencil kernel starts here: wait for the predecessor grid (programmatic dependent launch), let the
+// successor's launch begin, and locate this thread's cell.
 __device__ __forceinline__ CellId cell_id(Dims d) {
+  pdl_wait();
+  pdl_trigger();
   CellId c;
   c.i = blockIdx.x * BX + threadIdx.x;
   c.j = blockIdx.y * BY + threadIdx.y;
@@ -122,18 +127,18 @@ __device__ __forceinline__ float4 noise4(const uint2* __restrict__ tab, f3 q) { 
   float4 t = sample_table(tab, q);
   return make_float4(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f, t.w * 2.0f - 1.0f);
 }
-template <bool kFusedCurl>
-__global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fields f, const uint2* __restrict__ noiseT,
-                                                const uint2* __restrict__ curlT, Dims d) {
-  CellId id = cell_id(d);
-  if (!id.ok) return;
-  const int i = id.i, j = id.j, k = id.k;
+// Per-cell physics of the forces kernel.  `nb` supplies the velY/vorticity neighbourhood: the centre
+// velY value, the centre vorticity, the gradient of |w| from the 6 clamped vorticity taps, and the
+// velY Laplacian (only evaluated when visc > 0).
+template <class Nb>
+__device__ __forceinline__ void forces_cell(const float* __restrict__ P, const Fields& f, const uint2* __restrict__ noiseT,
+                                            const uint2* __restrict__ curlT, Dims d, int i, int j, int k, const Nb& nb) {
   const size_t ci = cell(i, j, k, d.nx, d.ny);
   const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx), I = __ldg(P + P_intensity);
   const float seed = __ldg(P + P_seed), time = __ldg(P + P_time);
   const float* E = P + P_STRIDE;
   f3 p = mk3(__ldg(P + P_ox), __ldg(P + P_oy), __ldg(P + P_oz)) + mk3((float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f) * dx;
-  float4 v4 = __ldg(f.velY + ci);
+  float4 v4 = nb.vel_center();
   f3 v = xyz(v4);
   float4 s = __ldg(f.SY + ci);
   float4 s2 = __ldg(f.S2Y + ci);
@@ -238,12 +243,7 @@ __global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fie
   // ---- hot-gas viscosity (src/sim.js:339-346)
   const float visc = __ldg(P + P_visc);
   if (visc > 0.0f) {
-    f3 lapV = xyz(ldc(f.velY, i + 1, j, k, d)) + xyz(ldc(f.velY, i - 1, j, k, d));
-    lapV = lapV + xyz(ldc(f.velY, i, j + 1, k, d));
-    lapV = lapV + xyz(ldc(f.velY, i, j - 1, k, d));
-    lapV = lapV + xyz(ldc(f.velY, i, j, k + 1, d));
-    lapV = lapV + xyz(ldc(f.velY, i, j, k - 1, d));
-    lapV = lapV - xyz(v4) * 6.0f;
+    f3 lapV = nb.lap_v();
     float nu = visc * 1.5e-5f * powf(fmaxf(T, 293.0f) / 293.0f, 1.7f);
     v = v + lapV * fminf(nu * dt / (dx * dx), 0.15f);
   }
@@ -252,19 +252,8 @@ __global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fie
   const float lam = lamAge > 0.0f ? sstep(0.5f * lamAge, fmaxf(lamAge, 1e-3f), ageF) : 1.0f;
 
   // ---- vorticity confinement (src/sim.js:353-361)
-  float4 wc;
-  f3 g;
-  if (kFusedCurl) {
-    wc = curl_at(f.velY, i, j, k, d);
-    g = mk3(curl_at(f.velY, min(i + 1, d.nx - 1), j, k, d).w - curl_at(f.velY, max(i - 1, 0), j, k, d).w,
-            curl_at(f.velY, i, min(j + 1, d.ny - 1), k, d).w - curl_at(f.velY, i, max(j - 1, 0), k, d).w,
-            curl_at(f.velY, i, j, min(k + 1, d.nz - 1), d).w - curl_at(f.velY, i, j, max(k - 1, 0), d).w);
-  } else {
-    wc = __ldg(f.vort + ci);
-    g = mk3(ldc(f.vort, i + 1, j, k, d).w - ldc(f.vort, i - 1, j, k, d).w,
-            ldc(f.vort, i, j + 1, k, d).w - ldc(f.vort, i, j - 1, k, d).w,
-            ldc(f.vort, i, j, k + 1, d).w - ldc(f.vort, i, j, k - 1, d).w);
-  }
+  const float4 wc = nb.vort_center();
+  const f3 g = nb.grad_w();
   const float gl = len3(g);
   if (gl > 1e-6f) {
     float gate = sstep(450.0f, 900.0f, T) * (1.0f - srcAll) * sstep(0.02f, 0.08f, p.y) * lam;
@@ -314,6 +303,141 @@ __global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fie
   f.S2[ci] = s2;
 }
 
+// Neighbourhood from global memory: either the vorticity field written by the curl stage, or (fused)
+// the 7 vorticity taps recomputed from clamped velY loads.
+template <bool kFusedCurl>
+struct GlobalNb {
+  const Fields& f;
+  Dims d;
+  int i, j, k;
+  __device__ float4 vel_center() const { return __ldg(f.velY + cell(i, j, k, d.nx, d.ny)); }
+  __device__ float4 vort_center() const {
+    return kFusedCurl ? curl_at(f.velY, i, j, k, d) : __ldg(f.vort + cell(i, j, k, d.nx, d.ny));
+  }
+  __device__ f3 grad_w() const {
+    if (kFusedCurl)
+      return mk3(curl_at(f.velY, min(i + 1, d.nx - 1), j, k, d).w - curl_at(f.velY, max(i - 1, 0), j, k, d).w,
+                 curl_at(f.velY, i, min(j + 1, d.ny - 1), k, d).w - curl_at(f.velY, i, max(j - 1, 0), k, d).w,
+                 curl_at(f.velY, i, j, min(k + 1, d.nz - 1), d).w - curl_at(f.velY, i, j, max(k - 1, 0), d).w);
+    return mk3(ldc(f.vort, i + 1, j, k, d).w - ldc(f.vort, i - 1, j, k, d).w,
+               ldc(f.vort, i, j + 1, k, d).w - ldc(f.vort, i, j - 1, k, d).w,
+               ldc(f.vort, i, j, k + 1, d).w - ldc(f.vort, i, j, k - 1, d).w);
+  }
+  __device__ f3 lap_v() const {   // src/sim.js:340-343, same summation order
+    f3 l = xyz(ldc(f.velY, i + 1, j, k, d)) + xyz(ldc(f.velY, i - 1, j, k, d));
+    l = l + xyz(ldc(f.velY, i, j + 1, k, d));
+    l = l + xyz(ldc(f.velY, i, j - 1, k, d));
+    l = l + xyz(ldc(f.velY, i, j, k + 1, d));
+    l = l + xyz(ldc(f.velY, i, j, k - 1, d));
+    return l - xyz(vel_center()) * 6.0f;
+  }
+};
+template <bool kFusedCurl>
+__global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fields f, const uint2* __restrict__ noiseT,
+                                                const uint2* __restrict__ curlT, Dims d) {
+  CellId id = cell_id(d);
+  if (!id.ok) return;
+  GlobalNb<kFusedCurl> nb{f, d, id.i, id.j, id.k};
+  forces_cell(P, f, noiseT, curlT, d, id.i, id.j, id.k, nb);
+}
+
+// ---- z-marching shared-memory variant of curl + forces ----
+// A CTA of 32 x 8 threads owns a 32 x 8 column tile and marches through FZ planes.  Shared memory holds a
+// ring of 5 velY planes (tile + 2-cell halo, clamped to the domain like `ld`) and a ring of 3 vorticity
+// planes (tile + 1-cell halo).  Vorticity at a halo position outside the domain is the vorticity of the
+// clamped position, which is what `ld(vortT, c +- e)` returns.  Each velY value is loaded ~2x per cell
+// (halo overhead) instead of the 42 gathers of the per-cell recompute.
+constexpr int FT_X = 32, FT_Y = 8, FZ = 16;
+constexpr int VX = FT_X + 4, VY = FT_Y + 4;      // velY plane with 2-cell halo
+constexpr int WX = FT_X + 2, WY = FT_Y + 2;      // vorticity plane with 1-cell halo
+// Ring slots are addressed by logical z (z >= -2): velY plane z lives in slot (z + 10) % 5, vorticity
+// plane z in slot (z + 9) % 3.
+__device__ __forceinline__ float4* vslot(float4* vbuf, int z) { return vbuf + ((z + 10) % 5) * (VX * VY); }
+__device__ __forceinline__ float4* wslot(float4* wbuf, int z) { return wbuf + ((z + 9) % 3) * (WX * WY); }
+struct TileNb {
+  const float4 *vm, *v0, *vp;   // velY planes z-1, z, z+1 (VX*VY each)
+  const float4 *wm, *w0, *wp;   // vorticity planes z-1, z, z+1 (WX*WY each)
+  int tx, ty;                   // thread position in the tile
+  __device__ float4 vel_center() const { return v0[(ty + 2) * VX + tx + 2]; }
+  __device__ float4 vort_center() const { return w0[(ty + 1) * WX + tx + 1]; }
+  __device__ f3 grad_w() const {
+    const int c = (ty + 1) * WX + tx + 1;
+    return mk3(w0[c + 1].w - w0[c - 1].w, w0[c + WX].w - w0[c - WX].w, wp[c].w - wm[c].w);
+  }
+  __device__ f3 lap_v() const {   // src/sim.js:340-343, same summation order
+    const int c = (ty + 2) * VX + tx + 2;
+    f3 l = xyz(v0[c + 1]) + xyz(v0[c - 1]);
+    l = l + xyz(v0[c + VX]);
+    l = l + xyz(v0[c - VX]);
+    l = l + xyz(vp[c]);
+    l = l + xyz(vm[c]);
+    return l - xyz(v0[c]) * 6.0f;
+  }
+};
+__device__ __forceinline__ int clampi(int v, int n) { return min(max(v, 0), n - 1); }
+// Loads logical plane z (clamped) of velY for the tile at (x0, y0) into `dst`.
+__device__ __forceinline__ void load_vplane(float4* dst, const float4* __restrict__ velY, int x0, int y0, int z, Dims d) {
+  const int zc = clampi(z, d.nz);
+  for (int t = threadIdx.y * FT_X + threadIdx.x; t < VX * VY; t += FT_X * FT_Y) {
+    const int lx = t % VX, ly = t / VX;
+    dst[t] = __ldg(velY + cell(clampi(x0 + lx - 2, d.nx), clampi(y0 + ly - 2, d.ny), zc, d.nx, d.ny));
+  }
+}
+// Vorticity of logical plane zlog into `dst` (positions clamped to the domain), from the velY ring.  The
+// planes it reads (clamp(zlog) and its clamped z neighbours) are resident in the ring when this is called.
+__device__ __forceinline__ void curl_plane(float4* dst, float4* vbuf, int zlog, int x0, int y0, Dims d) {
+  const int zc = clampi(zlog, d.nz);
+  const float4* PK = vslot(vbuf, clampi(zc - 1, d.nz));
+  const float4* P0 = vslot(vbuf, zc);
+  const float4* PF = vslot(vbuf, clampi(zc + 1, d.nz));
+  for (int t = threadIdx.y * FT_X + threadIdx.x; t < WX * WY; t += FT_X * FT_Y) {
+    const int lx = t % WX, ly = t / WX;
+    // clamp the position to the domain, then express it in tile coordinates (velY tile origin at -2)
+    const int gx = clampi(x0 + lx - 1, d.nx), gy = clampi(y0 + ly - 1, d.ny);
+    const int vx = gx - x0 + 2, vy = gy - y0 + 2;
+    const int xm = clampi(gx - 1, d.nx) - x0 + 2, xp = clampi(gx + 1, d.nx) - x0 + 2;
+    const int ym = clampi(gy - 1, d.ny) - y0 + 2, yp = clampi(gy + 1, d.ny) - y0 + 2;
+    f3 L = xyz(P0[vy * VX + xm]), R = xyz(P0[vy * VX + xp]);
+    f3 B = xyz(P0[ym * VX + vx]), T = xyz(P0[yp * VX + vx]);
+    f3 K = xyz(PK[vy * VX + vx]), F = xyz(PF[vy * VX + vx]);
+    f3 w = mk3((T.z - B.z) - (F.y - K.y), (F.x - K.x) - (R.z - L.z), (R.y - L.y) - (T.x - B.x)) * 0.5f;
+    dst[t] = make_float4(w.x, w.y, w.z, len3(w));
+  }
+}
+__global__ void __launch_bounds__(FT_X * FT_Y) k_forces_tiled(const float* __restrict__ P, Fields f, const uint2* __restrict__ noiseT,
+                                                              const uint2* __restrict__ curlT, Dims d) {
+  extern __shared__ float4 fsm[];
+  pdl_wait();
+  pdl_trigger();
+  float4* vbuf = fsm;                    // 5 * VX * VY
+  float4* wbuf = fsm + 5 * VX * VY;      // 3 * WX * WY
+  const int x0 = blockIdx.x * FT_X, y0 = blockIdx.y * FT_Y, z0 = blockIdx.z * FZ;
+  const int z1 = min(z0 + FZ, d.nz);
+  for (int z = z0 - 2; z <= z0 + 2; ++z) load_vplane(vslot(vbuf, z), f.velY, x0, y0, z, d);
+  __syncthreads();
+  for (int z = z0 - 1; z <= z0 + 1; ++z) curl_plane(wslot(wbuf, z), vbuf, z, x0, y0, d);
+  __syncthreads();
+  const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
+  for (int z = z0; z < z1; ++z) {
+    if (i < d.nx && j < d.ny) {
+      TileNb nb;
+      nb.vm = vslot(vbuf, z - 1); nb.v0 = vslot(vbuf, z); nb.vp = vslot(vbuf, z + 1);
+      nb.wm = wslot(wbuf, z - 1); nb.w0 = wslot(wbuf, z); nb.wp = wslot(wbuf, z + 1);
+      nb.tx = threadIdx.x;
+      nb.ty = threadIdx.y;
+      forces_cell(P, f, noiseT, curlT, d, i, j, z, nb);
+    }
+    if (z + 1 < z1) {
+      __syncthreads();                                   // everyone is done with vorticity plane z - 1
+      load_vplane(vslot(vbuf, z + 3), f.velY, x0, y0, z + 3, d);   // replaces plane z - 2
+      __syncthreads();
+      curl_plane(wslot(wbuf, z + 2), vbuf, z + 2, x0, y0, d);       // replaces vorticity plane z - 1
+      __syncthreads();
+    }
+  }
+}
+constexpr size_t FORCES_TILED_SMEM = sizeof(float4) * (5 * VX * VY + 3 * WX * WY);
+
 // ---------------- divergence minus the expansion target (src/sim.js:399-413) ----------------
 __global__ void __launch_bounds__(256) k_div(const float* __restrict__ P, const float4* __restrict__ velX,
                                              float* __restrict__ b0, Dims d) {
@@ -337,7 +461,7 @@ __device__ __forceinline__ float pr(const float* __restrict__ p, int x, int y, i
   return __ldg(p + cell(x, y, z, d.nx, d.ny));
 }
 __global__ void __launch_bounds__(256) k_project(const float* __restrict__ P, const float4* __restrict__ velX,
-                                                 const float* __restrict__ p0, const float4* __restrict__ geo,
+                                                 const float* __restrict__ p0, const unsigned char* __restrict__ solid,
                                                  float4* __restrict__ vel, Dims d) {
   CellId id = cell_id(d);
   if (!id.ok) return;
@@ -349,7 +473,7 @@ __global__ void __launch_bounds__(256) k_project(const float* __restrict__ P, co
              pr(p0, i, j + 1, k, d, me) - pr(p0, i, j - 1, k, d, me),
              pr(p0, i, j, k + 1, d, me) - pr(p0, i, j, k - 1, d, me)) / (2.0f * dx);
   f3 v = xyz(__ldg(velX + ci)) - g;
-  if (__ldg(&geo[ci].z) > 0.5f) v = mk3(0.0f, 0.0f, 0.0f);
+  if (__ldg(solid + ci)) v = mk3(0.0f, 0.0f, 0.0f);   // geo.b > 0.5
   if (j == 0) v.y = fmaxf(v.y, 0.0f);
   float vl = len3(v);
   if (vl > 20.0f || isnan(vl)) v = isnan(vl) ? mk3(0.0f, 0.0f, 0.0f) : v * 20.0f / vl;
@@ -357,20 +481,27 @@ __global__ void __launch_bounds__(256) k_project(const float* __restrict__ P, co
 }
 
 // ---------------- launchers ----------------
-void launch_adv1(const float* P, Fields f, Dims d, cudaStream_t st) { k_adv1<<<grid_for(d), block_shape(), 0, st>>>(P, f, d); }
-void launch_adv2(const float* P, Fields f, Dims d, cudaStream_t st) { k_adv2<<<grid_for(d), block_shape(), 0, st>>>(P, f, d); }
-void launch_curl(Fields f, Dims d, cudaStream_t st) { k_curl<<<grid_for(d), block_shape(), 0, st>>>(f, d); }
+void launch_adv1(const float* P, Fields f, Dims d, cudaStream_t st) { launch_pdl(k_adv1, grid_for(d), block_shape(), 0, st, P, f, d); }
+void launch_adv2(const float* P, Fields f, Dims d, cudaStream_t st) { launch_pdl(k_adv2, grid_for(d), block_shape(), 0, st, P, f, d); }
+void launch_curl(Fields f, Dims d, cudaStream_t st) { launch_pdl(k_curl, grid_for(d), block_shape(), 0, st, f, d); }
 void launch_forces(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
-  k_forces<true><<<grid_for(d), block_shape(), 0, st>>>(P, f, noise, curl, d);
+  dim3 g((d.nx + FT_X - 1) / FT_X, (d.ny + FT_Y - 1) / FT_Y, (d.nz + FZ - 1) / FZ);
+  launch_pdl(k_forces_tiled, g, dim3(FT_X, FT_Y), FORCES_TILED_SMEM, st, P, f, noise, curl, d);
+}
+void launch_forces_recompute(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
+  launch_pdl(k_forces<true>, grid_for(d), block_shape(), 0, st, P, f, noise, curl, d);
+}
+cudaError_t step_configure() {
+  return cudaFuncSetAttribute(k_forces_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
 }
 void launch_forces_unfused(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
-  k_forces<false><<<grid_for(d), block_shape(), 0, st>>>(P, f, noise, curl, d);
+  launch_pdl(k_forces<false>, grid_for(d), block_shape(), 0, st, P, f, noise, curl, d);
 }
 void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st) {
-  k_div<<<grid_for(d), block_shape(), 0, st>>>(P, f.velX, b0, d);
+  launch_pdl(k_div, grid_for(d), block_shape(), 0, st, P, (const float4*)f.velX, b0, d);
 }
 void launch_project(const float* P, Fields f, const float* p0, Dims d, cudaStream_t st) {
-  k_project<<<grid_for(d), block_shape(), 0, st>>>(P, f.velX, p0, f.geo, f.vel, d);
+  launch_pdl(k_project, grid_for(d), block_shape(), 0, st, P, (const float4*)f.velX, p0, (const unsigned char*)f.solid, f.vel, d);
 }
 
 }  // namespace fire

@@ -100,7 +100,7 @@ __device__ __forceinline__ float sdCapsule(f3 p, f3 a, f3 b, float r) {   // src
   return len3(pa - ba * h) - r;
 }
 __global__ void __launch_bounds__(256) k_geo(const float* __restrict__ P, const float* __restrict__ logs,
-                                             float4* __restrict__ geo, Dims d) {
+                                             float4* __restrict__ geo, unsigned char* __restrict__ solidMask, Dims d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
   if (i >= d.nx || j >= d.ny) return;
   const float dx = P[P_dx];
@@ -128,6 +128,11 @@ __global__ void __launch_bounds__(256) k_geo(const float* __restrict__ P, const 
   bed = bed * bedGain;
   float solid = dmin < -0.5f * dx ? 1.0f : 0.0f;
   geo[cell(i, j, k, d.nx, d.ny)] = make_float4(band, bed, solid, dmin);
+  solidMask[cell(i, j, k, d.nx, d.ny)] = solid > 0.5f ? 1 : 0;
+}
+__global__ void __launch_bounds__(256) k_solid_mask(const float4* __restrict__ geo, unsigned char* __restrict__ solid, long long n) {
+  long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t < n) solid[t] = geo[t].z > 0.5f ? 1 : 0;
 }
 
 void launch_noise_table(uint2* noise, int N, int seed, cudaStream_t st) {
@@ -138,9 +143,13 @@ void launch_curl_table(const uint2* noise, uint2* curl, int N, cudaStream_t st) 
   dim3 b(128), g((N + 127) / 128, N, N);
   k_curltab<<<g, b, 0, st>>>(noise, curl, N);
 }
-void launch_geo(const float* P, const float* logs, float4* geo, Dims d, cudaStream_t st) {
+void launch_geo(const float* P, const float* logs, float4* geo, unsigned char* solid, Dims d, cudaStream_t st) {
   dim3 b(32, 8), g((d.nx + 31) / 32, (d.ny + 7) / 8, d.nz);
-  k_geo<<<g, b, 0, st>>>(P, logs, geo, d);
+  k_geo<<<g, b, 0, st>>>(P, logs, geo, solid, d);
+}
+void launch_solid_mask(const float4* geo, unsigned char* solid, Dims d, cudaStream_t st) {
+  long long n = (long long)d.nx * d.ny * d.nz;
+  k_solid_mask<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(geo, solid, n);
 }
 
 }  // namespace fire

