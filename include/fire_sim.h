@@ -194,8 +194,8 @@ const char* fire_sim_last_error(FireSim* sim);
 int fire_sim_run_stage(FireSim* sim, int stage, float dt, void* stream);
 /* Multigrid pieces on level `level` (1 = smooth colour `arg`, 2 = restrict level -> level+1,
  * 3 = prolong level+1 -> level, 4 = shared-memory V-cycle from `level` to the coarsest level,
- * 5 = `arg` fused red-black sweeps), for kernel-level parity tests (mgSmooth/mgRestrict/mgProlong,
- * src/sim.js:417-495).                                                                              */
+ * 5 = `arg` red-black sweeps, 6 = level-0 residual norms into device scratch without waiting), for
+ * kernel-level parity tests and timing (mgSmooth/mgRestrict/mgProlong, src/sim.js:417-495).        */
 int fire_sim_run_mg(FireSim* sim, int op, int level, int arg, void* stream);
 /* Level arrays (which: 0 = p, 1 = b) of any multigrid level, as float32 host arrays.               */
 int fire_sim_level_io(FireSim* sim, int level, int which, void* host, size_t bytes, int to_device);

@@ -58,8 +58,11 @@ template <class R> inline R fmn(R a, R b) { return std::fmin(a, b); }
 template <class R> inline R fmx(R a, R b) { return std::fmax(a, b); }
 template <class R> inline R clampf(R x, R lo, R hi) { return fmn(fmx(x, lo), hi); }
 template <class R> inline R mixf(R a, R b, R t) { return a * (R(1) - t) + b * t; }
+// WGSL smoothstep (t = clamp((x - e0) / (e1 - e0), 0, 1); t^2 (3 - 2t)), evaluated as (x - e0) * (1 / (e1 - e0)),
+// which is within WGSL's accuracy for smoothstep and is how the CUDA kernels evaluate it.
 template <class R> inline R smoothstep(R e0, R e1, R x) {
-  R t = clampf((x - e0) / (e1 - e0), R(0), R(1));
+  const R inv = R(1) / (e1 - e0);
+  R t = clampf((x - e0) * inv, R(0), R(1));
   return t * t * (R(3) - R(2) * t);
 }
 template <class R> inline R dot3(const V3<R>& a, const V3<R>& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }

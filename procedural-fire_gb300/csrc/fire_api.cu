@@ -235,7 +235,7 @@ void record_vcycle(FireSim* s, cudaStream_t st) {
   const int T = s->tailFirst;
   const int top = std::min(T, n - 1);
   for (int i = 0; i < top; ++i) { record_smooth(s, i, 2, st); launch_restrict(s->levels[i], s->levels[i + 1], st); }
-  if (T < n) launch_tail(s->levels.data(), T, n, 2, 2, s->coarseIters, st);
+  if (T < n) launch_tail(s->levels.data(), T, n, 2, 2, s->coarseIters, s->dCounter + 2, st);
   else record_smooth(s, n - 1, s->coarseIters, st);
   for (int i = top - 1; i >= 0; --i) { launch_prolong(s->levels[i], s->levels[i + 1], st); record_smooth(s, i, 2, st); }
 }
@@ -544,6 +544,13 @@ int fire_sim_sync(FireSim* sim) {
   if (!sim) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));
   CK(cudaDeviceSynchronize());
+  // device-side bounded waits report through counter slot 2 instead of hanging
+  int err = 0;
+  CK(cudaMemcpy(&err, sim->dCounter + 2, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    CK(cudaMemset(sim->dCounter + 2, 0, sizeof(int)));
+    return set_err(sim, FIRE_ERR_CUDA, "a device-side wait timed out (multigrid tail bulk copy)");
+  }
   return FIRE_OK;
 }
 
@@ -791,13 +798,16 @@ int fire_sim_run_mg(FireSim* sim, int op, int level, int arg, void* stream) {
     case 1: if (arg != 0 && arg != 1) return FIRE_ERR_BAD_ARG; launch_smooth(sim->levels[level], arg, st); break;
     case 2: if (level >= n - 1) return FIRE_ERR_BAD_ARG; launch_restrict(sim->levels[level], sim->levels[level + 1], st); break;
     case 3: if (level >= n - 1) return FIRE_ERR_BAD_ARG; launch_prolong(sim->levels[level], sim->levels[level + 1], st); break;
+    case 6:   // level-0 residual norms into the device scratch, asynchronously (timing aid)
+      launch_residual(sim->levels[0], sim->dPartials, sim->dSmall, st);
+      break;
     case 5:   // `arg` red-black sweeps (each = colour 0 then colour 1), as the V-cycle runs them
       if (arg < 1) return FIRE_ERR_BAD_ARG;
       record_smooth(sim, level, arg, st);
       break;
     case 4:   // the shared-memory V-cycle from `level` down, if it fits
       if (tail_smem_bytes(sim->levels.data(), level, n) > TAIL_SMEM_BUDGET) return FIRE_ERR_BAD_ARG;
-      launch_tail(sim->levels.data(), level, n, 2, 2, sim->coarseIters, st);
+      launch_tail(sim->levels.data(), level, n, 2, 2, sim->coarseIters, sim->dCounter + 2, st);
       break;
     default: return FIRE_ERR_BAD_ARG;
   }

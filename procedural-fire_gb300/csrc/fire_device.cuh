@@ -14,10 +14,43 @@ namespace fire {
 
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
 __device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+// smoothstep with t = (x - e0) * (1 / (e1 - e0)): the reciprocal folds to a constant for literal edges, so
+// the ~15 smoothsteps per cell cost no division (well inside WGSL's smoothstep accuracy; the oracle uses
+// the same formula).
 __device__ __forceinline__ float sstep(float e0, float e1, float x) {
-  float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
+  const float inv = 1.0f / (e1 - e0);
+  float t = clampf((x - e0) * inv, 0.0f, 1.0f);
   return t * t * (3.0f - 2.0f * t);
 }
+
+// ---- double-float ("df64") accumulation: value = hi + lo with |lo| <= ulp(hi)/2 ----
+// GB300 executes FP64 on a slow path, so every cross-thread reduction accumulates in pairs of FP32 with
+// error-free TwoSum (~48-bit significand) instead of double; trees run in a fixed order, so results are
+// deterministic.
+struct df64 { float hi, lo; };
+__device__ __forceinline__ df64 df_make(float a) { df64 r; r.hi = a; r.lo = 0.0f; return r; }
+__device__ __forceinline__ df64 df_add(df64 a, df64 b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (b.hi - bb);   // TwoSum error of a.hi + b.hi
+  const float lo = err + (a.lo + b.lo);
+  df64 r;
+  r.hi = s + lo;
+  r.lo = lo - (r.hi - s);
+  return r;
+}
+__device__ __forceinline__ df64 df_shfl_down(df64 v, int o) {
+  df64 r;
+  r.hi = __shfl_down_sync(0xffffffffu, v.hi, o);
+  r.lo = __shfl_down_sync(0xffffffffu, v.lo, o);
+  return r;
+}
+__device__ __forceinline__ df64 df_warp_sum(df64 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = df_add(v, df_shfl_down(v, o));
+  return v;
+}
+__device__ __forceinline__ double df_to_double(df64 v) { return (double)v.hi + (double)v.lo; }
 
 struct f3 { float x, y, z; };
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }

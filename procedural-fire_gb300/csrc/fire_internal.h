@@ -74,7 +74,8 @@ void launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st);
 void launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st);
 // Single-CTA V-cycle over levels [first, n): all level arrays staged in shared memory.
 size_t tail_smem_bytes(const MGLevel* levels, int first, int n);
-void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, cudaStream_t st);
+// `err` receives 1 if the kernel's bounded wait for its bulk copies ran out (the kernel then returns early).
+void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st);
 // Opts the tail kernel into `max_tail_smem` bytes of dynamic shared memory on the current device.
 cudaError_t mg_configure(size_t max_tail_smem);
 constexpr size_t TAIL_SMEM_BUDGET = 200 * 1024;

@@ -10,8 +10,8 @@
 //    32 x 4 x 2 CTAs (32-bit index arithmetic, no integer division); at 128x256x128 the level-0 arrays
 //    (p and b, 33.5 MB) stay resident in the 129 MB L2 across the cycle;
 //  * every level small enough to fit, with all coarser ones, in one CTA's shared memory is solved by a
-//    single-CTA kernel that runs the rest of the V-cycle out of shared memory; levels of <= 1024 cells
-//    inside it run on one warp with __syncwarp, so the coarse sweeps cost no CTA-wide barriers;
+//    single-CTA kernel that runs the rest of the V-cycle out of shared memory; levels of <= 256 cells
+//    inside it run on one warp with __syncwarp, so the coarsest sweeps cost no CTA-wide barriers;
 //  * every kernel uses programmatic dependent launch (fire_launch.cuh) so consecutive launches overlap.
 #include "fire_device.cuh"
 #include "fire_launch.cuh"
@@ -32,7 +32,9 @@ __device__ __forceinline__ float rb_update(const float* p, const float* b, int x
   if (z < nz - 1) sum += p[c + sz]; else diag += 1.0f;
   if (y > 0) sum += p[c - sy]; else diag -= 1.0f;
   if (y < ny - 1) sum += p[c + sy]; else diag += 1.0f;
-  return (sum - h2 * b[c]) / diag;
+  // WGSL's `/` is specified to 2.5 ULP; the fast reciprocal-multiply quotient (<= 2 ULP) keeps the
+  // smoother at a handful of instructions per cell instead of an IEEE division sequence
+  return __fdividef(sum - h2 * b[c], diag);
 }
 __global__ void __launch_bounds__(GX * GY * GZ) k_smooth(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
                                                          float h, int color) {
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(GX * GY * GZ) k_prolong(float* __restrict__ p,
 // correction (exact for indices below 2^24), several times cheaper than integer division.  Levels with
 // at most TAIL_WARP_CELLS cells run on warp 0 alone, synchronised with __syncwarp.
 constexpr int TAIL_THREADS = 1024;
-constexpr int TAIL_WARP_CELLS = 1024;
+constexpr int TAIL_WARP_CELLS = 256;
 constexpr int TAIL_MAX_LEVELS = 12;
 struct TailLevels {
   int n;                       // number of levels in the tail
@@ -176,20 +178,34 @@ struct Team {
   static constexpr int size = kWarp ? 32 : TAIL_THREADS;
   __device__ __forceinline__ void sync() const { if (kWarp) __syncwarp(); else __syncthreads(); }
 };
+// Spreads a team over a box of ax x ay x az items: thread extents (tx, ty, tz) and this thread's start.
+// Each thread then strides through the box in 3D, so no index division happens per item.
+struct Box3 {
+  int tx, ty, tz, x0, y0, z0;
+  __device__ Box3(int size, int rank, int ax, int ay, int az) {
+    tx = min(ax, size);
+    ty = min(ay, size / tx);
+    tz = min(az, size / (tx * ty));
+    x0 = rank % tx;
+    const int r = rank / tx;
+    y0 = r % ty;
+    z0 = r / ty;
+    if (z0 >= tz) z0 = 1 << 30;   // surplus thread: its loops never run (prolongation is read-modify-write)
+  }
+};
 template <bool kWarp>
 __device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters) {
   const int hx = (nx + 1) >> 1;
-  const int total = hx * ny * nz;
   const float h2 = h * h;
-  const FastDiv dhx(hx), dny(ny);
+  const Box3 bx(tm.size, tm.rank, hx, ny, nz);
   for (int it = 0; it < iters; ++it)
     for (int color = 0; color < 2; ++color) {
-      for (int t = tm.rank; t < total; t += tm.size) {
-        const int r = dhx.div(t), gx = t - r * hx;
-        const int z = dny.div(r), y = r - z * ny;
-        const int x = gx * 2 + ((y + z + color) & 1);
-        if (x < nx) p[x + nx * (y + ny * z)] = rb_update(p, b, x, y, z, nx, ny, nz, h2);
-      }
+      for (int z = bx.z0; z < nz; z += bx.tz)
+        for (int y = bx.y0; y < ny; y += bx.ty)
+          for (int gx = bx.x0; gx < hx; gx += bx.tx) {
+            const int x = gx * 2 + ((y + z + color) & 1);
+            if (x < nx) p[x + nx * (y + ny * z)] = rb_update(p, b, x, y, z, nx, ny, nz, h2);
+          }
       tm.sync();
     }
 }
@@ -202,13 +218,14 @@ __device__ void tail_restrict(const Team<kWarp>& tm, const TailLevels& T, float*
   float* pc = sm + T.off[l + 1];
   float* bc = pc + cnx * cny * cnz;
   const float ih2 = 1.0f / (T.h[l] * T.h[l]);
-  const FastDiv dcx(cnx), dcy(cny);
-  for (int t = tm.rank; t < cnx * cny * cnz; t += tm.size) {
-    const int r = dcx.div(t), cx = t - r * cnx;
-    const int cz = dcy.div(r), cy = r - cz * cny;
-    bc[t] = restrict_cell(p, b, cx, cy, cz, nx, ny, nz, ih2);
-    pc[t] = 0.0f;
-  }
+  const Box3 bx(tm.size, tm.rank, cnx, cny, cnz);
+  for (int cz = bx.z0; cz < cnz; cz += bx.tz)
+    for (int cy = bx.y0; cy < cny; cy += bx.ty)
+      for (int cx = bx.x0; cx < cnx; cx += bx.tx) {
+        const int t = cx + cnx * (cy + cny * cz);
+        bc[t] = restrict_cell(p, b, cx, cy, cz, nx, ny, nz, ih2);
+        pc[t] = 0.0f;
+      }
   tm.sync();
 }
 template <bool kWarp>
@@ -216,12 +233,13 @@ __device__ void tail_prolong(const Team<kWarp>& tm, const TailLevels& T, float* 
   const int nx = T.nx[l], ny = T.ny[l], nz = T.nz[l];
   float* p = sm + T.off[l];
   const float* pc = sm + T.off[l + 1];
-  const FastDiv dx_(nx), dy_(ny);
-  for (int t = tm.rank; t < nx * ny * nz; t += tm.size) {
-    const int r = dx_.div(t), x = t - r * nx;
-    const int z = dy_.div(r), y = r - z * ny;
-    p[t] = p[t] + prolong_cell(pc, x, y, z, nx / 2, ny / 2, nz / 2);
-  }
+  const Box3 bx(tm.size, tm.rank, nx, ny, nz);
+  for (int z = bx.z0; z < nz; z += bx.tz)
+    for (int y = bx.y0; y < ny; y += bx.ty)
+      for (int x = bx.x0; x < nx; x += bx.tx) {
+        const int t = x + nx * (y + ny * z);
+        p[t] = p[t] + prolong_cell(pc, x, y, z, nx / 2, ny / 2, nz / 2);
+      }
   tm.sync();
 }
 // V-cycle over tail levels [from, n) with one team (src/sim.js:588-599 restricted to these levels).
@@ -243,16 +261,68 @@ __device__ void tail_vcycle(const Team<kWarp>& tm, const TailLevels& T, float* s
     tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
   }
 }
-__global__ void __launch_bounds__(TAIL_THREADS, 1) k_tail(TailLevels T, int pre, int post, int coarse) {
+// ---- TMA bulk copies between global and shared memory (cp.async.bulk, mbarrier completion) ----
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+// Waits for phase 0 of the barrier with an iteration limit; returns false if the limit was reached.
+__device__ __forceinline__ bool mbar_wait0(uint64_t* bar) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned done;
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(done) : "r"(smem_addr(bar)), "r"(0u) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+// Makes this thread's generic-proxy shared-memory writes visible to the async proxy (TMA); every writing
+// thread runs it before the CTA barrier that precedes a bulk store.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, unsigned bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ bool bulk_ok(const void* g, const void* s, unsigned bytes) {
+  return ((reinterpret_cast<uintptr_t>(g) | reinterpret_cast<uintptr_t>(s) | bytes) & 15u) == 0;
+}
+
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_tail(TailLevels T, int pre, int post, int coarse, int* err) {
   extern __shared__ float sm[];
+  __shared__ alignas(8) uint64_t bar;
   pdl_wait();
   pdl_trigger();
   const int tid = threadIdx.x;
-  {  // stage the first tail level's p and b (restriction already wrote them)
+  {  // stage the first tail level's p and b (restriction already wrote them) with two TMA bulk copies
     const int n0 = T.nx[0] * T.ny[0] * T.nz[0];
     float* p = sm + T.off[0];
     float* b = p + n0;
-    for (int t = tid; t < n0; t += TAIL_THREADS) { p[t] = T.gp[0][t]; b[t] = T.gb[0][t]; }
+    const unsigned bytes = (unsigned)n0 * 4u;
+    const bool bulk = bulk_ok(T.gp[0], p, bytes) && bulk_ok(T.gb[0], b, bytes);
+    if (bulk) {
+      if (tid == 0) {
+        mbar_init(&bar, 1);
+        mbar_expect_tx(&bar, 2u * bytes);
+        bulk_g2s(p, T.gp[0], bytes, &bar);
+        bulk_g2s(b, T.gb[0], bytes, &bar);
+      }
+      __syncthreads();                        // the barrier is initialised before anyone polls it
+      if (!mbar_wait0(&bar)) {                // bounded wait: report and leave instead of hanging
+        if (tid == 0) atomicExch(err, 1);
+        return;
+      }
+    } else {
+      for (int t = tid; t < n0; t += TAIL_THREADS) { p[t] = T.gp[0][t]; b[t] = T.gb[0][t]; }
+    }
     __syncthreads();
   }
   const Team<false> cta{tid};
@@ -277,11 +347,19 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_tail(TailLevels T, int pre,
       tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
     }
   }
-  // write every tail level back (level 0 of the tail feeds the next prolongation)
-  for (int l = 0; l < T.n; ++l) {
-    const int nl = T.nx[l] * T.ny[l] * T.nz[l];
-    const float* p = sm + T.off[l];
-    for (int t = tid; t < nl; t += TAIL_THREADS) { T.gp[l][t] = p[t]; T.gb[l][t] = p[nl + t]; }
+  // write the first tail level's p back (it feeds the next prolongation) with one bulk store; the coarser
+  // tail levels are scratch and stay in shared memory
+  {
+    const int n0 = T.nx[0] * T.ny[0] * T.nz[0];
+    const float* p = sm + T.off[0];
+    const unsigned bytes = (unsigned)n0 * 4u;
+    if (bulk_ok(T.gp[0], p, bytes)) {
+      fence_proxy_async();
+      __syncthreads();
+      if (tid == 0) bulk_s2g(T.gp[0], p, bytes);
+    } else {
+      for (int t = tid; t < n0; t += TAIL_THREADS) T.gp[0][t] = p[t];
+    }
   }
 }
 
@@ -293,22 +371,23 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 // One partial pair per CTA (3D grid over the level, RZ planes per thread); the CTA index is its slot.
-// The per-cell residual and its square are FP32 (GB300's FP64 rate is a small fraction of FP32; the
-// convergence test needs ~2 digits of the norm); each thread's RZ-cell sum is widened to FP64 and every
-// reduction above the thread is FP64 in a fixed order, so the result is deterministic.
+// The per-cell residual and its square are FP32; each thread's RZ-cell sum and every reduction above the
+// thread accumulate in double-float (df64, fire_device.cuh) in a fixed order, so the result is
+// deterministic and carries ~48 bits without FP64 instructions.  Partials: float4 (rr.hi, rr.lo, bb.hi, bb.lo).
 constexpr int RZ = 4;
 __global__ void __launch_bounds__(RB) k_residual(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
-                                                 float ih2, double* __restrict__ partials) {
-  __shared__ double sr[RB / 32], sb[RB / 32];
+                                                 float ih2, float4* __restrict__ partials) {
+  __shared__ df64 sr[RB / 32], sb[RB / 32];
   pdl_wait();
   pdl_trigger();
   const int x = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y;
   const int tid = threadIdx.x + GX * (threadIdx.y + GY * threadIdx.z);
-  float rrf = 0.0f, bbf = 0.0f;
+  float rrf = 0.0f, bbf = 0.0f;   // this thread's RZ cells in FP32, widened to df64 once below
   if (x < nx && y < ny) {
-    for (int k = 0; k < RZ; ++k) {
+#pragma unroll
+    for (int k = 0; k < RZ; ++k) {   // unrolled without early exit: all RZ cells' loads are in flight together
       const int z = (blockIdx.z * GZ + threadIdx.z) * RZ + k;
-      if (z >= nz) break;
+      if (z >= nz) continue;
       const int t = x + nx * (y + ny * z);
       const float me = __ldg(p + t);
       const float lap = (pghost(p, x - 1, y, z, nx, ny, nz, me) + pghost(p, x + 1, y, z, nx, ny, nz, me) +
@@ -320,40 +399,39 @@ __global__ void __launch_bounds__(RB) k_residual(const float* __restrict__ p, co
       bbf += bv * bv;
     }
   }
-  double rr = warp_sum((double)rrf);
-  double bb = warp_sum((double)bbf);
+  df64 rr = df_warp_sum(df_make(rrf));
+  df64 bb = df_warp_sum(df_make(bbf));
   if ((tid & 31) == 0) { sr[tid >> 5] = rr; sb[tid >> 5] = bb; }
   __syncthreads();
   if (tid < 32) {
-    rr = tid < RB / 32 ? sr[tid] : 0.0;
-    bb = tid < RB / 32 ? sb[tid] : 0.0;
-    rr = warp_sum(rr);
-    bb = warp_sum(bb);
-    if (tid == 0) {
-      const int slot = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-      partials[2 * slot] = rr;
-      partials[2 * slot + 1] = bb;
-    }
+    rr = tid < RB / 32 ? sr[tid] : df_make(0.0f);
+    bb = tid < RB / 32 ? sb[tid] : df_make(0.0f);
+    rr = df_warp_sum(rr);
+    bb = df_warp_sum(bb);
+    if (tid == 0) partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = make_float4(rr.hi, rr.lo, bb.hi, bb.lo);
   }
 }
-// Sums `count` pairs of partials in a fixed order: thread t takes pairs t, t+1024, ...; then a tree.
+// Sums `count` partial pairs in a fixed order (thread t takes t, t+1024, ...; then a fixed tree), in df64;
+// out2 = (||r||^2, ||b||^2) as doubles.
 constexpr int SUMT = 1024;
-__global__ void __launch_bounds__(SUMT) k_sum_pairs(const double* __restrict__ partials, int count, double* __restrict__ out2) {
-  __shared__ double sa[SUMT / 32], sb[SUMT / 32];
+__global__ void __launch_bounds__(SUMT) k_sum_pairs(const float4* __restrict__ partials, int count, double* __restrict__ out2) {
+  __shared__ df64 sa[SUMT / 32], sb[SUMT / 32];
   pdl_wait();
   pdl_trigger();
-  double a = 0.0, b = 0.0;
-  for (int i = threadIdx.x; i < count; i += SUMT) { a += partials[2 * i]; b += partials[2 * i + 1]; }
-  a = warp_sum(a);
-  b = warp_sum(b);
+  df64 a = df_make(0.0f), b = df_make(0.0f);
+  for (int i = threadIdx.x; i < count; i += SUMT) {
+    const float4 q = partials[i];
+    a = df_add(a, df64{q.x, q.y});
+    b = df_add(b, df64{q.z, q.w});
+  }
+  a = df_warp_sum(a);
+  b = df_warp_sum(b);
   if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
   __syncthreads();
   if (threadIdx.x < 32) {
-    a = sa[threadIdx.x];
-    b = sb[threadIdx.x];
-    a = warp_sum(a);
-    b = warp_sum(b);
-    if (threadIdx.x == 0) { out2[0] = a; out2[1] = b; }
+    a = df_warp_sum(sa[threadIdx.x]);
+    b = df_warp_sum(sb[threadIdx.x]);
+    if (threadIdx.x == 0) { out2[0] = df_to_double(a); out2[1] = df_to_double(b); }
   }
 }
 
@@ -375,7 +453,7 @@ size_t tail_smem_bytes(const MGLevel* levels, int first, int n) {
   for (int l = first; l < n; ++l) cells += (size_t)levels[l].nx * levels[l].ny * levels[l].nz;
   return cells * 2 * sizeof(float);
 }
-void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, cudaStream_t st) {
+void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st) {
   TailLevels T;
   T.n = n - first;
   T.small = T.n;
@@ -388,7 +466,7 @@ void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int
     T.gp[l] = L.p; T.gb[l] = L.b;
     if (T.small == T.n && L.nx * L.ny * L.nz <= TAIL_WARP_CELLS) T.small = l;
   }
-  launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), (size_t)off * sizeof(float), st, T, pre, post, coarse);
+  launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), (size_t)off * sizeof(float), st, T, pre, post, coarse, err);
 }
 cudaError_t mg_configure(size_t max_tail_smem) {
   return cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_tail_smem);
@@ -399,9 +477,10 @@ int residual_partials_count(const MGLevel& L) {
   return (int)(g.x * g.y * g.z);
 }
 void launch_residual(const MGLevel& L, double* partials, double* out2, cudaStream_t st) {
+  float4* part4 = reinterpret_cast<float4*>(partials);   // 16 bytes per CTA (the buffer holds 128 per CTA)
   launch_pdl(k_residual, residual_grid(L), kBlock, 0, st, (const float*)L.p, (const float*)L.b, L.nx, L.ny, L.nz,
-             1.0f / (L.h * L.h), partials);
-  launch_pdl(k_sum_pairs, dim3(1), dim3(SUMT), 0, st, (const double*)partials, residual_partials_count(L), out2);
+             1.0f / (L.h * L.h), part4);
+  launch_pdl(k_sum_pairs, dim3(1), dim3(SUMT), 0, st, (const float4*)part4, residual_partials_count(L), out2);
 }
 
 }  // namespace fire

@@ -9,6 +9,14 @@
 namespace fire {
 
 constexpr int BX = 32, BY = 4, BZ = 2;
+// Minimum resident CTAs per SM requested from the register allocator for the gather-heavy kernels
+// (latency-bound: more resident warps hide more of the dependent back-trace loads).
+#ifndef FIRE_ADV_MIN_CTAS
+#define FIRE_ADV_MIN_CTAS 4
+#endif
+#ifndef FIRE_FORCES_MIN_CTAS
+#define FIRE_FORCES_MIN_CTAS 4
+#endif
 
 struct CellId { int i, j, k; bool ok; };
 // Every stencil kernel starts here: wait for the predecessor grid (programmatic dependent launch), let the
@@ -41,7 +49,7 @@ __device__ __forceinline__ f3 backtrace(const float4* __restrict__ vel, f3 c, f3
 }
 
 // ---------------- adv1 (src/sim.js:142-157) ----------------
-__global__ void __launch_bounds__(256) k_adv1(const float* __restrict__ P, Fields f, Dims d) {
+__global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv1(const float* __restrict__ P, Fields f, Dims d) {
   CellId id = cell_id(d);
   if (!id.ok) return;
   const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx);
@@ -59,7 +67,7 @@ __global__ void __launch_bounds__(256) k_adv1(const float* __restrict__ P, Field
 }
 
 // ---------------- adv2 (src/sim.js:159-197) ----------------
-__global__ void __launch_bounds__(256) k_adv2(const float* __restrict__ P, Fields f, Dims d) {
+__global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv2(const float* __restrict__ P, Fields f, Dims d) {
   CellId id = cell_id(d);
   if (!id.ok) return;
   const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx);
@@ -404,7 +412,7 @@ __device__ __forceinline__ void curl_plane(float4* dst, float4* vbuf, int zlog, 
     dst[t] = make_float4(w.x, w.y, w.z, len3(w));
   }
 }
-__global__ void __launch_bounds__(FT_X * FT_Y) k_forces_tiled(const float* __restrict__ P, Fields f, const uint2* __restrict__ noiseT,
+__global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_tiled(const float* __restrict__ P, Fields f, const uint2* __restrict__ noiseT,
                                                               const uint2* __restrict__ curlT, Dims d) {
   extern __shared__ float4 fsm[];
   pdl_wait();

@@ -339,7 +339,7 @@ class FireSim:
         self._check(self._lib.fire_sim_run_stage(self._h, STAGES[name], float(dt), _stream_handle(stream)), f"stage {name}")
 
     def run_mg(self, op: str, level: int, arg: int = 0, stream=None):
-        code = {"smooth": 1, "restrict": 2, "prolong": 3, "tail": 4, "sweeps": 5}[op]
+        code = {"smooth": 1, "restrict": 2, "prolong": 3, "tail": 4, "sweeps": 5, "residual": 6}[op]
         self._check(self._lib.fire_sim_run_mg(self._h, code, level, arg, _stream_handle(stream)), f"mg {op}")
 
     def level(self, l: int, which: str) -> np.ndarray:
