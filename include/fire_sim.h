@@ -227,6 +227,29 @@ int fire_build_campfire(uint32_t seed, float* out, int max_logs);
  * reference's pcg hash (src/shaders/lib.js:11-18).                                                 */
 int fire_make_spots(uint32_t seed, int n, float flux_lo, float flux_hi, float sigma, float radius, float* out);
 
+/* ---- pressure solve without device allocation --------------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot allocate device memory when they
+ * need a pressure solve - hosts whose device memory belongs to another allocator (a caching or pooled
+ * allocator that must not be bypassed), frame loops that fixed their memory budget up front, or code
+ * recording into a CUDA graph, where cudaMalloc is not allowed.
+ *
+ * Runs `cycles` V(2,2) cycles of the step's multigrid on caller-owned level-0 device arrays: `p` (pressure,
+ * updated in place) and `b` (right-hand side, read only), both nx*ny*nz floats, x fastest; `h` is the cell
+ * size in metres.  The level rules, coarse sweep count and kernels are those of fire_sim_step.  Every coarser
+ * level lives in one file-scope device array of FIRE_NOALLOC_SCRATCH_BYTES that the library holds on every
+ * GPU that loads it until the process exits; nothing is allocated and nothing is freed.
+ *   - The first call on a device (the one current when it is called) sets that device up: it resolves the
+ *     array's device address and opts the coarse-level kernel into its shared memory.  Make that first call
+ *     before any stream capture.
+ *   - Grids whose coarse levels do not fit the array (level-0 grids beyond roughly 7 million cells) are
+ *     rejected with FIRE_ERR_BAD_ARG before any work is queued.
+ *   - All calls share the array and it keeps the last call's contents; each cycle rewrites the coarse
+ *     levels before reading them, so nothing needs clearing between calls.  Calls whose work overlaps on the
+ *     GPU (concurrent streams, or several host threads) race on the array: serialise them.
+ * Asynchronous on `stream` (a cudaStream_t, or NULL).                                                   */
+#define FIRE_NOALLOC_SCRATCH_BYTES (8u * 1024u * 1024u)
+int fire_poisson_vcycles_noalloc(float* p, const float* b, int nx, int ny, int nz, float h, int cycles, void* stream);
+
 /* ---- library ----------------------------------------------------------------------------------- */
 /* 1 if the library's kernels were built for the current device's architecture, else 0.             */
 int fire_device_ok(int device);

@@ -1,0 +1,115 @@
+// Pressure V-cycles on caller-owned arrays with no device allocation.
+//
+// Some callers cannot call cudaMalloc when they need a pressure solve: a host whose device memory is owned
+// by another allocator (a caching or pooled allocator that must not be bypassed), a frame loop that has
+// fixed its memory budget up front, or code that is recording work into a CUDA graph, where allocation is
+// not permitted.  fire_poisson_vcycles_noalloc serves them: the caller passes the level-0 pressure and
+// right-hand side; every coarser multigrid level lives in one file-scope device array of fixed size that
+// the library holds on every GPU that loads it, until the process exits.
+//
+// The V-cycle is the step's own (same kernels, same level rules, same coarse sweep count), so the result
+// equals fire_sim_step's solve on the same arrays.
+#include <cmath>
+#include <cstdint>
+#include <mutex>
+#include <vector>
+#include <algorithm>
+#include "../../include/fire_sim.h"
+#include "fire_internal.h"
+
+namespace fire {
+
+// 8 MiB of scratch: the coarse levels (p and b) of a level-0 grid of up to ~7 million cells.
+constexpr size_t NOALLOC_BYTES = (size_t)FIRE_NOALLOC_SCRATCH_BYTES;
+constexpr size_t NOALLOC_FLAG_BYTES = 256;   // the tail kernel's wait-timeout flag lives at the end
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+namespace {
+struct DeviceSetup {
+  bool ready = false;
+  unsigned char* base = nullptr;   // device address of g_noalloc_scratch on that device
+};
+std::mutex g_setup_mutex;
+DeviceSetup g_setup[64];
+
+// Once per device, with that device current: resolve the array's device address (in host code the
+// symbol name is only a host-side stand-in), opt the tail kernel into its shared memory, clear the flag.
+int setup_device(int dev, unsigned char** base) {
+  if (dev < 0 || dev >= 64) return FIRE_ERR_BAD_ARG;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  DeviceSetup& s = g_setup[dev];
+  if (!s.ready) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || ptr == nullptr) return FIRE_ERR_CUDA;
+    if (mg_configure(TAIL_SMEM_BUDGET) != cudaSuccess) return FIRE_ERR_CUDA;
+    if (cudaMemset(static_cast<unsigned char*>(ptr) + NOALLOC_BYTES - NOALLOC_FLAG_BYTES, 0, NOALLOC_FLAG_BYTES) != cudaSuccess)
+      return FIRE_ERR_CUDA;
+    s.base = static_cast<unsigned char*>(ptr);
+    s.ready = true;
+  }
+  *base = s.base;
+  return FIRE_OK;
+}
+size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+}  // namespace
+}  // namespace fire
+
+using namespace fire;
+
+extern "C" int fire_poisson_vcycles_noalloc(float* p, const float* b, int nx, int ny, int nz, float h, int cycles, void* stream) {
+  if (!p || !b || nx < 2 || ny < 2 || nz < 2 || !(h > 0.0f) || cycles < 0) return FIRE_ERR_BAD_ARG;
+  // level hierarchy and coarse sweep count as the simulation builds them (src/sim.js:79-92)
+  std::vector<MGLevel> levels;
+  {
+    int x = nx, y = ny, z = nz;
+    double hh = h;
+    while (true) {
+      levels.push_back(MGLevel{x, y, z, (float)hh, nullptr, nullptr});
+      if (x % 2 || y % 2 || z % 2 || std::min(x, std::min(y, z)) <= 6) break;
+      x /= 2; y /= 2; z /= 2; hh *= 2;
+    }
+  }
+  const int n = (int)levels.size();
+  size_t need = 0;
+  for (int l = 1; l < n; ++l) need += 2 * align256(sizeof(float) * (size_t)levels[l].nx * levels[l].ny * levels[l].nz);
+  if (need > NOALLOC_BYTES - NOALLOC_FLAG_BYTES) return FIRE_ERR_BAD_ARG;   // beyond the fixed scratch
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return FIRE_ERR_CUDA;
+  unsigned char* base = nullptr;
+  int rc = setup_device(dev, &base);
+  if (rc) return rc;
+
+  levels[0].p = p;
+  levels[0].b = const_cast<float*>(b);   // read only: smoothing and restriction read b, nothing writes it
+  size_t off = 0;
+  for (int l = 1; l < n; ++l) {
+    const size_t bytes = align256(sizeof(float) * (size_t)levels[l].nx * levels[l].ny * levels[l].nz);
+    levels[l].p = reinterpret_cast<float*>(base + off); off += bytes;
+    levels[l].b = reinterpret_cast<float*>(base + off); off += bytes;
+  }
+  int* err = reinterpret_cast<int*>(base + NOALLOC_BYTES - NOALLOC_FLAG_BYTES);
+  const MGLevel& C = levels.back();
+  const double PI = 3.14159265358979323846;
+  const double mu = (std::cos(PI / C.nx) + std::cos(PI / (2.0 * C.ny)) + std::cos(PI / C.nz)) / 3.0;
+  const int coarse = (int)std::max(8.0, std::min(64.0, std::ceil(std::log(0.05) / std::log(mu * mu))));
+  int T = n;
+  for (int l = n - 1; l >= 0; --l) {
+    if (tail_smem_bytes(levels.data(), l, n) <= TAIL_SMEM_BUDGET) T = l;
+    else break;
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int top = std::min(T, n - 1);
+  for (int c = 0; c < cycles; ++c) {   // V(2,2) (src/sim.js:588-599), as the simulation records it
+    for (int i = 0; i < top; ++i) {
+      for (int k = 0; k < 2; ++k) { launch_smooth(levels[i], 0, st); launch_smooth(levels[i], 1, st); }
+      launch_restrict(levels[i], levels[i + 1], st);
+    }
+    if (T < n) launch_tail(levels.data(), T, n, 2, 2, coarse, err, st);
+    else for (int k = 0; k < coarse; ++k) { launch_smooth(levels[n - 1], 0, st); launch_smooth(levels[n - 1], 1, st); }
+    for (int i = top - 1; i >= 0; --i) {
+      launch_prolong(levels[i], levels[i + 1], st);
+      for (int k = 0; k < 2; ++k) { launch_smooth(levels[i], 0, st); launch_smooth(levels[i], 1, st); }
+    }
+  }
+  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+}

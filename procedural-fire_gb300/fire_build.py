@@ -24,6 +24,7 @@ SOURCES = {
     "fire_mg.cu": [],
     "fire_stats.cu": [],
     "fire_api.cu": [],
+    "fire_noalloc.cu": [],
     "fire_scene.cpp": [],
 }
 
