@@ -208,9 +208,9 @@ def cpu_baseline(O, sim_tables, cycles: int, steps: int = 2):
 
 
 def _block(F):
-    """The 200-float block for the workload (as the GPU builds it for the first step)."""
+    """The 208-float block for the workload (uniforms and extension; the oracle ignores the derived slots)."""
     W = WORKLOAD
-    blk = np.zeros(200, np.float32)
+    blk = np.zeros(208, np.float32)
     blk[:64] = F.param_defaults()
     for i, v in enumerate(W["res"]):
         blk[i] = v
@@ -226,7 +226,7 @@ def _block(F):
     spots = F.make_spots(W["spot_seed"], W["spots"], W["flux"][0], W["flux"][1], W["sigma"], W["radius"])
     e[3] = len(spots)
     for i, s in enumerate(spots):
-        e[8 + 8 * i: 8 + 8 * i + 5] = s
+        e[16 + 8 * i: 16 + 8 * i + 5] = s
     return blk
 
 
@@ -329,7 +329,7 @@ def run_ours(args):
                    "mean_vcycles_per_step": cycles, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (fields ~740 MB vs 129 MB L2)"},
         "gcell_updates_per_s": value * cells / 1e9,
-        "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 200 * 4, "d2h_bytes_per_step": 17 * 8},
+        "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 208 * 4, "d2h_bytes_per_step": 17 * 8},
         "gpu_launches": int(round(args.steps * launches_per_step(sim, cycles))),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,

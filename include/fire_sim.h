@@ -141,7 +141,7 @@ int fire_sim_set_param_block(FireSim* sim, const float* block64);
 int fire_sim_get_param_block(FireSim* sim, float* block64);
 /* The block the next step would upload for time step dt (uniforms + extension, FIRE_BLOCK_FLOATS
  * floats): what uploadUniforms writes (src/sim.js:620-624), before this step's event envelopes.     */
-#define FIRE_BLOCK_FLOATS 200
+#define FIRE_BLOCK_FLOATS 208
 int fire_sim_peek_block(FireSim* sim, float dt, float* out);
 /* SIM_FIELDS index of a name, or -1; and the name of an index (src/sim.js:14-23).                   */
 int fire_param_index(const char* name);

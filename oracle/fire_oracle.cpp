@@ -277,8 +277,9 @@ static_assert(P_COUNT == 60, "SIM_FIELDS has 60 entries");
 
 // Build-defined extension block (no counterpart in the reference uniform): soot age gate, coal-bed gain
 // and Gaussian pyrolysis spots.  Layout: [0] sootAge0 [1] sootAge1 [2] bedGain [3] nSpots
-// [4] spotRef (g/s giving unit peak weight) [5..7] pad, then 16 spots x (x, y, z, sigma, flux g/s, 0, 0, 0).
-enum { E_sootAge0 = 0, E_sootAge1, E_bedGain, E_nSpots, E_spotRef, E_SPOTS = 8, E_COUNT = 8 + 16 * 8 };
+// [4] spotRef (g/s giving unit peak weight), [5..15] constants the CUDA host derives per step (the oracle
+// recomputes them where they are used), then from [16] 16 spots x (x, y, z, sigma, flux g/s, 0, 0, 0).
+enum { E_sootAge0 = 0, E_sootAge1, E_bedGain, E_nSpots, E_spotRef, E_SPOTS = 16, E_COUNT = 16 + 16 * 8 };
 
 // ------------------------------------------------------------------------------------------------
 // The simulation state (src/sim.js:48-101)

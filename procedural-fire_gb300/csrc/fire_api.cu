@@ -177,6 +177,19 @@ void fill_block(FireSim* s, float dt, float* out) {
   P[P_ox] = s->origin[0]; P[P_oy] = s->origin[1]; P[P_oz] = s->origin[2];
   P[P_nLogs] = (float)s->nLogs;
   std::memcpy(P + P_STRIDE, s->ext, sizeof(float) * E_COUNT);
+  // per-step constants shared by every cell, evaluated once here in FP32 as the per-cell code would
+  float* E = P + P_STRIDE;
+  E[E_decaySoot] = std::exp(-P[P_sootDissip] * dt);
+  E[E_decayFuel] = std::exp(-P[P_fuelDissip] * dt);
+  E[E_decayVit] = std::exp(-P[P_vitDecay] * dt);
+  E[E_decaySmoke] = std::exp(-P[P_smokeDissip] * dt);
+  E[E_decayVel] = std::exp(-P[P_velDissip] * dt);
+  float top = -1e30f;
+  for (int i = 0; i < (int)E[E_nSpots]; ++i) {
+    const float* sp = E + E_SPOTS + SPOT_STRIDE * i;
+    top = std::max(top, sp[1] + 4.0f * sp[3]);
+  }
+  E[E_spotTop] = top;
 }
 
 void advance_events(FireSim* s, float dt) {

@@ -19,12 +19,19 @@ enum ParamIndex {
 static_assert(P_COUNT == 60, "SIM_FIELDS has 60 entries");
 constexpr int P_STRIDE = 64;
 
-// Extension block appended after the 64-float parameter block (no counterpart in the reference).
-enum ExtIndex { E_sootAge0 = 0, E_sootAge1, E_bedGain, E_nSpots, E_spotRef, E_SPOTS = 8 };
+// Extension block appended after the 64-float parameter block (no counterpart in the reference): the soot
+// age gate, coal-bed gain and spots, plus per-step constants the host derives from the uniforms: the five
+// decay factors exp(-k dt) that are the same for every cell (src/sim.js:318, 327-329, 375; computed with the
+// same expf the oracle uses) and the height above which no spot contributes (max spot y + 4 sigma).
+enum ExtIndex {
+  E_sootAge0 = 0, E_sootAge1, E_bedGain, E_nSpots, E_spotRef, E_spotTop,
+  E_decaySoot, E_decayFuel, E_decayVit, E_decaySmoke, E_decayVel,
+  E_SPOTS = 16
+};
 constexpr int MAX_SPOTS = 16;
 constexpr int SPOT_STRIDE = 8;
-constexpr int E_COUNT = E_SPOTS + MAX_SPOTS * SPOT_STRIDE;   // 136
-constexpr int BLOCK_FLOATS = P_STRIDE + E_COUNT;            // 200 floats uploaded per step
+constexpr int E_COUNT = E_SPOTS + MAX_SPOTS * SPOT_STRIDE;   // 144
+constexpr int BLOCK_FLOATS = P_STRIDE + E_COUNT;            // 208 floats uploaded per step
 
 constexpr int TABLE_N = 128;          // noise / curl tables: 128^3 (src/main.js:36-37)
 constexpr int MAX_LOGS = 16;          // packLogs max (src/scene.js:92)

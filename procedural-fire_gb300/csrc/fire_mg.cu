@@ -36,15 +36,34 @@ __device__ __forceinline__ float rb_update(const float* p, const float* b, int x
   // smoother at a handful of instructions per cell instead of an IEEE division sequence
   return __fdividef(sum - h2 * b[c], diag);
 }
+// Each thread updates SMZ cells of one colour, SMZ planes apart in z (unrolled and independent, so their
+// loads are in flight together): the sweep is latency-bound on L2 hits, and fewer, longer CTAs also cut the
+// CTA turnover that leaves warp slots idle.
+#ifndef FIRE_SMOOTH_Z
+#define FIRE_SMOOTH_Z 2
+#endif
+constexpr int SMZ = FIRE_SMOOTH_Z;
 __global__ void __launch_bounds__(GX * GY * GZ) k_smooth(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
                                                          float h, int color) {
   pdl_wait();
   pdl_trigger();
-  const int gx = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y, z = blockIdx.z * GZ + threadIdx.z;
-  if (y >= ny || z >= nz) return;
-  const int x = gx * 2 + ((y + z + color) & 1);
-  if (x >= nx) return;
-  p[x + nx * (y + ny * z)] = rb_update(p, b, x, y, z, nx, ny, nz, h * h);
+  const int gx = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y;
+  const int zb = (blockIdx.z * GZ + threadIdx.z) * SMZ;
+  if (y >= ny) return;
+  const float h2 = h * h;
+  float v[SMZ];
+#pragma unroll
+  for (int k = 0; k < SMZ; ++k) {   // all reads first (a colour's cells never read each other) ...
+    const int z = zb + k;
+    const int x = gx * 2 + ((y + z + color) & 1);
+    if (z < nz && x < nx) v[k] = rb_update(p, b, x, y, z, nx, ny, nz, h2);
+  }
+#pragma unroll
+  for (int k = 0; k < SMZ; ++k) {   // ... then the writes
+    const int z = zb + k;
+    const int x = gx * 2 + ((y + z + color) & 1);
+    if (z < nz && x < nx) p[x + nx * (y + ny * z)] = v[k];
+  }
 }
 
 // ---------------- fused residual + restriction (src/sim.js:439-466) ----------------
@@ -440,7 +459,8 @@ static dim3 grid3(int x, int y, int z) { return dim3((x + GX - 1) / GX, (y + GY 
 static const dim3 kBlock(GX, GY, GZ);
 
 void launch_smooth(const MGLevel& L, int color, cudaStream_t st) {
-  launch_pdl(k_smooth, grid3((L.nx + 1) >> 1, L.ny, L.nz), kBlock, 0, st, L.p, (const float*)L.b, L.nx, L.ny, L.nz, L.h, color);
+  launch_pdl(k_smooth, grid3((L.nx + 1) >> 1, L.ny, (L.nz + SMZ - 1) / SMZ), kBlock, 0, st, L.p, (const float*)L.b, L.nx, L.ny,
+             L.nz, L.h, color);
 }
 void launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
   launch_pdl(k_restrict, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (const float*)F.p, (const float*)F.b, F.nx, F.ny, F.nz, F.h, C.b, C.p);

@@ -138,9 +138,12 @@ __device__ __forceinline__ float4 noise4(const uint2* __restrict__ tab, f3 q) { 
 // Per-cell physics of the forces kernel.  `nb` supplies the velY/vorticity neighbourhood: the centre
 // velY value, the centre vorticity, the gradient of |w| from the 6 clamped vorticity taps, and the
 // velY Laplacian (only evaluated when visc > 0).
+// The cell's own SY, S2Y and geometry values are passed in (the z-marching kernel prefetches them a plane
+// ahead).
 template <class Nb>
 __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const Fields& f, const uint2* __restrict__ noiseT,
-                                            const uint2* __restrict__ curlT, Dims d, int i, int j, int k, const Nb& nb) {
+                                            const uint2* __restrict__ curlT, Dims d, int i, int j, int k, const Nb& nb,
+                                            float4 s, float4 s2, const float4 geo) {
   const size_t ci = cell(i, j, k, d.nx, d.ny);
   const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx), I = __ldg(P + P_intensity);
   const float seed = __ldg(P + P_seed), time = __ldg(P + P_time);
@@ -148,9 +151,6 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   f3 p = mk3(__ldg(P + P_ox), __ldg(P + P_oy), __ldg(P + P_oz)) + mk3((float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f) * dx;
   float4 v4 = nb.vel_center();
   f3 v = xyz(v4);
-  float4 s = __ldg(f.SY + ci);
-  float4 s2 = __ldg(f.S2Y + ci);
-  float4 geo = __ldg(f.geo + ci);
 
   // ---- sources: pyrolysis on the hot log surfaces + the coal bed (src/sim.js:246-284)
   float src = 0.0f, anchor = 0.0f;
@@ -166,7 +166,7 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   }
   // Gaussian pyrolysis spots (build-defined extension; none by default)
   const int nSpots = (int)__ldg(E + E_nSpots);
-  if (nSpots > 0) {
+  if (nSpots > 0 && p.y < __ldg(E + E_spotTop)) {   // above every spot's 4-sigma reach the sum is exactly 0
     const float spotRef = __ldg(E + E_spotRef);
     float acc = 0.0f;
     for (int q = 0; q < nSpots; ++q) {
@@ -195,7 +195,9 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   s2.y = s2.y * (1.0f - srcAll);
   s2.x = fmaxf(s2.x, (1.0f - s.y) * srcW);
   s2.x = fmaxf(s2.x, (1.0f - s.y) * bed * 0.6f);
-  float wsrc = 1.0f - powf(1.0f - clampf(srcW + bed * 0.4f, 0.0f, 1.0f) * 0.5f, dt * 90.0f);
+  // pow(1, y) = 1 exactly, so cells without a source skip the pow (here and for the sponge/top factors below)
+  const float wsa = clampf(srcW + bed * 0.4f, 0.0f, 1.0f);
+  float wsrc = wsa > 0.0f ? 1.0f - powf(1.0f - wsa * 0.5f, dt * 90.0f) : 0.0f;
   v.y = mixf(v.y, fmaxf(v.y, __ldg(P + P_srcVel)), wsrc);
   s2.z += geo.x * (1.0f - anchor) * __ldg(P + P_smolder) * dt * I;
 
@@ -231,7 +233,7 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   s.z += __ldg(P + P_sootForm) * b * sstep(__ldg(E + E_sootAge0), __ldg(E + E_sootAge1), ageF) * sstep(1000.0f, 1400.0f, T) * (1.0f - s2.w);
   s.z *= expf(-sootOx * (0.25f + o) * sstep(1100.0f, 1400.0f, T) * dt);
   s.z *= expf(-sootOx * 0.5f * o * sstep(850.0f, 1100.0f, T) * (1.0f - sstep(1100.0f, 1300.0f, T)) * dt);
-  s.z *= expf(-__ldg(P + P_sootDissip) * dt);
+  s.z *= __ldg(E + E_decaySoot);   // exp(-sootDissip dt), the same for every cell (host-evaluated)
 
   // ---- cooling (src/sim.js:321-330)
   const float th = T * 0.001f;
@@ -240,9 +242,9 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   T = 293.0f + fmaxf(T - 293.0f, 0.0f) * expf(-__ldg(P + P_coolRate) * notBurning * dt);
   s.x = (T - 293.0f) * 0.001f;
   s.w = q * 1e-4f;
-  s.y *= expf(-__ldg(P + P_fuelDissip) * dt);
-  s2.x *= expf(-__ldg(P + P_vitDecay) * dt);
-  s2.z *= expf(-__ldg(P + P_smokeDissip) * dt);
+  s.y *= __ldg(E + E_decayFuel);    // exp(-fuelDissip dt)
+  s2.x *= __ldg(E + E_decayVit);    // exp(-vitDecay dt)
+  s2.z *= __ldg(E + E_decaySmoke);  // exp(-smokeDissip dt)
   s2.y = ageF * clampf(s.y + s2.x, 0.0f, 1.0f);
 
   // ---- buoyancy (src/sim.js:333)
@@ -280,7 +282,7 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   const float windK = sstep(0.05f, 0.5f, p.y) * (1.0f + __ldg(P + P_gust));
   v.x += (windX * windK - v.x) * dt * 0.35f * windK;
   v.z += (windZ * windK - v.z) * dt * 0.35f * windK;
-  v = v * expf(-__ldg(P + P_velDissip) * dt);
+  v = v * __ldg(E + E_decayVel);    // exp(-velDissip dt)
 
   // ---- solids & sponge layers (src/sim.js:378-388)
   if (geo.z > 0.5f) { v = mk3(0.0f, 0.0f, 0.0f); s.y = 0.0f; s2.y = 0.0f; }
@@ -289,11 +291,12 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   float sp = (1.0f - sstep(0.0f, 5.0f, side)) * __ldg(P + P_sponge);
   float wsy = sstep(0.03f, 0.4f, p.y);
   float wSx = windX * wsy, wSz = windZ * wsy;
-  float ks = 1.0f - powf(1.0f - 0.15f * clampf(sp, 0.0f, 1.0f), dt * 90.0f);
+  const float spc = clampf(sp, 0.0f, 1.0f);
+  float ks = spc > 0.0f ? 1.0f - powf(1.0f - 0.15f * spc, dt * 90.0f) : 0.0f;
   v.x = mixf(v.x, wSx, ks);
   v.z = mixf(v.z, wSz, ks);
   float top = sstep((float)d.ny - 10.0f, (float)d.ny, fp.y);
-  float kt = powf(1.0f - 0.1f * top, dt * 90.0f);
+  float kt = top > 0.0f ? powf(1.0f - 0.1f * top, dt * 90.0f) : 1.0f;
   s.z *= kt;
   s2.z *= kt;
 
@@ -346,7 +349,8 @@ __global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fie
   CellId id = cell_id(d);
   if (!id.ok) return;
   GlobalNb<kFusedCurl> nb{f, d, id.i, id.j, id.k};
-  forces_cell(P, f, noiseT, curlT, d, id.i, id.j, id.k, nb);
+  const size_t ci = cell(id.i, id.j, id.k, d.nx, d.ny);
+  forces_cell(P, f, noiseT, curlT, d, id.i, id.j, id.k, nb, __ldg(f.SY + ci), __ldg(f.S2Y + ci), __ldg(f.geo + ci));
 }
 
 // ---- z-marching shared-memory variant of curl + forces ----
@@ -426,14 +430,26 @@ __global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_ti
   for (int z = z0 - 1; z <= z0 + 1; ++z) curl_plane(wslot(wbuf, z), vbuf, z, x0, y0, d);
   __syncthreads();
   const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
+  const bool mine = i < d.nx && j < d.ny;
+  // this thread's SY, S2Y, geo for the current plane, loaded one plane ahead
+  float4 s_n = make_float4(0.0f, 0.0f, 0.0f, 0.0f), s2_n = s_n, g_n = s_n;
+  if (mine) {
+    const size_t c0 = cell(i, j, z0, d.nx, d.ny);
+    s_n = __ldg(f.SY + c0); s2_n = __ldg(f.S2Y + c0); g_n = __ldg(f.geo + c0);
+  }
   for (int z = z0; z < z1; ++z) {
-    if (i < d.nx && j < d.ny) {
+    const float4 s = s_n, s2 = s2_n, g = g_n;
+    if (mine && z + 1 < z1) {
+      const size_t c1 = cell(i, j, z + 1, d.nx, d.ny);
+      s_n = __ldg(f.SY + c1); s2_n = __ldg(f.S2Y + c1); g_n = __ldg(f.geo + c1);
+    }
+    if (mine) {
       TileNb nb;
       nb.vm = vslot(vbuf, z - 1); nb.v0 = vslot(vbuf, z); nb.vp = vslot(vbuf, z + 1);
       nb.wm = wslot(wbuf, z - 1); nb.w0 = wslot(wbuf, z); nb.wp = wslot(wbuf, z + 1);
       nb.tx = threadIdx.x;
       nb.ty = threadIdx.y;
-      forces_cell(P, f, noiseT, curlT, d, i, j, z, nb);
+      forces_cell(P, f, noiseT, curlT, d, i, j, z, nb, s, s2, g);
     }
     if (z + 1 < z1) {
       __syncthreads();                                   // everyone is done with vorticity plane z - 1

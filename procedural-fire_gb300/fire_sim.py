@@ -264,8 +264,8 @@ class FireSim:
         return {k: float(blk[i]) for i, k in enumerate(SIM_FIELDS)}
 
     def peek_block(self, dt: float) -> np.ndarray:
-        """The 200-float block (SIM_FIELDS uniforms + extension) the next step uploads."""
-        out = np.zeros(200, np.float32)
+        """The 208-float block (SIM_FIELDS uniforms + extension) the next step uploads."""
+        out = np.zeros(208, np.float32)
         self._check(self._lib.fire_sim_peek_block(self._h, float(dt), _ptr(out)), "peek_block")
         return out
 
