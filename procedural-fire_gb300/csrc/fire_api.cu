@@ -49,8 +49,8 @@ const float kParamDefaults[P_STRIDE] = {
 
 // ---- kernels defined in other translation units that the runtime launches directly ----
 cudaError_t kernels_probe();
-void launch_mg_decide(const double* sums2, double tol, int max_cycles, int* counter, double* rel_out,
-                      cudaGraphConditionalHandle h, cudaStream_t st);
+void launch_residual_decide(const MGLevel& L, double* partials, double* sums2, double tol, int max_cycles, int* counter,
+                            double* rel_out, cudaGraphConditionalHandle h, cudaStream_t st);
 void launch_mg_counter_reset(int* counter, cudaStream_t st);
 
 }  // namespace fire
@@ -288,8 +288,8 @@ int record_mg(FireSim* sim, cudaStream_t st) {
   cudaStream_t bs = sim->capStream;
   CK(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   record_vcycle(sim, bs);
-  launch_residual(sim->levels[0], sim->dPartials, sim->dSmall, bs);
-  launch_mg_decide(sim->dSmall, sim->mg_tol, sim->mg_max_cycles, sim->dCounter, sim->dSmall + 19, h, bs);
+  launch_residual_decide(sim->levels[0], sim->dPartials, sim->dSmall, sim->mg_tol, sim->mg_max_cycles, sim->dCounter,
+                         sim->dSmall + 19, h, bs);
   cudaGraph_t outg;
   CK(cudaStreamEndCapture(bs, &outg));
   return FIRE_OK;
@@ -437,11 +437,7 @@ int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSi
     double mu = (std::cos(PI / C.nx) + std::cos(PI / (2.0 * C.ny)) + std::cos(PI / C.nz)) / 3.0;   // src/sim.js:91-92
     sim->coarseIters = (int)std::max(8.0, std::min(64.0, std::ceil(std::log(0.05) / std::log(mu * mu))));
     const int n = (int)sim->levels.size();
-    sim->tailFirst = n;
-    for (int l = n - 1; l >= 0; --l) {
-      if (tail_smem_bytes(sim->levels.data(), l, n) <= TAIL_SMEM_BUDGET) sim->tailFirst = l;
-      else break;
-    }
+    sim->tailFirst = tail_first(sim->levels.data(), n);
   }
 
   // device arena
@@ -819,7 +815,7 @@ int fire_sim_run_mg(FireSim* sim, int op, int level, int arg, void* stream) {
       record_smooth(sim, level, arg, st);
       break;
     case 4:   // the shared-memory V-cycle from `level` down, if it fits
-      if (tail_smem_bytes(sim->levels.data(), level, n) > TAIL_SMEM_BUDGET) return FIRE_ERR_BAD_ARG;
+      if (!tail_fits(sim->levels.data(), level, n)) return FIRE_ERR_BAD_ARG;
       launch_tail(sim->levels.data(), level, n, 2, 2, sim->coarseIters, sim->dCounter + 2, st);
       break;
     default: return FIRE_ERR_BAD_ARG;

@@ -79,11 +79,17 @@ void launch_project(const float* P, Fields f, const float* p0, Dims d, cudaStrea
 void launch_smooth(const MGLevel& L, int color, cudaStream_t st);
 void launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st);
 void launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st);
-// Single-CTA V-cycle over levels [first, n): all level arrays staged in shared memory.
+// One launch runs the V-cycle over levels [first, n) out of shared memory: a single CTA when every level
+// fits in its shared memory, or a thread-block cluster whose CTAs each hold a z-slab of the finer tail
+// levels (distributed shared memory for the slab edges) with the coarsest levels gathered on CTA 0.
+// tail_fits: whether [first, n) can run as one tail launch; tail_first: the finest such `first` (n if none).
+bool tail_fits(const MGLevel* levels, int first, int n);
+int tail_first(const MGLevel* levels, int n);
+// Shared memory per CTA of the tail launch for [first, n).
 size_t tail_smem_bytes(const MGLevel* levels, int first, int n);
 // `err` receives 1 if the kernel's bounded wait for its bulk copies ran out (the kernel then returns early).
 void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st);
-// Opts the tail kernel into `max_tail_smem` bytes of dynamic shared memory on the current device.
+// Opts the tail kernels into `max_tail_smem` bytes of dynamic shared memory on the current device.
 cudaError_t mg_configure(size_t max_tail_smem);
 constexpr size_t TAIL_SMEM_BUDGET = 200 * 1024;
 // Residual / RHS sums of squares on a level: partial sums per CTA then a fixed-order final sum.

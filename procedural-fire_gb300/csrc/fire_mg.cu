@@ -13,6 +13,8 @@
 //    single-CTA kernel that runs the rest of the V-cycle out of shared memory; levels of <= 256 cells
 //    inside it run on one warp with __syncwarp, so the coarsest sweeps cost no CTA-wide barriers;
 //  * every kernel uses programmatic dependent launch (fire_launch.cuh) so consecutive launches overlap.
+#include <cooperative_groups.h>
+
 #include "fire_device.cuh"
 #include "fire_launch.cuh"
 
@@ -280,6 +282,32 @@ __device__ void tail_vcycle(const Team<kWarp>& tm, const TailLevels& T, float* s
     tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
   }
 }
+// The V-cycle over all levels of T with one CTA of TAIL_THREADS threads: levels above T.small with the
+// whole CTA, the rest on warp 0.
+__device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre, int post, int coarse) {
+  const Team<false> cta{tid};
+  const int S = T.small;
+  if (S == 0) {
+    if (tid < 32) tail_vcycle(Team<true>{tid}, T, sm, 0, pre, post, coarse);
+    __syncthreads();
+  } else if (S >= T.n) {
+    tail_vcycle(cta, T, sm, 0, pre, post, coarse);
+  } else {
+    // large levels [0, S) with the whole CTA; the V-cycle below S (levels S..n-1) on warp 0
+    for (int l = 0; l < S; ++l) {
+      float* p = sm + T.off[l];
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
+      tail_restrict(cta, T, sm, l);
+    }
+    if (tid < 32) tail_vcycle(Team<true>{tid}, T, sm, S, pre, post, coarse);
+    __syncthreads();
+    for (int l = S - 1; l >= 0; --l) {
+      tail_prolong(cta, T, sm, l);
+      float* p = sm + T.off[l];
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
+    }
+  }
+}
 // ---- TMA bulk copies between global and shared memory (cp.async.bulk, mbarrier completion) ----
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
@@ -344,28 +372,7 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_tail(TailLevels T, int pre,
     }
     __syncthreads();
   }
-  const Team<false> cta{tid};
-  const int S = T.small;
-  if (S == 0) {
-    if (tid < 32) tail_vcycle(Team<true>{tid}, T, sm, 0, pre, post, coarse);
-    __syncthreads();
-  } else if (S >= T.n) {
-    tail_vcycle(cta, T, sm, 0, pre, post, coarse);
-  } else {
-    // large levels [0, S) with the whole CTA; the V-cycle below S (levels S..n-1) on warp 0
-    for (int l = 0; l < S; ++l) {
-      float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
-      tail_restrict(cta, T, sm, l);
-    }
-    if (tid < 32) tail_vcycle(Team<true>{tid}, T, sm, S, pre, post, coarse);
-    __syncthreads();
-    for (int l = S - 1; l >= 0; --l) {
-      tail_prolong(cta, T, sm, l);
-      float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
-    }
-  }
+  tail_cta_vcycle(T, sm, tid, pre, post, coarse);
   // write the first tail level's p back (it feeds the next prolongation) with one bulk store; the coarser
   // tail levels are scratch and stay in shared memory
   {
@@ -382,6 +389,247 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_tail(TailLevels T, int pre,
   }
 }
 
+// ---------------- cluster tail: the finer tail levels spread over a thread-block cluster ----------------
+// CTA r of a CTAIL_CLUSTER-CTA cluster holds z-planes [r P, (r+1) P) of p and b of every distributed level
+// (P = nz / CTAIL_CLUSTER, even), at the same shared-memory offset in every CTA.  A plane just outside the
+// slab is read from the neighbouring CTA's shared memory through the cluster's distributed shared-memory
+// window, so each colour sweep, restriction and prolongation is one phase closed by a cluster barrier
+// (release/acquire at cluster scope) instead of a kernel launch.  The coarsest levels are gathered on CTA 0:
+// the last distributed restriction writes straight into CTA 0's shared memory, CTA 0 runs them as k_tail
+// does while the other CTAs wait at the barrier, and the prolongation reads them back from CTA 0.
+// Every arithmetic expression is the one of the launch-per-phase kernels above, in the same order.
+#ifndef FIRE_TAIL_CLUSTER
+#define FIRE_TAIL_CLUSTER 8
+#endif
+constexpr int CTAIL_CLUSTER = FIRE_TAIL_CLUSTER;
+constexpr int CTAIL_MIN_CELLS = 512;   // a distributed level gives every CTA at least this many cells
+struct CTailLevels {
+  int nd;                              // the first nd tail levels are distributed
+  int nx[TAIL_MAX_LEVELS], ny[TAIL_MAX_LEVELS], nz[TAIL_MAX_LEVELS], P[TAIL_MAX_LEVELS];
+  float h[TAIL_MAX_LEVELS];
+  int off[TAIL_MAX_LEVELS];            // float offset of the level's p slab in every CTA (its b slab follows)
+  float* gp;                           // global p and b of the first tail level
+  float* gb;
+  TailLevels G;                        // the gathered levels; offsets into CTA 0's shared memory
+};
+namespace cg = cooperative_groups;
+// This CTA's view of one distributed level.
+struct DSlab {
+  int nx, ny, nz, P, z0, plane;
+  float h;
+  float* p;                            // planes z0 .. z0+P-1 of p; b follows at p + P * plane
+};
+__device__ __forceinline__ DSlab make_slab(const CTailLevels& T, int l, unsigned r, float* sm) {
+  DSlab s;
+  s.nx = T.nx[l]; s.ny = T.ny[l]; s.nz = T.nz[l]; s.P = T.P[l];
+  s.z0 = (int)r * s.P;
+  s.plane = s.nx * s.ny;
+  s.h = T.h[l];
+  s.p = sm + T.off[l];
+  return s;
+}
+// Plane z (z0-1 <= z <= z0+P) of p: local, a neighbour CTA's edge plane, or nullptr outside the domain.
+__device__ __forceinline__ const float* dplane(const cg::cluster_group& cl, const DSlab& s, int z, unsigned r) {
+  if (z < 0 || z >= s.nz) return nullptr;
+  if (z < s.z0) return cl.map_shared_rank(s.p + (s.P - 1) * s.plane, (int)r - 1);
+  if (z >= s.z0 + s.P) return cl.map_shared_rank(s.p, (int)r + 1);
+  return s.p + (z - s.z0) * s.plane;
+}
+// rb_update with the z neighbours given as plane pointers (nullptr = domain face).
+__device__ __forceinline__ float rb_update_planes(const float* pl, const float* pm, const float* pu, const float* bm, int x, int y,
+                                                  int nx, int ny, float h2) {
+  const int c = x + y * nx;
+  float sum = 0.0f, diag = 6.0f;
+  if (x > 0) sum += pm[c - 1]; else diag += 1.0f;
+  if (x < nx - 1) sum += pm[c + 1]; else diag += 1.0f;
+  if (pl) sum += pl[c]; else diag += 1.0f;
+  if (pu) sum += pu[c]; else diag += 1.0f;
+  if (y > 0) sum += pm[c - nx]; else diag -= 1.0f;
+  if (y < ny - 1) sum += pm[c + nx]; else diag += 1.0f;
+  return __fdividef(sum - h2 * bm[c], diag);
+}
+__device__ void ct_smooth(const cg::cluster_group& cl, const DSlab& s, unsigned r, int tid, int iters) {
+  const int hx = (s.nx + 1) >> 1;
+  const float h2 = s.h * s.h;
+  const float* b = s.p + s.P * s.plane;
+  const Box3 bx(TAIL_THREADS, tid, hx, s.ny, s.P);
+  for (int it = 0; it < iters; ++it)
+    for (int color = 0; color < 2; ++color) {
+      for (int zl = bx.z0; zl < s.P; zl += bx.tz) {
+        const int z = s.z0 + zl;
+        float* pm = s.p + zl * s.plane;
+        const float* pl = dplane(cl, s, z - 1, r);
+        const float* pu = dplane(cl, s, z + 1, r);
+        const float* bm = b + zl * s.plane;
+        for (int y = bx.y0; y < s.ny; y += bx.ty)
+          for (int gx = bx.x0; gx < hx; gx += bx.tx) {
+            const int x = gx * 2 + ((y + z + color) & 1);
+            if (x < s.nx) pm[x + s.nx * y] = rb_update_planes(pl, pm, pu, bm, x, y, s.nx, s.ny, h2);
+          }
+      }
+      cl.sync();
+    }
+}
+// Fused residual + 8-child restriction of this CTA's slab into coarse planes z0/2 .. z0/2 + P/2 - 1.
+// cp points at coarse plane z0/2 of p (local, or in CTA 0 for a gathered level); b is cb_off floats after p.
+__device__ void ct_restrict(const cg::cluster_group& cl, const DSlab& s, unsigned r, int tid, float* cp, int cb_off) {
+  const int cnx = s.nx / 2, cny = s.ny / 2, cP = s.P / 2, nx = s.nx, ny = s.ny;
+  const float ih2 = 1.0f / (s.h * s.h);
+  const float* b = s.p + s.P * s.plane;
+  const Box3 bx(TAIL_THREADS, tid, cnx, cny, cP);
+  for (int czl = bx.z0; czl < cP; czl += bx.tz) {
+    const int fz = s.z0 + 2 * czl;   // first child plane
+    const float* q[4] = {dplane(cl, s, fz - 1, r), s.p + 2 * czl * s.plane, s.p + (2 * czl + 1) * s.plane, dplane(cl, s, fz + 2, r)};
+    const float* bq[2] = {b + 2 * czl * s.plane, b + (2 * czl + 1) * s.plane};
+    for (int cy = bx.y0; cy < cny; cy += bx.ty)
+      for (int cx = bx.x0; cx < cnx; cx += bx.tx) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int x = 2 * cx + (k & 1), y = 2 * cy + ((k >> 1) & 1), dz = (k >> 2) & 1;
+          const float* pl = q[dz];
+          const float* pm = q[1 + dz];
+          const float* pu = q[2 + dz];
+          const int c = x + nx * y;
+          const float me = pm[c];
+          const float gxm = x > 0 ? pm[c - 1] : -me, gxp = x < nx - 1 ? pm[c + 1] : -me;
+          const float gym = y > 0 ? pm[c - nx] : me, gyp = y < ny - 1 ? pm[c + nx] : -me;
+          const float gzm = pl ? pl[c] : -me, gzp = pu ? pu[c] : -me;
+          const float lap = (gxm + gxp + gym + gyp + gzm + gzp - 6.0f * me) * ih2;
+          acc += bq[dz][c] - lap;
+        }
+        const int t = cx + cnx * (cy + cny * czl);
+        cp[cb_off + t] = acc * 0.125f;
+        cp[t] = 0.0f;
+      }
+  }
+  cl.sync();
+}
+// Coarse source of a prolongation: a distributed level (slab of this CTA) or the gathered level in CTA 0.
+struct CSrc {
+  const float* base;   // distributed: this CTA's slab; gathered: plane 0 in CTA 0 (already mapped)
+  int z0, P, plane;
+  bool dist;
+};
+__device__ __forceinline__ const float* csrc_plane(const cg::cluster_group& cl, const CSrc& c, int cz, unsigned r) {
+  if (!c.dist) return c.base + cz * c.plane;
+  if (cz < c.z0) return cl.map_shared_rank(c.base + (c.P - 1) * c.plane, (int)r - 1);
+  if (cz >= c.z0 + c.P) return cl.map_shared_rank(c.base, (int)r + 1);
+  return c.base + (cz - c.z0) * c.plane;
+}
+// k_prolong's coarse-cell-centric prolongation for the coarse planes over this CTA's fine slab.
+__device__ void ct_prolong(const cg::cluster_group& cl, const DSlab& s, const CSrc& src, unsigned r, int tid) {
+  const int ncx = s.nx / 2, ncy = s.ny / 2, ncz = s.nz / 2, cP = s.P / 2, cz0 = s.z0 / 2, nx = s.nx;
+  const Box3 bx(TAIL_THREADS, tid, ncx, ncy, cP);
+  for (int czl = bx.z0; czl < cP; czl += bx.tz) {
+    const int cz = cz0 + czl;
+    const float* pq[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pq[a] = csrc_plane(cl, src, min(max(cz + a - 1, 0), ncz - 1), r);
+    for (int cy = bx.y0; cy < ncy; cy += bx.ty)
+      for (int cx = bx.x0; cx < ncx; cx += bx.tx) {
+        float v[3][3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const int qx = cx + c - 1, qy = cy + bb - 1, qz = cz + a - 1;
+              float val = pq[a][min(max(qx, 0), ncx - 1) + ncx * min(max(qy, 0), ncy - 1)];
+              if (qx < 0 || qx >= ncx) val = -val;
+              if (qz < 0 || qz >= ncz) val = -val;
+              if (qy >= ncy) val = -val;
+              v[a][bb][c] = val;
+            }
+#pragma unroll
+        for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+          for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+            for (int dx = 0; dx < 2; ++dx) {
+              const float fx = dx ? 0.25f : 0.75f, fy = dy ? 0.25f : 0.75f, fz = dz ? 0.25f : 0.75f;
+              float acc = 0.0f;
+#pragma unroll
+              for (int q = 0; q < 8; ++q) {
+                const int ox = q & 1, oy = (q >> 1) & 1, oz = (q >> 2) & 1;
+                const float wx = ox ? fx : 1.0f - fx, wy = oy ? fy : 1.0f - fy, wz = oz ? fz : 1.0f - fz;
+                acc += v[dz + oz][dy + oy][dx + ox] * wx * wy * wz;
+              }
+              float* pf = s.p + (2 * czl + dz) * s.plane + (2 * cx + dx) + nx * (2 * cy + dy);
+              *pf = *pf + acc;
+            }
+      }
+  }
+  cl.sync();
+}
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_ctail(CTailLevels T, int pre, int post, int coarse) {
+  extern __shared__ float4 sm4[];
+  float* sm = reinterpret_cast<float*>(sm4);
+  const cg::cluster_group cl = cg::this_cluster();
+  const unsigned r = cl.block_rank();
+  const int tid = threadIdx.x;
+  pdl_wait();
+  pdl_trigger();
+  const bool vec = ((reinterpret_cast<uintptr_t>(T.gp) | reinterpret_cast<uintptr_t>(T.gb)) & 15u) == 0;
+  {  // this CTA's slab of the first tail level: one contiguous z-range of p and of b in global memory
+    const DSlab s = make_slab(T, 0, r, sm);
+    const int n = s.P * s.plane;   // a multiple of 4: distributed levels have even nx and ny
+    const size_t g0 = (size_t)s.z0 * s.plane;
+    float* lb = s.p + n;
+    if (vec) {
+      const float4* gp = reinterpret_cast<const float4*>(T.gp + g0);
+      const float4* gb = reinterpret_cast<const float4*>(T.gb + g0);
+      for (int t = tid; t < n / 4; t += TAIL_THREADS) {
+        reinterpret_cast<float4*>(s.p)[t] = gp[t];
+        reinterpret_cast<float4*>(lb)[t] = gb[t];
+      }
+    } else {
+      for (int t = tid; t < n; t += TAIL_THREADS) { s.p[t] = T.gp[g0 + t]; lb[t] = T.gb[g0 + t]; }
+    }
+  }
+  cl.sync();
+  float* g0p = sm + T.G.off[0];
+  float* g0r = r == 0 ? g0p : cl.map_shared_rank(g0p, 0);
+  const int gplane = T.G.nx[0] * T.G.ny[0];
+  const int gcells = gplane * T.G.nz[0];
+  for (int l = 0; l < T.nd; ++l) {
+    const DSlab s = make_slab(T, l, r, sm);
+    ct_smooth(cl, s, r, tid, pre);
+    if (l + 1 < T.nd) {
+      const DSlab c = make_slab(T, l + 1, r, sm);
+      ct_restrict(cl, s, r, tid, c.p, c.P * c.plane);
+    } else {
+      ct_restrict(cl, s, r, tid, g0r + (s.z0 / 2) * gplane, gcells);
+    }
+  }
+  if (r == 0) tail_cta_vcycle(T.G, sm, tid, pre, post, coarse);
+  cl.sync();
+  for (int l = T.nd - 1; l >= 0; --l) {
+    const DSlab s = make_slab(T, l, r, sm);
+    CSrc src;
+    if (l + 1 < T.nd) {
+      const DSlab c = make_slab(T, l + 1, r, sm);
+      src = CSrc{c.p, c.z0, c.P, c.plane, true};
+    } else {
+      src = CSrc{g0r, 0, T.G.nz[0], gplane, false};
+    }
+    ct_prolong(cl, s, src, r, tid);
+    ct_smooth(cl, s, r, tid, post);
+  }
+  {  // the first tail level's p back to global memory (the next prolongation reads it)
+    const DSlab s = make_slab(T, 0, r, sm);
+    const int n = s.P * s.plane;
+    const size_t g0 = (size_t)s.z0 * s.plane;
+    if (vec) {
+      float4* gp = reinterpret_cast<float4*>(T.gp + g0);
+      for (int t = tid; t < n / 4; t += TAIL_THREADS) gp[t] = reinterpret_cast<const float4*>(s.p)[t];
+    } else {
+      for (int t = tid; t < n; t += TAIL_THREADS) T.gp[g0 + t] = s.p[t];
+    }
+  }
+}
+
 // ---------------- residual norms ||b - A p||^2 and ||b||^2 (FP64 above the thread, fixed order) ----------------
 constexpr int RB = GX * GY * GZ;
 __device__ __forceinline__ double warp_sum(double v) {
@@ -393,31 +641,48 @@ __device__ __forceinline__ double warp_sum(double v) {
 // The per-cell residual and its square are FP32; each thread's RZ-cell sum and every reduction above the
 // thread accumulate in double-float (df64, fire_device.cuh) in a fixed order, so the result is
 // deterministic and carries ~48 bits without FP64 instructions.  Partials: float4 (rr.hi, rr.lo, bb.hi, bb.lo).
-constexpr int RZ = 4;
+constexpr int RZ = 8;
+// Sums of r^2 and b^2 over planes z0 .. z0+RZ-1 of column (x, y), r = b - A p with the ghost rules of
+// pghost.  The column is marched in z with the z neighbours carried in registers; the x/y face tests are
+// per column, so a cell costs 6 loads and a handful of selects.
+__device__ __forceinline__ void residual_column(const float* __restrict__ p, const float* __restrict__ b, int x, int y, int z0, int nx,
+                                                int ny, int nz, float ih2, float& rr, float& bb) {
+  const int sy = nx, sz = nx * ny;
+  const bool hxm = x > 0, hxp = x < nx - 1, hym = y > 0, hyp = y < ny - 1;
+  int t = x + sy * y + sz * z0;
+  float prev = z0 > 0 ? __ldg(p + t - sz) : 0.0f;
+  float cur = __ldg(p + t);
+#pragma unroll
+  for (int k = 0; k < RZ; ++k) {
+    const int z = z0 + k;
+    if (z < nz) {
+      const bool hzp = z + 1 < nz;
+      const float next = hzp ? __ldg(p + t + sz) : 0.0f;
+      const float me = cur;
+      const float xm = hxm ? __ldg(p + t - 1) : -me, xp = hxp ? __ldg(p + t + 1) : -me;
+      const float ym = hym ? __ldg(p + t - sy) : me, yp = hyp ? __ldg(p + t + sy) : -me;
+      const float zm = z > 0 ? prev : -me, zp = hzp ? next : -me;
+      const float lap = (xm + xp + ym + yp + zm + zp - 6.0f * me) * ih2;
+      const float bv = __ldg(b + t);
+      const float res = bv - lap;
+      rr += res * res;
+      bb += bv * bv;
+      prev = cur;
+      cur = next;
+      t += sz;
+    }
+  }
+}
 __global__ void __launch_bounds__(RB) k_residual(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
                                                  float ih2, float4* __restrict__ partials) {
   __shared__ df64 sr[RB / 32], sb[RB / 32];
   pdl_wait();
   pdl_trigger();
   const int x = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y;
+  const int z0 = (blockIdx.z * GZ + threadIdx.z) * RZ;
   const int tid = threadIdx.x + GX * (threadIdx.y + GY * threadIdx.z);
   float rrf = 0.0f, bbf = 0.0f;   // this thread's RZ cells in FP32, widened to df64 once below
-  if (x < nx && y < ny) {
-#pragma unroll
-    for (int k = 0; k < RZ; ++k) {   // unrolled without early exit: all RZ cells' loads are in flight together
-      const int z = (blockIdx.z * GZ + threadIdx.z) * RZ + k;
-      if (z >= nz) continue;
-      const int t = x + nx * (y + ny * z);
-      const float me = __ldg(p + t);
-      const float lap = (pghost(p, x - 1, y, z, nx, ny, nz, me) + pghost(p, x + 1, y, z, nx, ny, nz, me) +
-                         pghost(p, x, y - 1, z, nx, ny, nz, me) + pghost(p, x, y + 1, z, nx, ny, nz, me) +
-                         pghost(p, x, y, z - 1, nx, ny, nz, me) + pghost(p, x, y, z + 1, nx, ny, nz, me) - 6.0f * me) * ih2;
-      const float bv = __ldg(b + t);
-      const float res = bv - lap;
-      rrf += res * res;
-      bbf += bv * bv;
-    }
-  }
+  if (x < nx && y < ny && z0 < nz) residual_column(p, b, x, y, z0, nx, ny, nz, ih2, rrf, bbf);
   df64 rr = df_warp_sum(df_make(rrf));
   df64 bb = df_warp_sum(df_make(bbf));
   if ((tid & 31) == 0) { sr[tid >> 5] = rr; sb[tid >> 5] = bb; }
@@ -430,27 +695,80 @@ __global__ void __launch_bounds__(RB) k_residual(const float* __restrict__ p, co
     if (tid == 0) partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = make_float4(rr.hi, rr.lo, bb.hi, bb.lo);
   }
 }
-// Sums `count` partial pairs in a fixed order (thread t takes t, t+1024, ...; then a fixed tree), in df64;
+// Sums `count` partial pairs in a fixed order, in df64, with RB threads standing in for SUMV virtual
+// threads: virtual thread v takes partials v, v+SUMV, ...; each virtual warp is reduced by a warp tree, and
+// the SUMV/32 warp sums by a final warp tree.  The result depends only on `count` and the partials, never on
+// which CTA runs it.  Thread 0 receives (sum of .xy pairs, sum of .zw pairs).  All RB threads must call it.
+constexpr int SUMV = 1024;
+constexpr int SUM_BATCH = 4;   // partials per virtual thread loaded together (4096 partials in one batch)
+__device__ __forceinline__ void sum_pairs_fixed(const float4* partials, int count, int tid, df64* sa, df64* sb, df64& A, df64& B) {
+  constexpr int J = SUMV / RB;
+  df64 a[J], b[J];
+#pragma unroll
+  for (int j = 0; j < J; ++j) { a[j] = df_make(0.0f); b[j] = df_make(0.0f); }
+  for (int i0 = 0; i0 < count; i0 += SUM_BATCH * SUMV) {
+    // all loads of the batch first (they are independent), then the adds in each virtual thread's order
+    float4 q[J][SUM_BATCH];
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+#pragma unroll
+      for (int u = 0; u < SUM_BATCH; ++u) {
+        const int i = i0 + u * SUMV + tid + RB * j;
+        q[j][u] = i < count ? __ldcg(partials + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+#pragma unroll
+      for (int u = 0; u < SUM_BATCH; ++u) {
+        if (i0 + u * SUMV + tid + RB * j < count) {
+          a[j] = df_add(a[j], df64{q[j][u].x, q[j][u].y});
+          b[j] = df_add(b[j], df64{q[j][u].z, q[j][u].w});
+        }
+      }
+  }
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const int v = tid + RB * j;
+    const df64 wa = df_warp_sum(a[j]);
+    const df64 wb = df_warp_sum(b[j]);
+    if ((tid & 31) == 0) { sa[v >> 5] = wa; sb[v >> 5] = wb; }
+  }
+  __syncthreads();
+  if (tid < 32) {
+    A = df_warp_sum(sa[tid]);
+    B = df_warp_sum(sb[tid]);
+  }
+}
 // out2 = (||r||^2, ||b||^2) as doubles.
-constexpr int SUMT = 1024;
-__global__ void __launch_bounds__(SUMT) k_sum_pairs(const float4* __restrict__ partials, int count, double* __restrict__ out2) {
-  __shared__ df64 sa[SUMT / 32], sb[SUMT / 32];
+__global__ void __launch_bounds__(RB) k_sum_pairs(const float4* __restrict__ partials, int count, double* __restrict__ out2) {
+  __shared__ df64 sa[SUMV / 32], sb[SUMV / 32];
   pdl_wait();
   pdl_trigger();
-  df64 a = df_make(0.0f), b = df_make(0.0f);
-  for (int i = threadIdx.x; i < count; i += SUMT) {
-    const float4 q = partials[i];
-    a = df_add(a, df64{q.x, q.y});
-    b = df_add(b, df64{q.z, q.w});
-  }
-  a = df_warp_sum(a);
-  b = df_warp_sum(b);
-  if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    a = df_warp_sum(sa[threadIdx.x]);
-    b = df_warp_sum(sb[threadIdx.x]);
-    if (threadIdx.x == 0) { out2[0] = df_to_double(a); out2[1] = df_to_double(b); }
+  df64 a, b;
+  sum_pairs_fixed(partials, count, threadIdx.x, sa, sb, a, b);
+  if (threadIdx.x == 0) { out2[0] = df_to_double(a); out2[1] = df_to_double(b); }
+}
+// The residual-driven loop's test after k_residual: sums the partials with sum_pairs_fixed (so the norm
+// equals k_residual + k_sum_pairs bit for bit), counts the cycle and sets the WHILE node's condition: loop
+// again while the relative residual is above `tol` and fewer than `max_cycles` cycles have run.
+__global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ partials, int count, double* __restrict__ sums2,
+                                                   double tol, int max_cycles, int* __restrict__ counter,
+                                                   double* __restrict__ rel_out, cudaGraphConditionalHandle h) {
+  __shared__ df64 sa[SUMV / 32], sb[SUMV / 32];
+  pdl_wait();
+  pdl_trigger();
+  df64 A, B;
+  sum_pairs_fixed(partials, count, threadIdx.x, sa, sb, A, B);
+  if (threadIdx.x == 0) {
+    const double s0 = df_to_double(A), s1 = df_to_double(B);
+    sums2[0] = s0;
+    sums2[1] = s1;
+    const int c = counter[0] + 1;
+    counter[0] = c;
+    counter[1] += 1;   // cumulative cycles since creation
+    const double rel = s1 > 0.0 ? sqrt(s0 / s1) : 0.0;
+    rel_out[0] = rel;
+    cudaGraphSetConditional(h, (rel > tol && c < max_cycles) ? 1u : 0u);
   }
 }
 
@@ -468,16 +786,42 @@ void launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
 void launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
   launch_pdl(k_prolong, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, F.p, (const float*)C.p, F.nx, F.ny, F.nz);
 }
-size_t tail_smem_bytes(const MGLevel* levels, int first, int n) {
-  size_t cells = 0;
-  for (int l = first; l < n; ++l) cells += (size_t)levels[l].nx * levels[l].ny * levels[l].nz;
-  return cells * 2 * sizeof(float);
+// Number of leading levels of [first, n) that the cluster tail distributes: each has z-planes for an even
+// number per CTA, at least CTAIL_MIN_CELLS cells per CTA, and a coarser level below it.
+static int tail_dist_levels(const MGLevel* levels, int first, int n) {
+  if (CTAIL_CLUSTER < 2) return 0;
+  int d = 0;
+  for (int l = first; l < n - 1 && d < TAIL_MAX_LEVELS; ++l) {
+    const MGLevel& L = levels[l];
+    const long cells = (long)L.nx * L.ny * L.nz;
+    if (L.nz % (2 * CTAIL_CLUSTER) != 0 || cells < (long)CTAIL_CLUSTER * CTAIL_MIN_CELLS) break;
+    ++d;
+  }
+  return d;
 }
-void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st) {
+size_t tail_smem_bytes(const MGLevel* levels, int first, int n) {
+  const int nd = tail_dist_levels(levels, first, n);
+  size_t floats = 0;
+  for (int l = first; l < n; ++l) {
+    const size_t cells = (size_t)levels[l].nx * levels[l].ny * levels[l].nz;
+    floats += 2 * (l < first + nd ? cells / CTAIL_CLUSTER : cells);
+  }
+  return floats * sizeof(float);
+}
+bool tail_fits(const MGLevel* levels, int first, int n) {
+  return first >= 0 && first < n && n - first - tail_dist_levels(levels, first, n) <= TAIL_MAX_LEVELS &&
+         tail_smem_bytes(levels, first, n) <= TAIL_SMEM_BUDGET;
+}
+int tail_first(const MGLevel* levels, int n) {
+  int first = n;
+  for (int l = n - 1; l >= 0 && tail_fits(levels, l, n); --l) first = l;
+  return first;
+}
+// Levels [first, n) as a TailLevels block whose first level's p starts `off` floats into shared memory.
+static TailLevels make_tail_levels(const MGLevel* levels, int first, int n, int off) {
   TailLevels T;
   T.n = n - first;
   T.small = T.n;
-  int off = 0;
   for (int l = 0; l < T.n; ++l) {
     const MGLevel& L = levels[first + l];
     T.nx[l] = L.nx; T.ny[l] = L.ny; T.nz[l] = L.nz; T.h[l] = L.h;
@@ -486,10 +830,48 @@ void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int
     T.gp[l] = L.p; T.gb[l] = L.b;
     if (T.small == T.n && L.nx * L.ny * L.nz <= TAIL_WARP_CELLS) T.small = l;
   }
-  launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), (size_t)off * sizeof(float), st, T, pre, post, coarse, err);
+  return T;
+}
+void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st) {
+  const size_t smem = tail_smem_bytes(levels, first, n);
+  const int nd = tail_dist_levels(levels, first, n);
+  if (nd == 0) {
+    launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), smem, st, make_tail_levels(levels, first, n, 0), pre, post, coarse, err);
+    return;
+  }
+  CTailLevels T;
+  T.nd = nd;
+  int off = 0;
+  for (int l = 0; l < nd; ++l) {
+    const MGLevel& L = levels[first + l];
+    T.nx[l] = L.nx; T.ny[l] = L.ny; T.nz[l] = L.nz; T.h[l] = L.h;
+    T.P[l] = L.nz / CTAIL_CLUSTER;
+    T.off[l] = off;
+    off += 2 * L.nx * L.ny * T.P[l];
+  }
+  T.gp = levels[first].p;
+  T.gb = levels[first].b;
+  T.G = make_tail_levels(levels, first + nd, n, off);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CTAIL_CLUSTER);
+  cfg.blockDim = dim3(TAIL_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CTAIL_CLUSTER;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 2;
+  cudaLaunchKernelEx(&cfg, k_ctail, T, pre, post, coarse);
 }
 cudaError_t mg_configure(size_t max_tail_smem) {
-  return cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_tail_smem);
+  cudaError_t e = cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_tail_smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_ctail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_tail_smem);
 }
 static dim3 residual_grid(const MGLevel& L) { return grid3(L.nx, L.ny, (L.nz + RZ - 1) / RZ); }
 int residual_partials_count(const MGLevel& L) {
@@ -500,30 +882,22 @@ void launch_residual(const MGLevel& L, double* partials, double* out2, cudaStrea
   float4* part4 = reinterpret_cast<float4*>(partials);   // 16 bytes per CTA (the buffer holds 128 per CTA)
   launch_pdl(k_residual, residual_grid(L), kBlock, 0, st, (const float*)L.p, (const float*)L.b, L.nx, L.ny, L.nz,
              1.0f / (L.h * L.h), part4);
-  launch_pdl(k_sum_pairs, dim3(1), dim3(SUMT), 0, st, (const float4*)part4, residual_partials_count(L), out2);
+  launch_pdl(k_sum_pairs, dim3(1), dim3(RB), 0, st, (const float4*)part4, residual_partials_count(L), out2);
+}
+void launch_residual_decide(const MGLevel& L, double* partials, double* sums2, double tol, int max_cycles, int* counter,
+                            double* rel_out, cudaGraphConditionalHandle h, cudaStream_t st) {
+  float4* part4 = reinterpret_cast<float4*>(partials);
+  launch_pdl(k_residual, residual_grid(L), kBlock, 0, st, (const float*)L.p, (const float*)L.b, L.nx, L.ny, L.nz,
+             1.0f / (L.h * L.h), part4);
+  launch_pdl(k_sum_decide, dim3(1), dim3(RB), 0, st, (const float4*)part4, residual_partials_count(L), sums2, tol, max_cycles,
+             counter, rel_out, h);
 }
 
 }  // namespace fire
 
 // ---------------- residual-driven loop control (conditional WHILE node body tail) ----------------
 namespace fire {
-// sums2 = (||r||^2, ||b||^2) of level 0 after the cycle just run.  Keeps looping while the relative
-// residual is above `tol` and fewer than `max_cycles` cycles have run.
-__global__ void k_mg_decide(const double* __restrict__ sums2, double tol, int max_cycles, int* __restrict__ counter,
-                            double* __restrict__ rel_out, cudaGraphConditionalHandle h) {
-  pdl_wait();
-  if (threadIdx.x != 0) return;
-  const int c = counter[0] + 1;
-  counter[0] = c;
-  counter[1] += 1;   // cumulative cycles since creation
-  const double rel = sums2[1] > 0.0 ? sqrt(sums2[0] / sums2[1]) : 0.0;
-  rel_out[0] = rel;
-  cudaGraphSetConditional(h, (rel > tol && c < max_cycles) ? 1u : 0u);
-}
+// The loop test itself is k_residual_decide (above); this resets the per-step cycle counter before the loop.
 __global__ void k_mg_counter_reset(int* counter) { if (threadIdx.x == 0) counter[0] = 0; }
-void launch_mg_decide(const double* sums2, double tol, int max_cycles, int* counter, double* rel_out,
-                      cudaGraphConditionalHandle h, cudaStream_t st) {
-  launch_pdl(k_mg_decide, dim3(1), dim3(32), 0, st, sums2, tol, max_cycles, counter, rel_out, h);
-}
 void launch_mg_counter_reset(int* counter, cudaStream_t st) { k_mg_counter_reset<<<1, 32, 0, st>>>(counter); }
 }  // namespace fire

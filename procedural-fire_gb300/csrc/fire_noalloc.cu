@@ -92,11 +92,7 @@ extern "C" int fire_poisson_vcycles_noalloc(float* p, const float* b, int nx, in
   const double PI = 3.14159265358979323846;
   const double mu = (std::cos(PI / C.nx) + std::cos(PI / (2.0 * C.ny)) + std::cos(PI / C.nz)) / 3.0;
   const int coarse = (int)std::max(8.0, std::min(64.0, std::ceil(std::log(0.05) / std::log(mu * mu))));
-  int T = n;
-  for (int l = n - 1; l >= 0; --l) {
-    if (tail_smem_bytes(levels.data(), l, n) <= TAIL_SMEM_BUDGET) T = l;
-    else break;
-  }
+  const int T = tail_first(levels.data(), n);
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int top = std::min(T, n - 1);
   for (int c = 0; c < cycles; ++c) {   // V(2,2) (src/sim.js:588-599), as the simulation records it

@@ -150,11 +150,13 @@ def test_rb_sweeps(level, sweeps):
     FC.compare(sim.level(level, "p"), orc.get_level(level, "p"), 1e-5, 1e-6, 0, what=f"sweeps L{level}")
 
 
-@pytest.mark.parametrize("res", [(8, 16, 8), (16, 32, 16), (12, 400, 12), (20, 30, 20)])
+@pytest.mark.parametrize("res", [(8, 16, 8), (16, 32, 16), (12, 400, 12), (20, 30, 20), (32, 64, 32), (48, 32, 32),
+                                 (64, 128, 64)])
 def test_mg_vcycle_tail_shapes(res):
-    """V-cycles whose shared-memory tail has only warp-sized levels (8x16x8), a CTA level above warp levels
-    (16x32x16), only CTA-sized levels (12x400x12: coarsest 6x200x6), and an odd coarsest level (20x30x20 ->
-    10x15x10)."""
+    """V-cycles whose shared-memory tail has only warp-sized levels (8x16x8), only CTA-sized levels (12x400x12:
+    coarsest 6x200x6), an odd coarsest level (20x30x20 -> 10x15x10), and cluster tails: one distributed
+    level over gathered levels (16x32x16), two distributed levels (32x64x32; 48x32x32 with nx not a power of
+    two), and two distributed levels below a launch-per-phase level (64x128x64)."""
     cfg = dict(res=res, size=(0.02 * res[0], 0.02 * res[1], 0.02 * res[2]), dt=0.01, vcycles=2)
     sim, orc = FC.make_pair(cfg)
     rng = np.random.default_rng(sum(res))
