@@ -250,6 +250,55 @@ int fire_make_spots(uint32_t seed, int n, float flux_lo, float flux_hi, float si
 #define FIRE_NOALLOC_SCRATCH_BYTES (8u * 1024u * 1024u)
 int fire_poisson_vcycles_noalloc(float* p, const float* b, int nx, int ny, int nz, float h, int cycles, void* stream);
 
+/* ---- standalone pressure Poisson solver --------------------------------------------------------
+ * The step's pressure equation (src/sim.js:415-495, 576-599: cell-centred 7-point Laplacian, p = 0 on the
+ * side and top faces, zero gradient at the floor, levels halved while every dimension is even and the
+ * smallest exceeds 6) solved on its own to a relative residual ||b - A x||_2 / ||b||_2 <= tol.
+ *   FIRE_POISSON_FP32  the step's V(2,2) cycle (the reference's multigrid, coarseIters coarsest sweeps) on x
+ *                      and b directly, repeated until the tolerance is met (research/webgpu-bench/poisson.mjs
+ *                      iterates the same cycle).  An FP32 x cannot represent the solution to much better
+ *                      than ~1e-5 relative residual on large grids (its rounding alone leaves that much), so
+ *                      this form stalls there.
+ *   FIRE_POISSON_FP16 / FIRE_POISSON_BF16 / FIRE_POISSON_IR32  iterative refinement: the solution is an FP32
+ *                      pair (x, x_lo) updated with error-free additions and the residual is formed from
+ *                      neighbour differences, all in FP32 arithmetic; each correction A e = r is one V(2,2)
+ *                      cycle whose level arrays are stored in IEEE half / bfloat16 / FP32 (arithmetic in FP32
+ *                      registers), with r scaled by the previous residual's RMS so it stays inside half's
+ *                      range, and the coarsest level solved exactly in FP64 (dense inverse; FP64 sweeps when
+ *                      it has more than 512 cells).  These reach 1e-6 and below.
+ * Residual norms and the RHS mean are double-float (FP32 pair) reductions in a fixed order: deterministic,
+ * ~44 significant bits.  The solve loop runs on the device (a CUDA graph with a conditional WHILE node):
+ * fire_poisson_solve queues it on `stream` and returns; fire_poisson_result waits and reports.
+ * No counterpart in the reference as an entry point: it exists there only inside FireSim.step and the
+ * research multigrid benchmarks.                                                                        */
+enum { FIRE_POISSON_FP32 = 0, FIRE_POISSON_FP16 = 1, FIRE_POISSON_BF16 = 2, FIRE_POISSON_IR32 = 3 };
+typedef struct FirePoisson FirePoisson;
+typedef struct {
+  int iterations;              /* V-cycles (FP32) or refinement steps (FP16/BF16) of the last solve     */
+  double rel_residual;         /* ||b - A x|| / ||b|| after the last solve                             */
+  double rel_residual_initial; /* before it                                                             */
+  double b_norm;               /* ||b||_2                                                               */
+} FirePoissonResult;
+/* res: grid (x fastest, then y, then z); h: cell size in metres; device: CUDA ordinal.                  */
+int fire_poisson_create(const int res[3], float h, int precision, int device, FirePoisson** out);
+int fire_poisson_destroy(FirePoisson* ps);
+/* x (in: initial guess, out: solution) and b are device arrays of res[0]*res[1]*res[2] floats, x 16-byte
+ * aligned.  x_lo (refinement forms; may be NULL): the low half of the solution pair, in/out like x; with
+ * NULL the pair starts at (x, 0) and only its rounded sum x is returned.  inner_cycles: V-cycles per
+ * refinement step (1..16; ignored by FIRE_POISSON_FP32, as is x_lo).                                      */
+int fire_poisson_solve(FirePoisson* ps, const float* b, float* x, float* x_lo, double tol, int max_iters, int inner_cycles,
+                       void* stream);
+int fire_poisson_result(FirePoisson* ps, FirePoissonResult* out);
+/* Relative residual of (b, x + x_lo) (x_lo may be NULL), double-float norms; synchronous.                  */
+int fire_poisson_residual(FirePoisson* ps, const float* b, const float* x, const float* x_lo, double* rel);
+/* Seeded zero-mean right-hand side on the device: n_sources Gaussian sources (centres uniform over the
+ * grid, sigma uniform in [1, 4] cells, amplitude standard normal) plus `noise` times per-cell standard
+ * normal noise, then the mean removed.  Asynchronous on `stream`.                                       */
+int fire_poisson_make_rhs(FirePoisson* ps, float* b, unsigned seed, int n_sources, float noise, void* stream);
+/* The sources of fire_poisson_make_rhs as 5 floats each (centre x, y, z in cells, sigma in cells,
+ * amplitude); host only.                                                                                */
+int fire_poisson_sources(unsigned seed, int n_sources, const int res[3], float* out);
+
 /* ---- library ----------------------------------------------------------------------------------- */
 /* 1 if the library's kernels were built for the current device's architecture, else 0.             */
 int fire_device_ok(int device);

@@ -1126,4 +1126,68 @@ double orc_poisson_study(int N, int face, int mode, double omega, int pre, int p
 }
 void orc_poisson_rhs(int N, float* out) { std::vector<float> b = krhs(N); std::memcpy(out, b.data(), b.size() * 4); }
 
+// ---- FP64 reference solution of the step's pressure equation (the operator of k_smooth / k_restrict:
+// sum of the six ghost-ruled neighbours minus 6 p, over h^2; p = 0 on sides and top, zero gradient at the
+// floor, src/sim.js:417-466).  -A is symmetric positive definite, so conjugate gradients apply. ----
+static void op_apply(int nx, int ny, int nz, double ih2, const double* x, double* out) {
+#pragma omp parallel for schedule(static)
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int i = 0; i < nx; ++i) {
+        const size_t c = cidx(i, y, z, nx, ny);
+        const double me = x[c];
+        const double xm = i > 0 ? x[c - 1] : -me, xp = i < nx - 1 ? x[c + 1] : -me;
+        const double ym = y > 0 ? x[c - nx] : me, yp = y < ny - 1 ? x[c + nx] : -me;
+        const double zm = z > 0 ? x[c - (size_t)nx * ny] : -me, zp = z < nz - 1 ? x[c + (size_t)nx * ny] : -me;
+        out[c] = (xm + xp + ym + yp + zm + zp - 6.0 * me) * ih2;
+      }
+}
+static double dotp(const double* a, const double* b, size_t n) {
+  double s = 0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (long long i = 0; i < (long long)n; ++i) s += a[i] * b[i];
+  return s;
+}
+// A x (FP64) for the tests.
+void orc_pressure_apply(int nx, int ny, int nz, double h, const double* x, double* out) { op_apply(nx, ny, nz, 1.0 / (h * h), x, out); }
+// ||b - A x|| / ||b|| in FP64 of FP32 arrays.
+double orc_pressure_rel_residual(int nx, int ny, int nz, double h, const float* b, const float* x) {
+  const size_t n = (size_t)nx * ny * nz;
+  std::vector<double> xd(x, x + n), ax(n);
+  op_apply(nx, ny, nz, 1.0 / (h * h), xd.data(), ax.data());
+  double rr = 0, bb = 0;
+#pragma omp parallel for reduction(+ : rr, bb) schedule(static)
+  for (long long i = 0; i < (long long)n; ++i) {
+    const double r = (double)b[i] - ax[i];
+    rr += r * r;
+    bb += (double)b[i] * (double)b[i];
+  }
+  return bb > 0 ? std::sqrt(rr / bb) : 0.0;
+}
+// Conjugate gradients on -A x = -b in FP64 from x = 0 until ||b - A x|| <= tol ||b||; returns iterations.
+int orc_pressure_cg(int nx, int ny, int nz, double h, const double* b, double* x, double tol, int maxit, double* rel_out) {
+  const size_t n = (size_t)nx * ny * nz;
+  const double ih2 = 1.0 / (h * h);
+  std::vector<double> r(n), p(n), q(n);
+  for (size_t i = 0; i < n; ++i) { x[i] = 0.0; r[i] = -b[i]; p[i] = r[i]; }   // residual of -A x = -b at x = 0
+  const double bb = dotp(b, b, n);
+  double rr = dotp(r.data(), r.data(), n);
+  int it = 0;
+  while (it < maxit && rr > tol * tol * bb) {
+    op_apply(nx, ny, nz, ih2, p.data(), q.data());
+    for (size_t i = 0; i < n; ++i) q[i] = -q[i];
+    const double alpha = rr / dotp(p.data(), q.data(), n);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+    const double rr2 = dotp(r.data(), r.data(), n);
+    const double beta = rr2 / rr;
+    rr = rr2;
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)n; ++i) p[i] = r[i] + beta * p[i];
+    ++it;
+  }
+  if (rel_out) *rel_out = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+  return it;
+}
+
 }  // extern "C"

@@ -59,6 +59,9 @@ def lib():
             "orc_step": (ip, [vp, ip, ip, dp]), "orc_reset": (None, [vp]),
             "orc_poisson_study": (dp, [ip, ip, ip, dp, ip, ip, ip, ip, vp]),
             "orc_poisson_rhs": (None, [ip, vp]),
+            "orc_pressure_apply": (None, [ip, ip, ip, dp, vp, vp]),
+            "orc_pressure_rel_residual": (dp, [ip, ip, ip, dp, vp, vp]),
+            "orc_pressure_cg": (ip, [ip, ip, ip, dp, vp, vp, dp, ip, vp]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -102,6 +105,33 @@ def poisson_study(N: int, face: bool, mode: int, omega: float = 1.0, pre: int = 
     r0 = lib().orc_poisson_study(N, int(face), mode, omega, pre, post, coarse, cycles, _ptr(hist))
     n = 6 if mode in (0, 1) else cycles
     return r0, hist[:n]
+
+
+def pressure_apply(x: np.ndarray, h: float) -> np.ndarray:
+    """A x in FP64 (the multigrid's operator with its ghost rules); x indexed [z, y, x]."""
+    x = np.ascontiguousarray(x, np.float64)
+    nz, ny, nx = x.shape
+    out = np.empty_like(x)
+    lib().orc_pressure_apply(nx, ny, nz, float(h), _ptr(x), _ptr(out))
+    return out
+
+
+def pressure_rel_residual(b: np.ndarray, x: np.ndarray, h: float) -> float:
+    """||b - A x|| / ||b|| in FP64 of FP32 arrays indexed [z, y, x]."""
+    b = np.ascontiguousarray(b, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    nz, ny, nx = b.shape
+    return float(lib().orc_pressure_rel_residual(nx, ny, nz, float(h), _ptr(b), _ptr(x)))
+
+
+def pressure_cg(b: np.ndarray, h: float, tol: float = 1e-12, maxit: int = 100000):
+    """FP64 conjugate-gradient solution of A x = b; returns (x, iterations, relative residual)."""
+    b = np.ascontiguousarray(b, np.float64)
+    nz, ny, nx = b.shape
+    x = np.zeros_like(b)
+    rel = np.zeros(1, np.float64)
+    it = lib().orc_pressure_cg(nx, ny, nz, float(h), _ptr(b), _ptr(x), float(tol), int(maxit), _ptr(rel))
+    return x, int(it), float(rel[0])
 
 
 class OracleSim:

@@ -52,6 +52,54 @@ __device__ __forceinline__ df64 df_warp_sum(df64 v) {
 }
 __device__ __forceinline__ double df_to_double(df64 v) { return (double)v.hi + (double)v.lo; }
 
+// Sums `count` float4 partial pairs (x + y, z + w as df64) in a fixed order with NT threads standing in for
+// SUMV virtual threads: virtual thread v takes partials v, v+SUMV, ...; each virtual warp is reduced by a
+// warp tree, and the SUMV/32 warp sums by a final warp tree.  The result depends only on `count` and the
+// partials, never on which CTA or how many real threads run it.  Thread 0 receives (A, B); all NT threads
+// of the CTA must call it (one __syncthreads inside); sa, sb: shared arrays of SUMV/32 entries.
+constexpr int SUMV = 1024;
+constexpr int SUM_BATCH = 4;   // partials per virtual thread loaded together
+template <int NT>
+__device__ __forceinline__ void sum_pairs_fixed(const float4* partials, int count, int tid, df64* sa, df64* sb, df64& A, df64& B) {
+  static_assert(SUMV % NT == 0 && NT % 32 == 0, "virtual threads map onto whole warps");
+  constexpr int J = SUMV / NT;
+  df64 a[J], b[J];
+#pragma unroll
+  for (int j = 0; j < J; ++j) { a[j] = df_make(0.0f); b[j] = df_make(0.0f); }
+  for (int i0 = 0; i0 < count; i0 += SUM_BATCH * SUMV) {
+    // all loads of the batch first (they are independent), then the adds in each virtual thread's order
+    float4 q[J][SUM_BATCH];
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+#pragma unroll
+      for (int u = 0; u < SUM_BATCH; ++u) {
+        const int i = i0 + u * SUMV + tid + NT * j;
+        q[j][u] = i < count ? __ldcg(partials + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+#pragma unroll
+    for (int j = 0; j < J; ++j)
+#pragma unroll
+      for (int u = 0; u < SUM_BATCH; ++u) {
+        if (i0 + u * SUMV + tid + NT * j < count) {
+          a[j] = df_add(a[j], df64{q[j][u].x, q[j][u].y});
+          b[j] = df_add(b[j], df64{q[j][u].z, q[j][u].w});
+        }
+      }
+  }
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const int v = tid + NT * j;
+    const df64 wa = df_warp_sum(a[j]);
+    const df64 wb = df_warp_sum(b[j]);
+    if ((tid & 31) == 0) { sa[v >> 5] = wa; sb[v >> 5] = wb; }
+  }
+  __syncthreads();
+  if (tid < 32) {
+    A = df_warp_sum(sa[tid]);
+    B = df_warp_sum(sb[tid]);
+  }
+}
+
 struct f3 { float x, y, z; };
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }
 __device__ __forceinline__ f3 xyz(const float4& v) { return mk3(v.x, v.y, v.z); }

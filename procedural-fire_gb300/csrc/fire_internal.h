@@ -83,12 +83,15 @@ void launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st);
 // fits in its shared memory, or a thread-block cluster whose CTAs each hold a z-slab of the finer tail
 // levels (distributed shared memory for the slab edges) with the coarsest levels gathered on CTA 0.
 // tail_fits: whether [first, n) can run as one tail launch; tail_first: the finest such `first` (n if none).
-bool tail_fits(const MGLevel* levels, int first, int n);
-int tail_first(const MGLevel* levels, int n);
+// coarse64: the coarsest level is solved in FP64: exactly with `cinv` (its dense inverse, transposed, in
+// global memory) when given, else by `coarse` FP64 sweeps on a double copy in shared memory.
+bool tail_fits(const MGLevel* levels, int first, int n, bool coarse64 = false);
+int tail_first(const MGLevel* levels, int n, bool coarse64 = false);
 // Shared memory per CTA of the tail launch for [first, n).
-size_t tail_smem_bytes(const MGLevel* levels, int first, int n);
+size_t tail_smem_bytes(const MGLevel* levels, int first, int n, bool coarse64 = false);
 // `err` receives 1 if the kernel's bounded wait for its bulk copies ran out (the kernel then returns early).
-void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st);
+void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st,
+                 bool coarse64 = false, const double* cinv = nullptr);
 // Opts the tail kernels into `max_tail_smem` bytes of dynamic shared memory on the current device.
 cudaError_t mg_configure(size_t max_tail_smem);
 constexpr size_t TAIL_SMEM_BUDGET = 200 * 1024;

@@ -13,6 +13,7 @@
 //    single-CTA kernel that runs the rest of the V-cycle out of shared memory; levels of <= 256 cells
 //    inside it run on one warp with __syncwarp, so the coarsest sweeps cost no CTA-wide barriers;
 //  * every kernel uses programmatic dependent launch (fire_launch.cuh) so consecutive launches overlap.
+#include <algorithm>
 #include <cooperative_groups.h>
 
 #include "fire_device.cuh"
@@ -179,6 +180,9 @@ struct TailLevels {
   int off[TAIL_MAX_LEVELS];    // float offset of level l's p in shared memory (b follows p)
   float* gp[TAIL_MAX_LEVELS];  // global copies (written back at the end)
   float* gb[TAIL_MAX_LEVELS];
+  int coarse64;                // 1: the coarsest level is solved in FP64: p = cinv b with the dense inverse
+  int doff;                    //    (transposed, global memory) if cinv is set, else `coarse` FP64 sweeps on a
+  const double* cinv;          //    double copy at float offset doff
 };
 struct FastDiv {
   int d;
@@ -230,6 +234,57 @@ __device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int
       tm.sync();
     }
 }
+// `iters` red-black sweeps in FP64 on a double copy (dp: p then b) of one level; p is written back in FP32.
+// The update is mgSmooth's (src/sim.js:417-437) with IEEE double division.
+template <bool kWarp>
+__device__ void tail_smooth_fp64(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters, double* dp) {
+  const int n = nx * ny * nz;
+  double* db = dp + n;
+  for (int t = tm.rank; t < n; t += tm.size) { dp[t] = (double)p[t]; db[t] = (double)b[t]; }
+  tm.sync();
+  const int hx = (nx + 1) >> 1, sy = nx, sz = nx * ny;
+  const double h2 = (double)h * (double)h;
+  const Box3 bx(tm.size, tm.rank, hx, ny, nz);
+  for (int it = 0; it < iters; ++it)
+    for (int color = 0; color < 2; ++color) {
+      for (int z = bx.z0; z < nz; z += bx.tz)
+        for (int y = bx.y0; y < ny; y += bx.ty)
+          for (int gx = bx.x0; gx < hx; gx += bx.tx) {
+            const int x = gx * 2 + ((y + z + color) & 1);
+            if (x >= nx) continue;
+            const int c = x + y * sy + z * sz;
+            double sum = 0.0, diag = 6.0;
+            if (x > 0) sum += dp[c - 1]; else diag += 1.0;
+            if (x < nx - 1) sum += dp[c + 1]; else diag += 1.0;
+            if (z > 0) sum += dp[c - sz]; else diag += 1.0;
+            if (z < nz - 1) sum += dp[c + sz]; else diag += 1.0;
+            if (y > 0) sum += dp[c - sy]; else diag -= 1.0;
+            if (y < ny - 1) sum += dp[c + sy]; else diag += 1.0;
+            dp[c] = (sum - h2 * db[c]) / diag;
+          }
+      tm.sync();
+    }
+  for (int t = tm.rank; t < n; t += tm.size) p[t] = (float)dp[t];
+  tm.sync();
+}
+// Exact coarsest solve in FP64: p = A^-1 b with the dense inverse stored transposed (mt[j * n + i] = inv[i][j]),
+// so the team's lanes read consecutive rows; four accumulators break the FMA dependency chain.
+template <bool kWarp>
+__device__ void tail_direct_fp64(const Team<kWarp>& tm, float* p, const float* b, int n, const double* __restrict__ mt) {
+  for (int i = tm.rank; i < n; i += tm.size) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int j = 0;
+    for (; j + 3 < n; j += 4) {
+      a0 = fma(__ldg(mt + (size_t)j * n + i), (double)b[j], a0);
+      a1 = fma(__ldg(mt + (size_t)(j + 1) * n + i), (double)b[j + 1], a1);
+      a2 = fma(__ldg(mt + (size_t)(j + 2) * n + i), (double)b[j + 2], a2);
+      a3 = fma(__ldg(mt + (size_t)(j + 3) * n + i), (double)b[j + 3], a3);
+    }
+    for (; j < n; ++j) a0 = fma(__ldg(mt + (size_t)j * n + i), (double)b[j], a0);
+    p[i] = (float)((a0 + a1) + (a2 + a3));
+  }
+  tm.sync();
+}
 template <bool kWarp>
 __device__ void tail_restrict(const Team<kWarp>& tm, const TailLevels& T, float* sm, int l) {
   const int nx = T.nx[l], ny = T.ny[l], nz = T.nz[l];
@@ -274,7 +329,13 @@ __device__ void tail_vcycle(const Team<kWarp>& tm, const TailLevels& T, float* s
   }
   {
     float* p = sm + T.off[n - 1];
-    tail_smooth(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse);
+    if (T.coarse64 && T.cinv)
+      tail_direct_fp64(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.cinv);
+    else if (T.coarse64)
+      tail_smooth_fp64(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse,
+                       reinterpret_cast<double*>(sm + T.doff));
+    else
+      tail_smooth(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse);
   }
   for (int l = n - 2; l >= from; --l) {
     tail_prolong(tm, T, sm, l);
@@ -284,9 +345,71 @@ __device__ void tail_vcycle(const Team<kWarp>& tm, const TailLevels& T, float* s
 }
 // The V-cycle over all levels of T with one CTA of TAIL_THREADS threads: levels above T.small with the
 // whole CTA, the rest on warp 0.
+// Exact coarsest solve with the whole CTA: thread t forms a partial of row t % n over the columns
+// j = t / n, t / n + K, ... (K = TAIL_THREADS / n chunks, consecutive threads read consecutive rows), the
+// partials go to shared memory (dp) and each row is summed over its K partials in a fixed order.
+__device__ void tail_direct_fp64_cta(int tid, float* p, const float* b, int n, const double* __restrict__ mt, double* dp) {
+  const int K = TAIL_THREADS / n;
+  if (tid < n * K) {
+    const int i = tid % n, k = tid / n;
+    double a0 = 0.0, a1 = 0.0;
+    int j = k;
+    for (; j + K < n; j += 2 * K) {
+      a0 = fma(__ldg(mt + (size_t)j * n + i), (double)b[j], a0);
+      a1 = fma(__ldg(mt + (size_t)(j + K) * n + i), (double)b[j + K], a1);
+    }
+    if (j < n) a0 = fma(__ldg(mt + (size_t)j * n + i), (double)b[j], a0);
+    dp[k * n + i] = a0 + a1;
+  }
+  __syncthreads();
+  if (tid < n) {
+    double s = 0.0;
+    for (int k = 0; k < K; ++k) s += dp[k * n + tid];
+    p[tid] = (float)s;
+  }
+  __syncthreads();
+}
 __device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre, int post, int coarse) {
   const Team<false> cta{tid};
   const int S = T.small;
+  if (T.coarse64 && T.cinv) {
+    // levels [0, S) with the CTA, [S, n-1) on warp 0, the exact coarsest solve with the whole CTA
+    const int n = T.n, top = min(S, n - 1);
+    for (int l = 0; l < top; ++l) {
+      float* p = sm + T.off[l];
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
+      tail_restrict(cta, T, sm, l);
+    }
+    if (tid < 32) {
+      const Team<true> wp{tid};
+      for (int l = top; l < n - 1; ++l) {
+        float* p = sm + T.off[l];
+        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
+        tail_restrict(wp, T, sm, l);
+      }
+    }
+    __syncthreads();
+    {
+      float* p = sm + T.off[n - 1];
+      const int nc = T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1];
+      tail_direct_fp64_cta(tid, p, p + nc, nc, T.cinv, reinterpret_cast<double*>(sm + T.doff));
+    }
+    if (tid < 32) {
+      const Team<true> wp{tid};
+      for (int l = n - 2; l >= top; --l) {
+        tail_prolong(wp, T, sm, l);
+        float* p = sm + T.off[l];
+        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
+      }
+    }
+    __syncthreads();
+    for (int l = top - 1; l >= 0; --l) {
+      tail_prolong(cta, T, sm, l);
+      float* p = sm + T.off[l];
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
+    }
+    return;
+  }
   if (S == 0) {
     if (tid < 32) tail_vcycle(Team<true>{tid}, T, sm, 0, pre, post, coarse);
     __syncthreads();
@@ -695,57 +818,13 @@ __global__ void __launch_bounds__(RB) k_residual(const float* __restrict__ p, co
     if (tid == 0) partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = make_float4(rr.hi, rr.lo, bb.hi, bb.lo);
   }
 }
-// Sums `count` partial pairs in a fixed order, in df64, with RB threads standing in for SUMV virtual
-// threads: virtual thread v takes partials v, v+SUMV, ...; each virtual warp is reduced by a warp tree, and
-// the SUMV/32 warp sums by a final warp tree.  The result depends only on `count` and the partials, never on
-// which CTA runs it.  Thread 0 receives (sum of .xy pairs, sum of .zw pairs).  All RB threads must call it.
-constexpr int SUMV = 1024;
-constexpr int SUM_BATCH = 4;   // partials per virtual thread loaded together (4096 partials in one batch)
-__device__ __forceinline__ void sum_pairs_fixed(const float4* partials, int count, int tid, df64* sa, df64* sb, df64& A, df64& B) {
-  constexpr int J = SUMV / RB;
-  df64 a[J], b[J];
-#pragma unroll
-  for (int j = 0; j < J; ++j) { a[j] = df_make(0.0f); b[j] = df_make(0.0f); }
-  for (int i0 = 0; i0 < count; i0 += SUM_BATCH * SUMV) {
-    // all loads of the batch first (they are independent), then the adds in each virtual thread's order
-    float4 q[J][SUM_BATCH];
-#pragma unroll
-    for (int j = 0; j < J; ++j)
-#pragma unroll
-      for (int u = 0; u < SUM_BATCH; ++u) {
-        const int i = i0 + u * SUMV + tid + RB * j;
-        q[j][u] = i < count ? __ldcg(partials + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      }
-#pragma unroll
-    for (int j = 0; j < J; ++j)
-#pragma unroll
-      for (int u = 0; u < SUM_BATCH; ++u) {
-        if (i0 + u * SUMV + tid + RB * j < count) {
-          a[j] = df_add(a[j], df64{q[j][u].x, q[j][u].y});
-          b[j] = df_add(b[j], df64{q[j][u].z, q[j][u].w});
-        }
-      }
-  }
-#pragma unroll
-  for (int j = 0; j < J; ++j) {
-    const int v = tid + RB * j;
-    const df64 wa = df_warp_sum(a[j]);
-    const df64 wb = df_warp_sum(b[j]);
-    if ((tid & 31) == 0) { sa[v >> 5] = wa; sb[v >> 5] = wb; }
-  }
-  __syncthreads();
-  if (tid < 32) {
-    A = df_warp_sum(sa[tid]);
-    B = df_warp_sum(sb[tid]);
-  }
-}
 // out2 = (||r||^2, ||b||^2) as doubles.
 __global__ void __launch_bounds__(RB) k_sum_pairs(const float4* __restrict__ partials, int count, double* __restrict__ out2) {
   __shared__ df64 sa[SUMV / 32], sb[SUMV / 32];
   pdl_wait();
   pdl_trigger();
   df64 a, b;
-  sum_pairs_fixed(partials, count, threadIdx.x, sa, sb, a, b);
+  sum_pairs_fixed<RB>(partials, count, threadIdx.x, sa, sb, a, b);
   if (threadIdx.x == 0) { out2[0] = df_to_double(a); out2[1] = df_to_double(b); }
 }
 // The residual-driven loop's test after k_residual: sums the partials with sum_pairs_fixed (so the norm
@@ -758,7 +837,7 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
   pdl_wait();
   pdl_trigger();
   df64 A, B;
-  sum_pairs_fixed(partials, count, threadIdx.x, sa, sb, A, B);
+  sum_pairs_fixed<RB>(partials, count, threadIdx.x, sa, sb, A, B);
   if (threadIdx.x == 0) {
     const double s0 = df_to_double(A), s1 = df_to_double(B);
     sums2[0] = s0;
@@ -799,26 +878,31 @@ static int tail_dist_levels(const MGLevel* levels, int first, int n) {
   }
   return d;
 }
-size_t tail_smem_bytes(const MGLevel* levels, int first, int n) {
+// Floats after the tail levels' p/b arrays where the FP64 copy of the coarsest level starts (8-byte aligned).
+static size_t tail_fp64_offset(size_t floats) { return (floats + 1) & ~(size_t)1; }
+size_t tail_smem_bytes(const MGLevel* levels, int first, int n, bool coarse64) {
   const int nd = tail_dist_levels(levels, first, n);
   size_t floats = 0;
   for (int l = first; l < n; ++l) {
     const size_t cells = (size_t)levels[l].nx * levels[l].ny * levels[l].nz;
     floats += 2 * (l < first + nd ? cells / CTAIL_CLUSTER : cells);
   }
+  if (coarse64)   // the FP64 copy of the coarsest level (sweeps) or the direct solve's row partials
+    floats = tail_fp64_offset(floats) +
+             std::max<size_t>(4 * (size_t)levels[n - 1].nx * levels[n - 1].ny * levels[n - 1].nz, 2 * (size_t)TAIL_THREADS);
   return floats * sizeof(float);
 }
-bool tail_fits(const MGLevel* levels, int first, int n) {
+bool tail_fits(const MGLevel* levels, int first, int n, bool coarse64) {
   return first >= 0 && first < n && n - first - tail_dist_levels(levels, first, n) <= TAIL_MAX_LEVELS &&
-         tail_smem_bytes(levels, first, n) <= TAIL_SMEM_BUDGET;
+         tail_smem_bytes(levels, first, n, coarse64) <= TAIL_SMEM_BUDGET;
 }
-int tail_first(const MGLevel* levels, int n) {
+int tail_first(const MGLevel* levels, int n, bool coarse64) {
   int first = n;
-  for (int l = n - 1; l >= 0 && tail_fits(levels, l, n); --l) first = l;
+  for (int l = n - 1; l >= 0 && tail_fits(levels, l, n, coarse64); --l) first = l;
   return first;
 }
 // Levels [first, n) as a TailLevels block whose first level's p starts `off` floats into shared memory.
-static TailLevels make_tail_levels(const MGLevel* levels, int first, int n, int off) {
+static TailLevels make_tail_levels(const MGLevel* levels, int first, int n, int off, bool coarse64, const double* cinv) {
   TailLevels T;
   T.n = n - first;
   T.small = T.n;
@@ -830,13 +914,17 @@ static TailLevels make_tail_levels(const MGLevel* levels, int first, int n, int 
     T.gp[l] = L.p; T.gb[l] = L.b;
     if (T.small == T.n && L.nx * L.ny * L.nz <= TAIL_WARP_CELLS) T.small = l;
   }
+  T.coarse64 = coarse64 ? 1 : 0;
+  T.doff = (int)tail_fp64_offset((size_t)off);
+  T.cinv = coarse64 ? cinv : nullptr;
   return T;
 }
-void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st) {
-  const size_t smem = tail_smem_bytes(levels, first, n);
+void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st, bool coarse64,
+                 const double* cinv) {
+  const size_t smem = tail_smem_bytes(levels, first, n, coarse64);
   const int nd = tail_dist_levels(levels, first, n);
   if (nd == 0) {
-    launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), smem, st, make_tail_levels(levels, first, n, 0), pre, post, coarse, err);
+    launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), smem, st, make_tail_levels(levels, first, n, 0, coarse64, cinv), pre, post, coarse, err);
     return;
   }
   CTailLevels T;
@@ -851,7 +939,7 @@ void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int
   }
   T.gp = levels[first].p;
   T.gb = levels[first].b;
-  T.G = make_tail_levels(levels, first + nd, n, off);
+  T.G = make_tail_levels(levels, first + nd, n, off, coarse64, cinv);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CTAIL_CLUSTER);
   cfg.blockDim = dim3(TAIL_THREADS);

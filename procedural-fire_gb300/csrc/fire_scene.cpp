@@ -67,4 +67,21 @@ int fire_make_spots(uint32_t seed, int n, float flux_lo, float flux_hi, float si
   return FIRE_OK;
 }
 
+// Sources of the seeded Poisson right-hand side: centre uniform over the grid (cell units), sigma uniform
+// in [1, 4] cells, amplitude standard normal (Box-Muller on two uniforms).
+int fire_poisson_sources(unsigned seed, int n, const int res[3], float* out) {
+  if (!out || !res || n < 0 || n > 4096) return FIRE_ERR_BAD_ARG;
+  const double PI = 3.141592653589793;
+  for (int i = 0; i < n; ++i) {
+    const uint32_t k = 6u * (uint32_t)i;
+    const double u1 = std::fmax(rand2(seed, k + 4u), 1e-12), u2 = rand2(seed, k + 5u);
+    out[5 * i + 0] = (float)(rand2(seed, k + 0u) * res[0]);
+    out[5 * i + 1] = (float)(rand2(seed, k + 1u) * res[1]);
+    out[5 * i + 2] = (float)(rand2(seed, k + 2u) * res[2]);
+    out[5 * i + 3] = (float)(1.0 + 3.0 * rand2(seed, k + 3u));
+    out[5 * i + 4] = (float)(std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * PI * u2));
+  }
+  return FIRE_OK;
+}
+
 }  // extern "C"

@@ -25,6 +25,7 @@ SOURCES = {
     "fire_stats.cu": [],
     "fire_api.cu": [],
     "fire_noalloc.cu": [],
+    "fire_poisson.cu": [],
     "fire_scene.cpp": [],
 }
 

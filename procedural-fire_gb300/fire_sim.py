@@ -105,6 +105,13 @@ _SIGS = {
     "fire_build_campfire": (_ip, [ctypes.c_uint32, _vp, _ip]),
     "fire_make_spots": (_ip, [ctypes.c_uint32, _ip, _fp, _fp, _fp, _fp, _vp]),
     "fire_poisson_vcycles_noalloc": (_ip, [_vp, _vp, _ip, _ip, _ip, _fp, _ip, _vp]),
+    "fire_poisson_create": (_ip, [_vp, _fp, _ip, _ip, ctypes.POINTER(_vp)]),
+    "fire_poisson_destroy": (_ip, [_vp]),
+    "fire_poisson_solve": (_ip, [_vp, _vp, _vp, _vp, _dp, _ip, _ip, _vp]),
+    "fire_poisson_result": (_ip, [_vp, _vp]),
+    "fire_poisson_residual": (_ip, [_vp, _vp, _vp, _vp, ctypes.POINTER(_dp)]),
+    "fire_poisson_make_rhs": (_ip, [_vp, _vp, ctypes.c_uint, _ip, _fp, _vp]),
+    "fire_poisson_sources": (_ip, [ctypes.c_uint, _ip, _vp, _vp]),
     "fire_device_ok": (_ip, [_ip]),
     "fire_version": (ctypes.c_char_p, []),
 }
@@ -381,3 +388,83 @@ class FireSim:
     def stats_async(self, out_ptr: int, stream=None):
         """Queues S stats + heat release into a pinned host buffer of 17 doubles (no wait)."""
         self._check(self._lib.fire_sim_stats_async(self._h, ctypes.c_void_p(out_ptr), _stream_handle(stream)), "stats_async")
+
+
+# ---------------------------------------------------------------------------------------------------
+# Standalone pressure Poisson solver (the step's multigrid, src/sim.js:415-495, 576-599, iterated to a
+# tolerance; plain FP32 or FP16/BF16-storage iterative refinement).
+PRECISIONS = {"fp32": 0, "fp16": 1, "bf16": 2, "ir32": 3}
+
+
+class FirePoissonResult(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("rel_residual", ctypes.c_double),
+                ("rel_residual_initial", ctypes.c_double), ("b_norm", ctypes.c_double)]
+
+
+def _dev_ptr(a) -> int:
+    """Device address of a torch tensor (or an int address)."""
+    return int(a) if isinstance(a, int) else int(a.data_ptr())
+
+
+def poisson_sources(seed: int, n: int, res) -> np.ndarray:
+    """The (centre x, y, z, sigma, amplitude) rows of fire_poisson_make_rhs, cell units."""
+    out = np.zeros((max(n, 1), 5), np.float32)
+    r = (ctypes.c_int * 3)(*[int(v) for v in res])
+    rc = load_library().fire_poisson_sources(seed, n, r, _ptr(out))
+    if rc:
+        raise FireError(rc, "poisson_sources")
+    return out[:n]
+
+
+class Poisson:
+    """Standalone solver for the step's pressure equation on device arrays of res[0]*res[1]*res[2] floats."""
+
+    def __init__(self, res, h: float, precision: str = "fp32", device: int = 0):
+        self._lib = load_library()
+        self.res = tuple(int(v) for v in res)
+        self.h = float(h)
+        self.precision = precision
+        r = (ctypes.c_int * 3)(*self.res)
+        hnd = ctypes.c_void_p()
+        rc = self._lib.fire_poisson_create(r, self.h, PRECISIONS[precision], device, ctypes.byref(hnd))
+        if rc:
+            raise FireError(rc, "fire_poisson_create")
+        self._h = hnd
+
+    def close(self):
+        if self._h:
+            self._lib.fire_poisson_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            raise FireError(rc, what)
+
+    def solve(self, b, x, tol: float = 1e-6, max_iters: int = 50, inner_cycles: int = 1, x_lo=None, stream=None):
+        """Queues the solve of A x = b (x, and x_lo if given, hold the initial guess); returns without waiting."""
+        lo = ctypes.c_void_p(_dev_ptr(x_lo)) if x_lo is not None else None
+        self._check(self._lib.fire_poisson_solve(self._h, ctypes.c_void_p(_dev_ptr(b)), ctypes.c_void_p(_dev_ptr(x)), lo, float(tol),
+                                                 int(max_iters), int(inner_cycles), _stream_handle(stream)), "fire_poisson_solve")
+
+    def result(self) -> Dict[str, float]:
+        r = FirePoissonResult()
+        self._check(self._lib.fire_poisson_result(self._h, ctypes.byref(r)), "fire_poisson_result")
+        return {"iterations": r.iterations, "rel_residual": r.rel_residual,
+                "rel_residual_initial": r.rel_residual_initial, "b_norm": r.b_norm}
+
+    def residual(self, b, x, x_lo=None) -> float:
+        v = ctypes.c_double()
+        lo = ctypes.c_void_p(_dev_ptr(x_lo)) if x_lo is not None else None
+        self._check(self._lib.fire_poisson_residual(self._h, ctypes.c_void_p(_dev_ptr(b)), ctypes.c_void_p(_dev_ptr(x)), lo,
+                                                    ctypes.byref(v)), "fire_poisson_residual")
+        return v.value
+
+    def make_rhs(self, b, seed: int = 3, n_sources: int = 32, noise: float = 1e-3, stream=None):
+        self._check(self._lib.fire_poisson_make_rhs(self._h, ctypes.c_void_p(_dev_ptr(b)), seed, n_sources, float(noise),
+                                                    _stream_handle(stream)), "fire_poisson_make_rhs")
