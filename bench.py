@@ -230,6 +230,51 @@ def _block(F):
     return blk
 
 
+# Standalone pressure solve: 256x512x256 cells at 5 mm, seeded zero-mean RHS of 32 Gaussian sources
+# (sigma 1-4 cells, amplitude N(0,1)) plus 1e-3 white noise, solved from x = 0 to a 1e-6 relative residual.
+POISSON = dict(name="poisson-256x512x256", res=(256, 512, 256), h=0.005, seed=3, sources=32, noise=1e-3, tol=1e-6)
+
+
+def run_poisson(dev: int, reps: int = 3):
+    """Times each form of the standalone solver on the POISSON workload (device time, CUDA events).  The
+    FP32 form (the step's V-cycle on an FP32 x) cannot get below the FP32 representation floor of the
+    solution (~2e-5 here); it is timed to 3e-5 and its floor reported."""
+    import torch
+    import fire_sim as F
+    P = POISSON
+    n = P["res"][0] * P["res"][1] * P["res"][2]
+    b = torch.empty(n, dtype=torch.float32, device=f"cuda:{dev}")
+    x = torch.zeros_like(b)
+    lo = torch.zeros_like(b)
+    st = torch.cuda.current_stream(dev)
+    forms = {}
+    for prec in ("fp32", "ir32", "fp16", "bf16"):
+        ps = F.Poisson(P["res"], P["h"], prec, device=dev)
+        ps.make_rhs(b, seed=P["seed"], n_sources=P["sources"], noise=P["noise"])
+        tol = 3e-5 if prec == "fp32" else P["tol"]
+        times = []
+        for r in range(reps + 1):
+            x.zero_(); lo.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            ps.solve(b, x, tol=tol, max_iters=60, x_lo=lo, stream=st.cuda_stream)
+            e1.record(st)
+            res = ps.result()
+            if r > 0:
+                times.append(e0.elapsed_time(e1))
+        forms[prec] = {"ms": statistics.median(times), "iterations": res["iterations"], "rel_residual": res["rel_residual"],
+                       "tol": tol}
+        if prec == "fp32":
+            ps.solve(b, x, tol=0.0, max_iters=30, stream=st.cuda_stream)
+            forms[prec]["floor_rel_residual"] = ps.result()["rel_residual"]
+        ps.close()
+    base = forms["ir32"]["ms"]
+    return {"workload": P["name"], "grid": list(P["res"]), "tol": P["tol"], "rhs": "32 seeded Gaussian sources + 1e-3 noise, mean removed",
+            "forms": forms, "speedup_vs_ir32": {k: base / forms[k]["ms"] for k in ("fp16", "bf16")},
+            "note": "ir32/fp16/bf16: iterative refinement with FP32-pair x, level storage FP32/half/bfloat16, exact FP64 "
+                    "coarsest solve; fp32: the step's V(2,2) cycle on an FP32 x (stalls at its representation floor)"}
+
+
 # ------------------------------------------------------------------------------------------ arms
 def run_ours(args):
     import torch
@@ -340,7 +385,11 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": clocks,
         "diag_last_step": {"hrr_kw": float(diag[16]), "T_max": 293.0 + 1000.0 * float(diag[1])},
+        "poisson": None,
     }
+    if world == 1 and not args.no_poisson:
+        sim.close()   # frees the step's arena before the 256x512x256 solves
+        out["poisson"] = run_poisson(dev)
     return out
 
 
@@ -397,6 +446,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--preroll", type=int, default=WORKLOAD["preroll"], help="untimed steps that develop the fire")
+    ap.add_argument("--no-poisson", action="store_true", help="skip the standalone 256x512x256 pressure-solve timings")
     ap.add_argument("--mg-fixed", type=int, default=0,
                     help="profiling aid: N fixed V-cycles per step instead of the residual-driven solve")
     args = ap.parse_args(argv)

@@ -144,6 +144,91 @@ __global__ void __launch_bounds__(NT) k_psmooth_rb(T* __restrict__ p, const T* _
   }
 }
 
+// Two adjacent entries (2 g, 2 g + 1) as one 4- or 8-byte load / store.
+template <typename T> struct Pair;
+template <> struct Pair<float> {
+  static __device__ __forceinline__ float2 ld(const float* p) { return *reinterpret_cast<const float2*>(p); }
+  static __device__ __forceinline__ void st(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+};
+template <> struct Pair<__half> {
+  static __device__ __forceinline__ float2 ld(const __half* p) { return __half22float2(*reinterpret_cast<const __half2*>(p)); }
+  static __device__ __forceinline__ void st(__half* p, float a, float b) { *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b); }
+};
+template <> struct Pair<__nv_bfloat16> {
+  static __device__ __forceinline__ float2 ld(const __nv_bfloat16* p) { return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p)); }
+  static __device__ __forceinline__ void st(__nv_bfloat16* p, float a, float b) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
+  }
+};
+// k_psmooth_rb with a pair of same-colour cells (half-indices 2 g, 2 g + 1 of one row) per thread and SMZ
+// rows: b, the y and z neighbours and the result move as pairs; the three x neighbours of the pair are one
+// pair plus one scalar of the other colour (which side depends on the row's x parity s).  Needs nx % 4 == 0
+// so every colour half and row starts at an even entry.  Same arithmetic and order as k_psmooth_rb.
+template <typename T, bool kZero>
+__global__ void __launch_bounds__(NT) k_psmooth_rb2(T* __restrict__ p, const T* __restrict__ b, int nx, int ny, int nz, float h, int color) {
+  pdl_wait();
+  pdl_trigger();
+  const int hx = nx >> 1, half = hx * ny * nz, ry = hx, rz = hx * ny;
+  const int g = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y;
+  const int zb = (blockIdx.z * GZ + threadIdx.z) * SMZ;
+  const int gx = 2 * g;
+  if (gx >= hx || y >= ny) return;
+  T* __restrict__ pc = p + color * half;
+  const T* __restrict__ po = p + (1 - color) * half;
+  const T* __restrict__ bc = b + color * half;
+  const float h2 = h * h;
+  float v0[SMZ], v1[SMZ];
+#pragma unroll
+  for (int k = 0; k < SMZ; ++k) {
+    const int z = zb + k;
+    if (z < nz) {
+      const int s = (y + z + color) & 1;
+      const int r = gx + ry * y + rz * z;
+      float2 o = make_float2(0.0f, 0.0f), ym = o, yp = o, zm = o, zp = o;
+      float side = 0.0f;
+      // x neighbours: s = 0 -> entries 2g-1 (cell 0's x-), 2g, 2g+1; s = 1 -> 2g, 2g+1, 2g+2 (cell 1's x+)
+      const bool cell0_xm = gx > 0 || s, cell1_xp = gx + 1 < hx - 1 || !s;
+      if (!kZero) {
+        o = Pair<T>::ld(po + r);
+        if (!s && cell0_xm) side = Sto<T>::ld(po + r - 1);
+        if (s && cell1_xp) side = Sto<T>::ld(po + r + 2);
+        if (z > 0) zm = Pair<T>::ld(po + r - rz);
+        if (z < nz - 1) zp = Pair<T>::ld(po + r + rz);
+        if (y > 0) ym = Pair<T>::ld(po + r - ry);
+        if (y < ny - 1) yp = Pair<T>::ld(po + r + ry);
+      }
+      const float2 bv = Pair<T>::ld(bc + r);
+      // cell 0 (half-index 2g): x- = s ? o.x : side, x+ = s ? o.y : o.x
+      {
+        float sum = 0.0f, diag = 6.0f;
+        if (cell0_xm) { if (!kZero) sum += s ? o.x : side; } else diag += 1.0f;
+        if (!kZero) sum += s ? o.y : o.x;   // x+ of cell 0 always exists (cell 1 follows it)
+        if (z > 0) { if (!kZero) sum += zm.x; } else diag += 1.0f;
+        if (z < nz - 1) { if (!kZero) sum += zp.x; } else diag += 1.0f;
+        if (y > 0) { if (!kZero) sum += ym.x; } else diag -= 1.0f;
+        if (y < ny - 1) { if (!kZero) sum += yp.x; } else diag += 1.0f;
+        v0[k] = __fdividef(sum - h2 * bv.x, diag);
+      }
+      // cell 1 (half-index 2g+1): x- = s ? o.y : o.x, x+ = s ? side : o.y
+      {
+        float sum = 0.0f, diag = 6.0f;
+        if (!kZero) sum += s ? o.y : o.x;   // x- of cell 1 always exists
+        if (cell1_xp) { if (!kZero) sum += s ? side : o.y; } else diag += 1.0f;
+        if (z > 0) { if (!kZero) sum += zm.y; } else diag += 1.0f;
+        if (z < nz - 1) { if (!kZero) sum += zp.y; } else diag += 1.0f;
+        if (y > 0) { if (!kZero) sum += ym.y; } else diag -= 1.0f;
+        if (y < ny - 1) { if (!kZero) sum += yp.y; } else diag += 1.0f;
+        v1[k] = __fdividef(sum - h2 * bv.y, diag);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < SMZ; ++k) {
+    const int z = zb + k;
+    if (z < nz) Pair<T>::st(pc + gx + ry * y + rz * z, v0[k], v1[k]);
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ float pgv(const LV<T>& L, int x, int y, int z, float me) {
   if (x < 0 || z < 0 || x >= L.nx || z >= L.nz || y >= L.ny) return -me;
@@ -213,6 +298,101 @@ __global__ void __launch_bounds__(NT) k_pprolong(TF* __restrict__ p, int fsplit,
           acc += v[dz + oz][dy + oy][dx + ox] * wx * wy * wz;
         }
         TF* pf = F.at(2 * cx + dx, 2 * cy + dy, 2 * cz + dz);
+        Sto<TF>::st(pf, Sto<TF>::ld(pf) + acc);
+      }
+}
+
+// Value of cell (x, y, z) of a red-black split level (half = nx/2 * ny * nz, hx = nx/2).
+template <typename T>
+__device__ __forceinline__ float ld_rb(const T* p, int half, int hx, int ny, int x, int y, int z) {
+  return Sto<T>::ld(p + (((x + y + z) & 1) ? half : 0) + (x >> 1) + hx * (y + ny * z));
+}
+// Fused residual + 8-child restriction (src/sim.js:439-466) from a red-black split fine level into a plain
+// coarse level.  The 32 distinct fine values the 8 children and their faces need (a 4x4x4 block without
+// its edges and corners) are loaded once into v[z][y][x] (offsets -1..2 around the children); the
+// arithmetic and its order are k_prestrict's, so the results are identical.
+template <typename TF, typename TC>
+__global__ void __launch_bounds__(NT) k_prestrict_rb(const TF* __restrict__ p, const TF* __restrict__ b, int nx, int ny, int nz, float h,
+                                                     TC* __restrict__ bc, TC* __restrict__ pc) {
+  pdl_wait();
+  pdl_trigger();
+  const int cnx = nx / 2, cny = ny / 2, cnz = nz / 2;
+  const int cx = blockIdx.x * GX + threadIdx.x, cy = blockIdx.y * GY + threadIdx.y, cz = blockIdx.z * GZ + threadIdx.z;
+  if (cx >= cnx || cy >= cny || cz >= cnz) return;
+  const int hx = nx >> 1, half = hx * ny * nz;
+  const int x0 = 2 * cx - 1, y0 = 2 * cy - 1, z0 = 2 * cz - 1;
+  float v[4][4][4];
+#pragma unroll
+  for (int iz = 0; iz < 4; ++iz)
+#pragma unroll
+    for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+      for (int ix = 0; ix < 4; ++ix) {
+        const bool cz_ = iz == 1 || iz == 2, cy_ = iy == 1 || iy == 2, cx_ = ix == 1 || ix == 2;
+        const int inner = (cz_ ? 1 : 0) + (cy_ ? 1 : 0) + (cx_ ? 1 : 0);
+        v[iz][iy][ix] = 0.0f;
+        if (inner >= 2) {   // children (inner == 3) and their face neighbours (inner == 2)
+          const int x = x0 + ix, y = y0 + iy, z = z0 + iz;
+          if (x >= 0 && x < nx && y >= 0 && y < ny && z >= 0 && z < nz) v[iz][iy][ix] = ld_rb(p, half, hx, ny, x, y, z);
+        }
+      }
+  const float ih2 = 1.0f / (h * h);
+  float acc = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int dx = q & 1, dy = (q >> 1) & 1, dz = (q >> 2) & 1;
+    const int ix = 1 + dx, iy = 1 + dy, iz = 1 + dz;
+    const int x = 2 * cx + dx, y = 2 * cy + dy, z = 2 * cz + dz;
+    const float me = v[iz][iy][ix];
+    const float gxm = x > 0 ? v[iz][iy][ix - 1] : -me, gxp = x < nx - 1 ? v[iz][iy][ix + 1] : -me;
+    const float gym = y > 0 ? v[iz][iy - 1][ix] : me, gyp = y < ny - 1 ? v[iz][iy + 1][ix] : -me;
+    const float gzm = z > 0 ? v[iz - 1][iy][ix] : -me, gzp = z < nz - 1 ? v[iz + 1][iy][ix] : -me;
+    const float lap = (gxm + gxp + gym + gyp + gzm + gzp - 6.0f * me) * ih2;
+    acc += ld_rb(b, half, hx, ny, x, y, z) - lap;
+  }
+  const int t = cx + cnx * (cy + cny * cz);
+  Sto<TC>::st(bc + t, acc * 0.125f);
+  Sto<TC>::st(pc + t, 0.0f);
+}
+// k_pprolong from a plain coarse level into a red-black split fine level: child (2cx+dx, 2cy+dy, 2cz+dz)
+// is entry cx of colour half (dx + dy + dz) & 1 in its row.
+template <typename TF, typename TC>
+__global__ void __launch_bounds__(NT) k_pprolong_rb(TF* __restrict__ p, const TC* __restrict__ pc, int nx, int ny, int nz) {
+  pdl_wait();
+  pdl_trigger();
+  const int ncx = nx / 2, ncy = ny / 2, ncz = nz / 2;
+  const int cx = blockIdx.x * GX + threadIdx.x, cy = blockIdx.y * GY + threadIdx.y, cz = blockIdx.z * GZ + threadIdx.z;
+  if (cx >= ncx || cy >= ncy || cz >= ncz) return;
+  const int hx = nx >> 1, half = hx * ny * nz;
+  float v[3][3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int qx = cx + c - 1, qy = cy + bb - 1, qz = cz + a - 1;
+        float val = Sto<TC>::ld(pc + min(max(qx, 0), ncx - 1) + ncx * (min(max(qy, 0), ncy - 1) + ncy * min(max(qz, 0), ncz - 1)));
+        if (qx < 0 || qx >= ncx) val = -val;
+        if (qz < 0 || qz >= ncz) val = -val;
+        if (qy >= ncy) val = -val;
+        v[a][bb][c] = val;
+      }
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const float fx = dx ? 0.25f : 0.75f, fy = dy ? 0.25f : 0.75f, fz = dz ? 0.25f : 0.75f;
+        float acc = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int ox = q & 1, oy = (q >> 1) & 1, oz = (q >> 2) & 1;
+          const float wx = ox ? fx : 1.0f - fx, wy = oy ? fy : 1.0f - fy, wz = oz ? fz : 1.0f - fz;
+          acc += v[dz + oz][dy + oy][dx + ox] * wx * wy * wz;
+        }
+        TF* pf = p + (((dx + dy + dz) & 1) ? half : 0) + cx + hx * ((2 * cy + dy) + ny * (2 * cz + dz));
         Sto<TF>::st(pf, Sto<TF>::ld(pf) + acc);
       }
 }
@@ -307,6 +487,74 @@ __global__ void __launch_bounds__(NT) k_pres(const float* __restrict__ xh, const
         bb += bv * bv;
         prev = cur; cur = next;
         lprev = lcur; lcur = lnext;
+        t += sz;
+      }
+    }
+  }
+  cta_partial(rr, bb, partials, blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
+}
+
+// k_pres for even nx with one thread per x pair (2 gx, 2 gx + 1) and RZ planes: every load of xh, xl and b
+// is a float2 (plus one scalar on each side for the x neighbours), and the two residuals land at entry gx
+// of the two colour halves when rT is red-black split.
+// kFull: nz is a multiple of the planes a CTA covers, so no plane test is needed inside the march.
+template <typename TR, bool kFull>
+__global__ void __launch_bounds__(NT) k_pres2(const float* __restrict__ xh, const float* __restrict__ xl, const float* __restrict__ b,
+                                              TR* __restrict__ rT, int rsplit, const PState* __restrict__ ps, int nx, int ny, int nz, float ih2,
+                                              float4* __restrict__ partials) {
+  pdl_wait();
+  pdl_trigger();
+  const int hx = nx >> 1;
+  const int gx = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y;
+  const int z0 = (blockIdx.z * GZ + threadIdx.z) * RZ;
+  float rr = 0.0f, bb = 0.0f;
+  if (gx < hx && y < ny && z0 < nz) {
+    const float s = rT ? ps->sc[1] : 1.0f;
+    const int sy = nx, sz = nx * ny, halfn = hx * ny * nz;
+    const bool hxm = gx > 0, hxp = gx < hx - 1, hym = y > 0, hyp = y < ny - 1;
+    const float2 zero2 = make_float2(0.0f, 0.0f);
+    auto ld2 = [](const float* q) { return __ldg(reinterpret_cast<const float2*>(q)); };
+    int t = 2 * gx + sy * y + sz * z0;
+    float2 hp = z0 > 0 ? ld2(xh + t - sz) : zero2, hc = ld2(xh + t);
+    float2 lp = zero2, lc = zero2;
+    if (xl) { lp = z0 > 0 ? ld2(xl + t - sz) : zero2; lc = ld2(xl + t); }
+#pragma unroll
+    for (int k = 0; k < RZ; ++k) {
+      const int z = z0 + k;
+      if (kFull || z < nz) {
+        const bool hzm = z > 0, hzp = z + 1 < nz;
+        const float2 hn = hzp ? ld2(xh + t + sz) : zero2;
+        const float hl = hxm ? __ldg(xh + t - 1) : 0.0f, hr = hxp ? __ldg(xh + t + 2) : 0.0f;
+        const float2 hym2 = hym ? ld2(xh + t - sy) : zero2, hyp2 = hyp ? ld2(xh + t + sy) : zero2;
+        const float d0 = lap_diff(hc.x, hl, hc.y, hym2.x, hyp2.x, hp.x, hn.x, hxm, true, hym, hyp, hzm, hzp);
+        const float d1 = lap_diff(hc.y, hc.x, hr, hym2.y, hyp2.y, hp.y, hn.y, true, hxp, hym, hyp, hzm, hzp);
+        float dl0 = 0.0f, dl1 = 0.0f;
+        float2 ln = zero2;
+        if (xl) {
+          ln = hzp ? ld2(xl + t + sz) : zero2;
+          const float ll = hxm ? __ldg(xl + t - 1) : 0.0f, lr = hxp ? __ldg(xl + t + 2) : 0.0f;
+          const float2 lym2 = hym ? ld2(xl + t - sy) : zero2, lyp2 = hyp ? ld2(xl + t + sy) : zero2;
+          dl0 = lap_diff(lc.x, ll, lc.y, lym2.x, lyp2.x, lp.x, ln.x, hxm, true, hym, hyp, hzm, hzp);
+          dl1 = lap_diff(lc.y, lc.x, lr, lym2.y, lyp2.y, lp.y, ln.y, true, hxp, hym, hyp, hzm, hzp);
+        }
+        const float2 bv = ld2(b + t);
+        const float r0 = (bv.x - d0 * ih2) - dl0 * ih2, r1 = (bv.y - d1 * ih2) - dl1 * ih2;
+        if (rT) {
+          if (rsplit) {
+            const int c0 = (y + z) & 1, idx = gx + hx * (y + ny * z);
+            Sto<TR>::st(rT + c0 * halfn + idx, r0 * s);
+            Sto<TR>::st(rT + (1 - c0) * halfn + idx, r1 * s);
+          } else {
+            Sto<TR>::st(rT + t, r0 * s);
+            Sto<TR>::st(rT + t + 1, r1 * s);
+          }
+        }
+        rr += r0 * r0;
+        rr += r1 * r1;
+        bb += bv.x * bv.x;
+        bb += bv.y * bv.y;
+        hp = hc; hc = hn;
+        lp = lc; lc = ln;
         t += sz;
       }
     }
@@ -470,7 +718,11 @@ int storage_of(int prec) { return prec == FIRE_POISSON_FP16 ? STO_F16 : prec == 
 
 template <typename T>
 void psmooth_t(const PLevel& L, int color, int zero, cudaStream_t st) {
-  if (L.split) {
+  if (L.split && L.nx % 4 == 0) {
+    const dim3 g = grid3(L.nx >> 2, L.ny, (L.nz + SMZ - 1) / SMZ);
+    if (zero) launch_pdl(k_psmooth_rb2<T, true>, g, kBlock, 0, st, (T*)L.p, (const T*)L.b, L.nx, L.ny, L.nz, L.h, color);
+    else launch_pdl(k_psmooth_rb2<T, false>, g, kBlock, 0, st, (T*)L.p, (const T*)L.b, L.nx, L.ny, L.nz, L.h, color);
+  } else if (L.split) {
     const dim3 g = grid3(L.nx >> 1, L.ny, (L.nz + SMZ - 1) / SMZ);
     if (zero) launch_pdl(k_psmooth_rb<T, true>, g, kBlock, 0, st, (T*)L.p, (const T*)L.b, L.nx, L.ny, L.nz, L.h, color);
     else launch_pdl(k_psmooth_rb<T, false>, g, kBlock, 0, st, (T*)L.p, (const T*)L.b, L.nx, L.ny, L.nz, L.h, color);
@@ -488,8 +740,12 @@ void psmooth(const PLevel& L, int color, int zero, cudaStream_t st) {
 }
 template <typename TF, typename TC>
 void prestrict_tt(const PLevel& F, const PLevel& C, cudaStream_t st) {
-  launch_pdl(k_prestrict<TF, TC>, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (const TF*)F.p, (const TF*)F.b, F.split, F.nx, F.ny, F.nz, F.h,
-             (TC*)C.b, (TC*)C.p, C.split);
+  if (F.split && !C.split)
+    launch_pdl(k_prestrict_rb<TF, TC>, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (const TF*)F.p, (const TF*)F.b, F.nx, F.ny, F.nz, F.h,
+               (TC*)C.b, (TC*)C.p);
+  else
+    launch_pdl(k_prestrict<TF, TC>, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (const TF*)F.p, (const TF*)F.b, F.split, F.nx, F.ny, F.nz,
+               F.h, (TC*)C.b, (TC*)C.p, C.split);
 }
 template <typename TF>
 void prestrict_to(const PLevel& F, const PLevel& C, cudaStream_t st) {
@@ -508,7 +764,10 @@ void prestrict(const PLevel& F, const PLevel& C, cudaStream_t st) {
 }
 template <typename TF, typename TC>
 void pprolong_tt(const PLevel& F, const PLevel& C, cudaStream_t st) {
-  launch_pdl(k_pprolong<TF, TC>, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (TF*)F.p, F.split, (const TC*)C.p, C.split, F.nx, F.ny, F.nz);
+  if (F.split && !C.split)
+    launch_pdl(k_pprolong_rb<TF, TC>, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (TF*)F.p, (const TC*)C.p, F.nx, F.ny, F.nz);
+  else
+    launch_pdl(k_pprolong<TF, TC>, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (TF*)F.p, F.split, (const TC*)C.p, C.split, F.nx, F.ny, F.nz);
 }
 template <typename TF>
 void pprolong_from(const PLevel& F, const PLevel& C, cudaStream_t st) {
@@ -526,13 +785,24 @@ void pprolong(const PLevel& F, const PLevel& C, cudaStream_t st) {
   }
 }
 
-dim3 pres_grid(const PLevel& L) { return dim3((L.nx + GX - 1) / GX, (L.ny + GY - 1) / GY, (L.nz + GZ * RZ - 1) / (GZ * RZ)); }
+// The residual kernel's grid: x pairs for even nx (k_pres2), single cells otherwise (k_pres).
+dim3 pres_grid(const PLevel& L) {
+  const int cols = (L.nx % 2 == 0) ? L.nx / 2 : L.nx;
+  return dim3((cols + GX - 1) / GX, (L.ny + GY - 1) / GY, (L.nz + GZ * RZ - 1) / (GZ * RZ));
+}
 
 // r = b - A (xh + xl); written scaled into level 0's RHS when `write` (refinement forms); partials for the test.
 template <typename TR>
 void pres_t(FirePoisson* ps, const PState* state, const float* b, const float* xh, const float* xl, TR* rT, int rsplit, cudaStream_t st) {
   const PLevel& L = ps->levels[0];
-  launch_pdl(k_pres<TR>, pres_grid(L), kBlock, 0, st, xh, xl, b, rT, rsplit, state, L.nx, L.ny, L.nz, 1.0f / (L.h * L.h), ps->partials);
+  if (L.nx % 2 == 0 && L.nz % (GZ * RZ) == 0)
+    launch_pdl(k_pres2<TR, true>, pres_grid(L), kBlock, 0, st, xh, xl, b, rT, rsplit, state, L.nx, L.ny, L.nz, 1.0f / (L.h * L.h),
+               ps->partials);
+  else if (L.nx % 2 == 0)
+    launch_pdl(k_pres2<TR, false>, pres_grid(L), kBlock, 0, st, xh, xl, b, rT, rsplit, state, L.nx, L.ny, L.nz, 1.0f / (L.h * L.h),
+               ps->partials);
+  else
+    launch_pdl(k_pres<TR>, pres_grid(L), kBlock, 0, st, xh, xl, b, rT, rsplit, state, L.nx, L.ny, L.nz, 1.0f / (L.h * L.h), ps->partials);
 }
 void pres(FirePoisson* ps, const PState* state, const float* b, const float* xh, const float* xl, bool write, cudaStream_t st) {
   const PLevel& L = ps->levels[0];
@@ -800,7 +1070,8 @@ int fire_poisson_create(const int res[3], float h, int precision, int device, Fi
     PLevel& L = ps->levels[l];
     L.nx = M.nx; L.ny = M.ny; L.nz = M.nz; L.h = M.h;
     L.sto = (ps->ir && l < ps->tailFirst) ? sto : STO_F32;
-    L.split = (ps->ir && l < ps->tailFirst && M.nx % 2 == 0) ? 1 : 0;   // the tail's levels stay plain
+    // level 0 (the only level whose arrays outgrow L2) in the red-black split layout; the rest plain
+    L.split = (ps->ir && l == 0 && l < ps->tailFirst && M.nx % 2 == 0) ? 1 : 0;
     const size_t bytes = align_up((size_t)M.nx * M.ny * M.nz * elem_bytes(L.sto));
     if (l == 0 && !ps->ir) { pOff[l] = bOff[l] = (size_t)-1; continue; }
     pOff[l] = off; off += bytes;
@@ -860,7 +1131,8 @@ int fire_poisson_solve(FirePoisson* ps, const float* b, float* x, float* x_lo, d
   if (x_lo && ((const void*)x_lo == (const void*)x || (const void*)x_lo == (const void*)b)) return FIRE_ERR_BAD_ARG;
   if (ps->ir && (inner_cycles < 1 || inner_cycles > 16)) return FIRE_ERR_BAD_ARG;
   if (!ps->ir) { inner_cycles = 1; x_lo = nullptr; }
-  if (((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(x_lo)) & 15u) != 0) return FIRE_ERR_BAD_ARG;   // float4 update
+  // the update and the residual read x, x_lo and b as float2 pairs
+  if (((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(x_lo) | reinterpret_cast<uintptr_t>(b)) & 15u) != 0) return FIRE_ERR_BAD_ARG;
   DeviceGuard dg(ps->device);
   if (!ps->exec || ps->gb != b || ps->gx != x || ps->gxl != x_lo || ps->gtol != tol || ps->gmax != max_iters || ps->ginner != inner_cycles) {
     const int rc = build_graph(ps, b, x, x_lo, tol, max_iters, inner_cycles);
@@ -890,6 +1162,7 @@ int fire_poisson_result(FirePoisson* ps, FirePoissonResult* out) {
 
 int fire_poisson_residual(FirePoisson* ps, const float* b, const float* x, const float* x_lo, double* rel) {
   if (!ps || !b || !x || !rel) return FIRE_ERR_BAD_ARG;
+  if (((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(x_lo) | reinterpret_cast<uintptr_t>(b)) & 15u) != 0) return FIRE_ERR_BAD_ARG;
   DeviceGuard dg(ps->device);
   cudaStream_t st = ps->capStream;
   launch_pdl(k_sumsq, dim3(SUMSQ_CTAS), dim3(NT), 0, st, b, ps->cells, ps->partials);

@@ -149,13 +149,16 @@ def test_fp32_form_is_the_step_vcycle(oracle_mod):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["ir32", "fp16", "bf16"])
-def test_solve_to_tolerance(oracle_mod, precision):
+@pytest.mark.parametrize("precision,res", [("ir32", (64, 128, 64)), ("fp16", (64, 128, 64)), ("bf16", (64, 128, 64)),
+                                           ("fp16", (34, 64, 32)), ("bf16", (36, 40, 24))])
+def test_solve_to_tolerance(oracle_mod, precision, res):
     """The refinement forms reach 1e-6 relative residual on the solution pair; the FP64 oracle recomputes
-    that residual and its CG solution bounds the error."""
+    that residual and its CG solution bounds the error.  Grids cover the paired red-black sweep (nx % 4 == 0),
+    the single-cell one (34: nx % 4 == 2, odd next level) and a z extent that is no multiple of the residual
+    kernel's planes (24)."""
     torch = _torch()
     import fire_sim as F
-    res, h, tol = (64, 128, 64), 0.005, 1e-6
+    h, tol = 0.005, 1e-6
     ps = F.Poisson(res, h, precision)
     n = res[0] * res[1] * res[2]
     b = torch.empty(n, dtype=torch.float32, device="cuda")
@@ -164,7 +167,7 @@ def test_solve_to_tolerance(oracle_mod, precision):
     ps.make_rhs(b, seed=3, n_sources=32, noise=1e-3)
     ps.solve(b, x, tol=tol, max_iters=40, x_lo=lo)
     r = ps.result()
-    assert r["rel_residual"] <= tol and 1 <= r["iterations"] <= 20, r
+    assert r["rel_residual"] <= tol and 1 <= r["iterations"] < 40, r
     shape = (res[2], res[1], res[0])
     bnp = b.cpu().numpy().reshape(shape).astype(np.float64)
     x64 = x.cpu().numpy().reshape(shape).astype(np.float64) + lo.cpu().numpy().reshape(shape).astype(np.float64)
