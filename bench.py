@@ -275,6 +275,74 @@ def run_poisson(dev: int, reps: int = 3):
                     "coarsest solve; fp32: the step's V(2,2) cycle on an FP32 x (stalls at its representation floor)"}
 
 
+# Ensemble: 64 independent fires, 16 each at 32x64x32, 48x96x48, 64x128x64 and 96x192x96 cells of 1.25 cm,
+# each with its own seed and 2-8 spots of 1-4 g/s, 4 V(2,2) cycles per step, dt = 1/120 s.
+ENSEMBLE = dict(name="ensemble-64-fires", grids=((32, 64, 32), (48, 96, 48), (64, 128, 64), (96, 192, 96)), per_grid=16,
+                cell_m=0.0125, dt=1.0 / 120.0, vcycles=4, preroll=20)
+
+
+def _ensemble_members():
+    rng = np.random.default_rng(4)
+    members = []
+    for g in ENSEMBLE["grids"]:
+        for k in range(ENSEMBLE["per_grid"]):
+            size = tuple(ENSEMBLE["cell_m"] * v for v in g)
+            members.append(dict(res=g, size=size, seed=1000 + len(members), spots=int(rng.integers(2, 9))))
+    return members
+
+
+def _ensemble_configure(sim, m, F):
+    sim.set_spots(F.make_spots(m["seed"], m["spots"], 1.0, 4.0, 0.02, 0.3 * m["size"][0]))
+    sim.set_params({"seed": float(m["seed"]), "vortEps": 0.3, "turbAmp": 0.2})
+    sim.set_soot_age(0.02, 0.06)
+    sim.set_bed_gain(0.0)
+
+
+def run_ensemble(dev: int, steps: int = 20):
+    """Aggregate cell updates/s of the 64-fire ensemble stepped by batched launches, against the same 64
+    simulations stepped one after another (each its own per-step CUDA graph)."""
+    import torch
+    import fire_sim as F
+    E = ENSEMBLE
+    members = _ensemble_members()
+    cells = sum(int(np.prod(m["res"])) for m in members)
+    st = torch.cuda.current_stream(dev)
+    ens = F.Ensemble(members, vcycles=E["vcycles"], device=dev)
+    for s, m in zip(ens.members, members):
+        _ensemble_configure(s, m, F)
+    ens.step(E["dt"], E["preroll"], stream=st.cuda_stream)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    ens.step(E["dt"], steps, stream=st.cuda_stream)
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms_batched = e0.elapsed_time(e1) / steps
+    ens.close()
+    sims = []
+    for m in members:
+        s = F.FireSim(res=m["res"], size=m["size"], vcycles=E["vcycles"], device=dev)
+        _ensemble_configure(s, m, F)
+        sims.append(s)
+    for s in sims:
+        s.step(E["dt"], E["preroll"], stream=st.cuda_stream)
+    torch.cuda.synchronize(dev)
+    e0.record(st)
+    for _ in range(steps):
+        for s in sims:
+            s.step(E["dt"], 1, stream=st.cuda_stream)
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms_single = e0.elapsed_time(e1) / steps
+    for s in sims:
+        s.close()
+    return {"workload": E["name"], "members": len(members), "cells": cells, "steps": steps,
+            "ms_per_step_batched": ms_batched, "ms_per_step_one_at_a_time": ms_single,
+            "gcell_updates_per_s_batched": cells / (ms_batched * 1e-3) / 1e9,
+            "gcell_updates_per_s_one_at_a_time": cells / (ms_single * 1e-3) / 1e9,
+            "speedup": ms_single / ms_batched}
+
+
 # ------------------------------------------------------------------------------------------ arms
 def run_ours(args):
     import torch
@@ -387,9 +455,13 @@ def run_ours(args):
         "diag_last_step": {"hrr_kw": float(diag[16]), "T_max": 293.0 + 1000.0 * float(diag[1])},
         "poisson": None,
     }
-    if world == 1 and not args.no_poisson:
-        sim.close()   # frees the step's arena before the 256x512x256 solves
-        out["poisson"] = run_poisson(dev)
+    out["ensemble"] = None
+    if world == 1 and not (args.no_poisson and args.no_ensemble):
+        sim.close()   # frees the step's arena before the standalone workloads
+        if not args.no_poisson:
+            out["poisson"] = run_poisson(dev)
+        if not args.no_ensemble:
+            out["ensemble"] = run_ensemble(dev)
     return out
 
 
@@ -447,6 +519,7 @@ def main(argv=None):
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--preroll", type=int, default=WORKLOAD["preroll"], help="untimed steps that develop the fire")
     ap.add_argument("--no-poisson", action="store_true", help="skip the standalone 256x512x256 pressure-solve timings")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-fire ensemble timings")
     ap.add_argument("--mg-fixed", type=int, default=0,
                     help="profiling aid: N fixed V-cycles per step instead of the residual-driven solve")
     args = ap.parse_args(argv)

@@ -250,6 +250,27 @@ int fire_make_spots(uint32_t seed, int n, float flux_lo, float flux_hi, float si
 #define FIRE_NOALLOC_SCRATCH_BYTES (8u * 1024u * 1024u)
 int fire_poisson_vcycles_noalloc(float* p, const float* b, int nx, int ny, int nz, float h, int cycles, void* stream);
 
+/* ---- ensembles of independent simulations ------------------------------------------------------
+ * n (<= 64) simulations of possibly different grids advanced together: each stage of a step is one
+ * kernel launch over all members, the multigrid levels are batched level by level and the members'
+ * shared-memory tails run in one launch per tail form, all captured in one CUDA graph per step.  The
+ * members are FireSim handles owned by the ensemble: configure them (params, spots, soot age, events) and
+ * read them (fields, stats) with the fire_sim_* functions, but step them only through the ensemble and do
+ * not destroy them.  Every member must use fixed V-cycles (mg_max_cycles = 0) with the same count, the
+ * same device and the same noise_seed (the noise/curl tables are shared).  The batched kernels run the
+ * per-simulation kernels' bodies, so a member's fields are those fire_sim_step gives it alone up to FP32
+ * rounding (FMA contraction may differ between the two compiled forms).  No counterpart in the reference
+ * (one FireSim per page).                                                                               */
+typedef struct FireEnsemble FireEnsemble;
+int fire_ensemble_create(const FireConfig* cfgs, int n, FireEnsemble** out);
+int fire_ensemble_destroy(FireEnsemble* e);
+int fire_ensemble_size(FireEnsemble* e);
+int fire_ensemble_sim(FireEnsemble* e, int index, FireSim** out);
+/* n_steps steps of dt seconds for every member, asynchronous on `stream`.                              */
+int fire_ensemble_step(FireEnsemble* e, float dt, int n_steps, void* stream);
+int fire_ensemble_sync(FireEnsemble* e);
+const char* fire_ensemble_last_error(FireEnsemble* e);
+
 /* ---- standalone pressure Poisson solver --------------------------------------------------------
  * The step's pressure equation (src/sim.js:415-495, 576-599: cell-centred 7-point Laplacian, p = 0 on the
  * side and top faces, zero gradient at the floor, levels halved while every dimension is even and the

@@ -917,3 +917,248 @@ int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream) {
 }
 
 }  // extern "C"
+
+// ==================================================================================================
+// Ensemble: many independent simulations of uneven sizes advanced together.  Every stage of a step is
+// one launch over all members (a BatchMap concatenates their block grids), the multigrid levels outside
+// each member's shared-memory tail are batched level by level, and the tails of all members run in one
+// launch per tail form; the whole step is one CUDA graph.  Members are ordinary FireSim handles (created
+// and owned by the ensemble) so their parameters, spots, events, fields and diagnostics use the FireSim
+// API; their parameter blocks are staged into one contiguous device array and copied with one copy.
+struct FireEnsemble {
+  int device = 0;
+  std::vector<FireSim*> sims;
+  float* dBlocks = nullptr;                 // n x BLOCK_FLOATS on the device
+  float* hRing = nullptr;                   // ENS_RING slots of n x BLOCK_FLOATS, pinned
+  cudaEvent_t ringEv[4] = {};
+  bool ringUsed[4] = {};
+  int ringPos = 0;
+  void* dTail[2] = {nullptr, nullptr};      // tail descriptors by form (single CTA, cluster)
+  int tailCount[2] = {0, 0};
+  size_t tailSmem[2] = {0, 0};
+  int* dErr = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long steps = 0;
+  std::string err;
+};
+
+namespace {
+constexpr int ENS_RING = 4;
+
+// Appends simulation `inst` with a gx x gy x gz block grid to a map.
+void map_add(BatchMap& m, int inst, dim3 g) {
+  const int k = m.n++;
+  m.inst[k] = inst;
+  m.gx[k] = (int)g.x;
+  m.gy[k] = (int)g.y;
+  m.prefix[k + 1] = m.prefix[k] + (int)(g.x * g.y * g.z);
+}
+BatchMap map_empty() {
+  BatchMap m;
+  std::memset(&m, 0, sizeof m);
+  return m;
+}
+
+int ens_err(FireEnsemble* e, int code, const char* msg) {
+  if (e) e->err = msg;
+  return code;
+}
+
+// Records one ensemble step (src/sim.js:633-644 for every member): adv1, adv2, curl + forces, div,
+// `vcycles` V(2,2) cycles, project.
+int record_ensemble_step(FireEnsemble* e, cudaStream_t st) {
+  const int n = (int)e->sims.size();
+  StepBatch SB;
+  std::memset(&SB, 0, sizeof SB);
+  BatchMap cellMap = map_empty(), forcesMap = map_empty();
+  int depth = 0;
+  for (int i = 0; i < n; ++i) {
+    FireSim* s = e->sims[i];
+    SB.s[i] = StepInst{e->dBlocks + (size_t)i * BLOCK_FLOATS, s->f, s->d, s->levels[0].b, s->levels[0].p};
+    map_add(cellMap, i, step_grid(s->d));
+    map_add(forcesMap, i, forces_grid(s->d));
+    depth = std::max(depth, std::min(s->tailFirst, (int)s->levels.size() - 1));
+  }
+  // per level: the members that have it outside their tail, and every member's level l and l + 1
+  std::vector<BatchMap> smoothMap(depth, map_empty()), coarseMap(depth, map_empty());
+  std::vector<LevelBatch> LB(depth + 1);
+  for (int l = 0; l <= depth; ++l) std::memset(&LB[l], 0, sizeof(LevelBatch));
+  for (int i = 0; i < n; ++i) {
+    FireSim* s = e->sims[i];
+    const int top = std::min(s->tailFirst, (int)s->levels.size() - 1);
+    for (int l = 0; l <= depth && l < (int)s->levels.size(); ++l) LB[l].l[i] = s->levels[l];
+    for (int l = 0; l < top; ++l) {
+      map_add(smoothMap[l], i, smooth_grid(s->levels[l]));
+      map_add(coarseMap[l], i, coarse_grid(s->levels[l + 1]));
+    }
+  }
+  const int V = e->sims[0]->vcycles;
+  launch_adv1_batch(cellMap, SB, st);
+  launch_adv2_batch(cellMap, SB, st);
+  launch_forces_batch(forcesMap, SB, e->sims[0]->noise, e->sims[0]->curl, st);
+  launch_div_batch(cellMap, SB, st);
+  for (int c = 0; c < V; ++c) {
+    for (int l = 0; l < depth; ++l) {
+      for (int k = 0; k < 2; ++k) { launch_smooth_batch(smoothMap[l], LB[l], 0, st); launch_smooth_batch(smoothMap[l], LB[l], 1, st); }
+      launch_restrict_batch(coarseMap[l], LB[l], LB[l + 1], st);
+    }
+    for (int kind = 0; kind < 2; ++kind)
+      launch_tail_batch(kind, e->dTail[kind], e->tailCount[kind], e->tailSmem[kind], 2, 2, e->dErr, st);
+    for (int l = depth - 1; l >= 0; --l) {
+      launch_prolong_batch(coarseMap[l], LB[l], LB[l + 1], st);
+      for (int k = 0; k < 2; ++k) { launch_smooth_batch(smoothMap[l], LB[l], 0, st); launch_smooth_batch(smoothMap[l], LB[l], 1, st); }
+    }
+  }
+  launch_project_batch(cellMap, SB, st);
+  return cudaGetLastError() == cudaSuccess ? FIRE_OK : ens_err(e, FIRE_ERR_CUDA, "ensemble step launch failed");
+}
+
+int build_ensemble_graph(FireEnsemble* e) {
+  if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+  if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
+  cudaStream_t st;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return FIRE_ERR_CUDA;
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaStreamDestroy(st); return FIRE_ERR_CUDA; }
+  const int rc = record_ensemble_step(e, st);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &g);
+  cudaStreamDestroy(st);
+  if (rc || ce != cudaSuccess) { if (g) cudaGraphDestroy(g); return rc ? rc : ens_err(e, FIRE_ERR_CUDA, "ensemble capture failed"); }
+  e->graph = g;
+  if (cudaGraphInstantiate(&e->exec, g, 0) != cudaSuccess) return ens_err(e, FIRE_ERR_CUDA, "ensemble graph instantiate failed");
+  return FIRE_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int fire_ensemble_destroy(FireEnsemble* e) {
+  if (!e) return FIRE_ERR_BAD_ARG;
+  cudaSetDevice(e->device);
+  cudaDeviceSynchronize();
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  if (e->graph) cudaGraphDestroy(e->graph);
+  for (int k = 0; k < ENS_RING; ++k) if (e->ringEv[k]) cudaEventDestroy(e->ringEv[k]);
+  if (e->hRing) cudaFreeHost(e->hRing);
+  if (e->dBlocks) cudaFree(e->dBlocks);
+  for (int k = 0; k < 2; ++k) if (e->dTail[k]) cudaFree(e->dTail[k]);
+  if (e->dErr) cudaFree(e->dErr);
+  for (FireSim* s : e->sims) fire_sim_destroy(s);
+  delete e;
+  return FIRE_OK;
+}
+
+int fire_ensemble_create(const FireConfig* cfgs, int n, FireEnsemble** out) {
+  if (!cfgs || !out || n < 1 || n > BATCH_MAX) return FIRE_ERR_BAD_ARG;
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    // fixed cycle counts only (the residual-driven loop is per simulation), one device and table seed
+    if (cfgs[i].mg_max_cycles != 0 || cfgs[i].vcycles != cfgs[0].vcycles || cfgs[i].device != cfgs[0].device ||
+        cfgs[i].noise_seed != cfgs[0].noise_seed)
+      return FIRE_ERR_BAD_ARG;
+  }
+  FireEnsemble* e = new FireEnsemble();
+  e->device = cfgs[0].device;
+  for (int i = 0; i < n; ++i) {
+    FireSim* s = nullptr;
+    const int rc = fire_sim_create(&cfgs[i], nullptr, 0, &s);
+    if (rc) { fire_ensemble_destroy(e); return rc; }
+    e->sims.push_back(s);
+    if (s->tailFirst >= (int)s->levels.size()) { fire_ensemble_destroy(e); return FIRE_ERR_BAD_ARG; }   // needs a tail
+  }
+  cudaSetDevice(e->device);
+  const size_t blkBytes = sizeof(float) * BLOCK_FLOATS * (size_t)n;
+  if (cudaMalloc((void**)&e->dBlocks, blkBytes) != cudaSuccess || cudaMalloc((void**)&e->dErr, sizeof(int)) != cudaSuccess ||
+      cudaMemset(e->dErr, 0, sizeof(int)) != cudaSuccess ||
+      cudaHostAlloc((void**)&e->hRing, blkBytes * ENS_RING, cudaHostAllocDefault) != cudaSuccess) {
+    fire_ensemble_destroy(e);
+    return FIRE_ERR_OOM;
+  }
+  for (int k = 0; k < ENS_RING; ++k)
+    if (cudaEventCreateWithFlags(&e->ringEv[k], cudaEventDisableTiming) != cudaSuccess) { fire_ensemble_destroy(e); return FIRE_ERR_CUDA; }
+  // tail descriptors, grouped by form
+  std::vector<unsigned char> desc[2];
+  for (int i = 0; i < n; ++i) {
+    FireSim* s = e->sims[i];
+    const int L = (int)s->levels.size();
+    const int kind = tail_kind(s->levels.data(), s->tailFirst, L);
+    const size_t sz = tail_desc_size(kind);
+    desc[kind].resize(desc[kind].size() + sz);
+    tail_desc_fill(s->levels.data(), s->tailFirst, L, s->coarseIters, desc[kind].data() + desc[kind].size() - sz);
+    e->tailCount[kind] += 1;
+    e->tailSmem[kind] = std::max(e->tailSmem[kind], tail_smem_bytes(s->levels.data(), s->tailFirst, L));
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (!e->tailCount[k]) continue;
+    if (cudaMalloc(&e->dTail[k], desc[k].size()) != cudaSuccess ||
+        cudaMemcpy(e->dTail[k], desc[k].data(), desc[k].size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+      fire_ensemble_destroy(e);
+      return FIRE_ERR_CUDA;
+    }
+  }
+  *out = e;
+  return FIRE_OK;
+}
+
+int fire_ensemble_size(FireEnsemble* e) { return e ? (int)e->sims.size() : FIRE_ERR_BAD_ARG; }
+
+int fire_ensemble_sim(FireEnsemble* e, int i, FireSim** out) {
+  if (!e || !out || i < 0 || i >= (int)e->sims.size()) return FIRE_ERR_BAD_ARG;
+  *out = e->sims[i];
+  return FIRE_OK;
+}
+
+int fire_ensemble_step(FireEnsemble* e, float dt, int n_steps, void* stream) {
+  if (!e || n_steps < 0 || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
+  if (cudaSetDevice(e->device) != cudaSuccess) return FIRE_ERR_CUDA;
+  cudaStream_t st = as_stream(stream);
+  if (!e->exec) {
+    const int rc = build_ensemble_graph(e);
+    if (rc) return rc;
+  }
+  const int n = (int)e->sims.size();
+  for (int step = 0; step < n_steps; ++step) {
+    const int k = e->ringPos;
+    e->ringPos = (k + 1) % ENS_RING;
+    if (e->ringUsed[k] && cudaEventSynchronize(e->ringEv[k]) != cudaSuccess) return FIRE_ERR_CUDA;
+    e->ringUsed[k] = true;
+    float* slot = e->hRing + (size_t)k * BLOCK_FLOATS * n;
+    for (int i = 0; i < n; ++i) {
+      FireSim* s = e->sims[i];
+      advance_events(s, dt);
+      fill_block(s, dt, slot + (size_t)i * BLOCK_FLOATS);
+      if (!s->geoReady || s->logsDirty) {   // emitter geometry from this member's own block and logs
+        int rc = upload_block(s, dt, st, true);
+        if (rc) return rc;
+        if ((rc = ensure_geo(s, st))) return rc;
+      }
+    }
+    if (cudaMemcpyAsync(e->dBlocks, slot, sizeof(float) * BLOCK_FLOATS * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaEventRecord(e->ringEv[k], st) != cudaSuccess || cudaGraphLaunch(e->exec, st) != cudaSuccess)
+      return FIRE_ERR_CUDA;
+    for (FireSim* s : e->sims) {                                               // src/sim.js:646-647
+      s->time += dt;
+      s->frame += 1;
+      s->stepsRun += 1;
+    }
+    e->steps += 1;
+  }
+  return FIRE_OK;
+}
+
+int fire_ensemble_sync(FireEnsemble* e) {
+  if (!e) return FIRE_ERR_BAD_ARG;
+  if (cudaSetDevice(e->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return FIRE_ERR_CUDA;
+  int err = 0;
+  if (cudaMemcpy(&err, e->dErr, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FIRE_ERR_CUDA;
+  if (err) {
+    cudaMemset(e->dErr, 0, sizeof(int));
+    return ens_err(e, FIRE_ERR_CUDA, "a device-side wait timed out (multigrid tail bulk copy)");
+  }
+  return FIRE_OK;
+}
+
+const char* fire_ensemble_last_error(FireEnsemble* e) { return e ? e->err.c_str() : "null ensemble"; }
+
+}  // extern "C"

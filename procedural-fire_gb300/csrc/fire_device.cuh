@@ -100,6 +100,20 @@ __device__ __forceinline__ void sum_pairs_fixed(const float4* partials, int coun
   }
 }
 
+// The simulation of this CTA of a batched launch and the CTA's position in that simulation's grid
+// (binary search of the flat block index in the map's prefix sums).
+__device__ __forceinline__ void batch_locate(const BatchMap& m, uint3& blk, int& inst) {
+  const int b = (int)blockIdx.x;
+  int lo = 0, hi = m.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (m.prefix[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  const int lb = b - m.prefix[lo], gx = m.gx[lo], gy = m.gy[lo];
+  blk = make_uint3((unsigned)(lb % gx), (unsigned)((lb / gx) % gy), (unsigned)(lb / (gx * gy)));
+  inst = m.inst[lo];
+}
+
 struct f3 { float x, y, z; };
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }
 __device__ __forceinline__ f3 xyz(const float4& v) { return mk3(v.x, v.y, v.z); }

@@ -56,6 +56,30 @@ struct MGLevel {
   float* b;
 };
 
+// ---- batched launches over many independent simulations ----
+// A batched launch is one 1D grid whose flat blocks are the concatenated block grids of n simulations:
+// simulation inst[k] owns flat blocks [prefix[k], prefix[k+1]) laid out as its own gx x gy x gz grid.
+constexpr int BATCH_MAX = 64;
+struct BatchMap {
+  int n;
+  int prefix[BATCH_MAX + 1];
+  int gx[BATCH_MAX], gy[BATCH_MAX];
+  int inst[BATCH_MAX];
+};
+// What the step stages of one simulation need (device-resident array, one entry per simulation).
+struct StepInst {
+  const float* P;     // parameter block
+  Fields f;
+  Dims d;
+  float* b0;          // level-0 right-hand side (written by div)
+  const float* p0;    // level-0 pressure (read by project)
+};
+// Passed by value as a kernel parameter (it lives in the constant bank, so a CTA's simulation pointers
+// cost no registers to hold).
+struct StepBatch { StepInst s[BATCH_MAX]; };
+// One multigrid level of each simulation of a batch, by simulation index (kernel parameter).
+struct LevelBatch { MGLevel l[BATCH_MAX]; };
+
 // ---- kernel launchers (fire_tables.cu) ----
 void launch_noise_table(uint2* noise, int N, int seed, cudaStream_t st);
 void launch_curl_table(const uint2* noise, uint2* curl, int N, cudaStream_t st);
@@ -74,6 +98,14 @@ void launch_forces_recompute(const float* P, Fields f, const uint2* noise, const
 cudaError_t step_configure();
 void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st);
 void launch_project(const float* P, Fields f, const float* p0, Dims d, cudaStream_t st);
+// Block grids of the per-cell stages (adv1, adv2, div, project) and of the tiled forces stage.
+dim3 step_grid(Dims d);
+dim3 forces_grid(Dims d);
+void launch_adv1_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st);
+void launch_adv2_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st);
+void launch_forces_batch(const BatchMap& m, const StepBatch& I, const uint2* noise, const uint2* curl, cudaStream_t st);
+void launch_div_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st);
+void launch_project_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st);
 
 // ---- kernel launchers (fire_mg.cu) ----
 void launch_smooth(const MGLevel& L, int color, cudaStream_t st);
@@ -94,6 +126,19 @@ void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int
                  bool coarse64 = false, const double* cinv = nullptr);
 // Opts the tail kernels into `max_tail_smem` bytes of dynamic shared memory on the current device.
 cudaError_t mg_configure(size_t max_tail_smem);
+// Batched forms: one launch per level operation over the simulations of a BatchMap.
+dim3 smooth_grid(const MGLevel& L);
+dim3 coarse_grid(const MGLevel& C);   // restriction into / prolongation from level C
+void launch_smooth_batch(const BatchMap& m, const LevelBatch& L, int color, cudaStream_t st);
+void launch_restrict_batch(const BatchMap& m, const LevelBatch& F, const LevelBatch& C, cudaStream_t st);
+void launch_prolong_batch(const BatchMap& m, const LevelBatch& F, const LevelBatch& C, cudaStream_t st);
+// Tails of many simulations in one launch: kind 0 = single-CTA form, 1 = cluster form.  The host fills
+// tail_desc_size(kind) bytes per simulation with tail_desc_fill (with that simulation's coarsest sweeps),
+// copies them to the device, and launches `count` of them with the largest tail_smem_bytes among them.
+int tail_kind(const MGLevel* levels, int first, int n);
+size_t tail_desc_size(int kind);
+void tail_desc_fill(const MGLevel* levels, int first, int n, int coarse, void* out);
+void launch_tail_batch(int kind, const void* dev_descs, int count, size_t smem, int pre, int post, int* err, cudaStream_t st);
 constexpr size_t TAIL_SMEM_BUDGET = 200 * 1024;
 // Residual / RHS sums of squares on a level: partial sums per CTA then a fixed-order final sum.
 int residual_partials_count(const MGLevel& L);

@@ -14,6 +14,7 @@
 //    inside it run on one warp with __syncwarp, so the coarsest sweeps cost no CTA-wide barriers;
 //  * every kernel uses programmatic dependent launch (fire_launch.cuh) so consecutive launches overlap.
 #include <algorithm>
+#include <cstring>
 #include <cooperative_groups.h>
 
 #include "fire_device.cuh"
@@ -46,12 +47,12 @@ __device__ __forceinline__ float rb_update(const float* p, const float* b, int x
 #define FIRE_SMOOTH_Z 2
 #endif
 constexpr int SMZ = FIRE_SMOOTH_Z;
-__global__ void __launch_bounds__(GX * GY * GZ) k_smooth(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
-                                                         float h, int color) {
+__device__ __forceinline__ void smooth_body(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz, float h, int color,
+                                            uint3 blk) {
   pdl_wait();
   pdl_trigger();
-  const int gx = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y;
-  const int zb = (blockIdx.z * GZ + threadIdx.z) * SMZ;
+  const int gx = blk.x * GX + threadIdx.x, y = blk.y * GY + threadIdx.y;
+  const int zb = (blk.z * GZ + threadIdx.z) * SMZ;
   if (y >= ny) return;
   const float h2 = h * h;
   float v[SMZ];
@@ -89,12 +90,12 @@ __device__ __forceinline__ float restrict_cell(const float* p, const float* b, i
   }
   return acc * 0.125f;
 }
-__global__ void __launch_bounds__(GX * GY * GZ) k_restrict(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
-                                                           float h, float* __restrict__ bc, float* __restrict__ pc) {
+__device__ __forceinline__ void restrict_body(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz, float h,
+                                              float* __restrict__ bc, float* __restrict__ pc, uint3 blk) {
   pdl_wait();
   pdl_trigger();
   const int cnx = nx / 2, cny = ny / 2, cnz = nz / 2;
-  const int cx = blockIdx.x * GX + threadIdx.x, cy = blockIdx.y * GY + threadIdx.y, cz = blockIdx.z * GZ + threadIdx.z;
+  const int cx = blk.x * GX + threadIdx.x, cy = blk.y * GY + threadIdx.y, cz = blk.z * GZ + threadIdx.z;
   if (cx >= cnx || cy >= cny || cz >= cnz) return;
   const float ih2 = 1.0f / (h * h);
   const int t = cx + cnx * (cy + cny * cz);
@@ -126,11 +127,11 @@ __device__ __forceinline__ float prolong_cell(const float* pc, int x, int y, int
 // loaded once and the 8 fine children are formed from it.  For fine index c = 2 cc + d the trilinear base is
 // g0 = cc - 1 + d with fraction 0.75 (d = 0) or 0.25 (d = 1), so child d reads coarse offsets d-1 and d;
 // each child's sum runs in prolong_cell's order, so the result is identical.
-__global__ void __launch_bounds__(GX * GY * GZ) k_prolong(float* __restrict__ p, const float* __restrict__ pc, int nx, int ny, int nz) {
+__device__ __forceinline__ void prolong_body(float* __restrict__ p, const float* __restrict__ pc, int nx, int ny, int nz, uint3 blk) {
   pdl_wait();
   pdl_trigger();
   const int ncx = nx / 2, ncy = ny / 2, ncz = nz / 2;
-  const int cx = blockIdx.x * GX + threadIdx.x, cy = blockIdx.y * GY + threadIdx.y, cz = blockIdx.z * GZ + threadIdx.z;
+  const int cx = blk.x * GX + threadIdx.x, cy = blk.y * GY + threadIdx.y, cz = blk.z * GZ + threadIdx.z;
   if (cx >= ncx || cy >= ncy || cz >= ncz) return;
   float v[3][3][3];   // [dz][dy][dx] for offsets -1..1
 #pragma unroll
@@ -165,6 +166,38 @@ __global__ void __launch_bounds__(GX * GY * GZ) k_prolong(float* __restrict__ p,
       }
 }
 
+// Per-level kernels of one simulation, and their batched forms over many simulations (one grid; each CTA
+// finds its simulation's level from the BatchMap and runs the same body).
+__global__ void __launch_bounds__(GX * GY * GZ) k_smooth(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz, float h,
+                                                         int color) {
+  smooth_body(p, b, nx, ny, nz, h, color, blockIdx);
+}
+__global__ void __launch_bounds__(GX * GY * GZ) k_restrict(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
+                                                           float h, float* __restrict__ bc, float* __restrict__ pc) {
+  restrict_body(p, b, nx, ny, nz, h, bc, pc, blockIdx);
+}
+__global__ void __launch_bounds__(GX * GY * GZ) k_prolong(float* __restrict__ p, const float* __restrict__ pc, int nx, int ny, int nz) {
+  prolong_body(p, pc, nx, ny, nz, blockIdx);
+}
+__global__ void __launch_bounds__(GX * GY * GZ) k_smooth_b(const __grid_constant__ BatchMap m, const __grid_constant__ LevelBatch L, int color) {
+  uint3 blk; int i;
+  batch_locate(m, blk, i);
+  const MGLevel& v = L.l[i];
+  smooth_body(v.p, v.b, v.nx, v.ny, v.nz, v.h, color, blk);
+}
+__global__ void __launch_bounds__(GX * GY * GZ) k_restrict_b(const __grid_constant__ BatchMap m, const __grid_constant__ LevelBatch F,
+                                                             const __grid_constant__ LevelBatch C) {
+  uint3 blk; int i;
+  batch_locate(m, blk, i);
+  restrict_body(F.l[i].p, F.l[i].b, F.l[i].nx, F.l[i].ny, F.l[i].nz, F.l[i].h, C.l[i].b, C.l[i].p, blk);
+}
+__global__ void __launch_bounds__(GX * GY * GZ) k_prolong_b(const __grid_constant__ BatchMap m, const __grid_constant__ LevelBatch F,
+                                                            const __grid_constant__ LevelBatch C) {
+  uint3 blk; int i;
+  batch_locate(m, blk, i);
+  prolong_body(F.l[i].p, C.l[i].p, F.l[i].nx, F.l[i].ny, F.l[i].nz, blk);
+}
+
 // ---------------- single-CTA tail V-cycle out of shared memory ----------------
 // Cells are visited as a flat index split into (x, y, z) with a float-reciprocal quotient and a one-step
 // correction (exact for indices below 2^24), several times cheaper than integer division.  Levels with
@@ -180,6 +213,7 @@ struct TailLevels {
   int off[TAIL_MAX_LEVELS];    // float offset of level l's p in shared memory (b follows p)
   float* gp[TAIL_MAX_LEVELS];  // global copies (written back at the end)
   float* gb[TAIL_MAX_LEVELS];
+  int coarse;                  // coarsest-level sweeps (used by the batched tails; per-simulation launches pass it)
   int coarse64;                // 1: the coarsest level is solved in FP64: p = cinv b with the dense inverse
   int doff;                    //    (transposed, global memory) if cinv is set, else `coarse` FP64 sweeps on a
   const double* cinv;          //    double copy at float offset doff
@@ -466,7 +500,7 @@ __device__ __forceinline__ bool bulk_ok(const void* g, const void* s, unsigned b
   return ((reinterpret_cast<uintptr_t>(g) | reinterpret_cast<uintptr_t>(s) | bytes) & 15u) == 0;
 }
 
-__global__ void __launch_bounds__(TAIL_THREADS, 1) k_tail(TailLevels T, int pre, int post, int coarse, int* err) {
+__device__ __forceinline__ void tail_body(const TailLevels& T, int pre, int post, int coarse, int* err) {
   extern __shared__ float sm[];
   __shared__ alignas(8) uint64_t bar;
   pdl_wait();
@@ -686,7 +720,7 @@ __device__ void ct_prolong(const cg::cluster_group& cl, const DSlab& s, const CS
   }
   cl.sync();
 }
-__global__ void __launch_bounds__(TAIL_THREADS, 1) k_ctail(CTailLevels T, int pre, int post, int coarse) {
+__device__ __forceinline__ void ctail_body(const CTailLevels& T, int pre, int post, int coarse) {
   extern __shared__ float4 sm4[];
   float* sm = reinterpret_cast<float*>(sm4);
   const cg::cluster_group cl = cg::this_cluster();
@@ -751,6 +785,20 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_ctail(CTailLevels T, int pr
       for (int t = tid; t < n; t += TAIL_THREADS) T.gp[g0 + t] = s.p[t];
     }
   }
+}
+
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_tail(TailLevels T, int pre, int post, int coarse, int* err) {
+  tail_body(T, pre, post, coarse, err);
+}
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_ctail(CTailLevels T, int pre, int post, int coarse) { ctail_body(T, pre, post, coarse); }
+// Batched tails: CTA b (single-CTA form) or cluster b (cluster form) runs the tail of simulation b.
+// Each simulation's coarsest sweeps come from its descriptor.
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_tail_b(const TailLevels* __restrict__ T, int pre, int post, int* err) {
+  tail_body(T[blockIdx.x], pre, post, T[blockIdx.x].coarse, err);
+}
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_ctail_b(const CTailLevels* __restrict__ T, int pre, int post) {
+  const CTailLevels& t = T[blockIdx.x / CTAIL_CLUSTER];
+  ctail_body(t, pre, post, t.G.coarse);
 }
 
 // ---------------- residual norms ||b - A p||^2 and ||b||^2 (FP64 above the thread, fixed order) ----------------
@@ -914,19 +962,14 @@ static TailLevels make_tail_levels(const MGLevel* levels, int first, int n, int 
     T.gp[l] = L.p; T.gb[l] = L.b;
     if (T.small == T.n && L.nx * L.ny * L.nz <= TAIL_WARP_CELLS) T.small = l;
   }
+  T.coarse = 0;
   T.coarse64 = coarse64 ? 1 : 0;
   T.doff = (int)tail_fp64_offset((size_t)off);
   T.cinv = coarse64 ? cinv : nullptr;
   return T;
 }
-void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st, bool coarse64,
-                 const double* cinv) {
-  const size_t smem = tail_smem_bytes(levels, first, n, coarse64);
-  const int nd = tail_dist_levels(levels, first, n);
-  if (nd == 0) {
-    launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), smem, st, make_tail_levels(levels, first, n, 0, coarse64, cinv), pre, post, coarse, err);
-    return;
-  }
+// The cluster tail's descriptor: the first nd levels distributed, the rest gathered on CTA 0.
+static CTailLevels make_ctail_levels(const MGLevel* levels, int first, int n, int nd, bool coarse64, const double* cinv) {
   CTailLevels T;
   T.nd = nd;
   int off = 0;
@@ -940,6 +983,17 @@ void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int
   T.gp = levels[first].p;
   T.gb = levels[first].b;
   T.G = make_tail_levels(levels, first + nd, n, off, coarse64, cinv);
+  return T;
+}
+void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st, bool coarse64,
+                 const double* cinv) {
+  const size_t smem = tail_smem_bytes(levels, first, n, coarse64);
+  const int nd = tail_dist_levels(levels, first, n);
+  if (nd == 0) {
+    launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), smem, st, make_tail_levels(levels, first, n, 0, coarse64, cinv), pre, post, coarse, err);
+    return;
+  }
+  const CTailLevels T = make_ctail_levels(levels, first, n, nd, coarse64, cinv);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CTAIL_CLUSTER);
   cfg.blockDim = dim3(TAIL_THREADS);
@@ -957,9 +1011,58 @@ void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int
   cudaLaunchKernelEx(&cfg, k_ctail, T, pre, post, coarse);
 }
 cudaError_t mg_configure(size_t max_tail_smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_tail_smem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_ctail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_tail_smem);
+  for (const void* k : {(const void*)k_tail, (const void*)k_ctail, (const void*)k_tail_b, (const void*)k_ctail_b}) {
+    const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_tail_smem);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+dim3 smooth_grid(const MGLevel& L) { return grid3((L.nx + 1) >> 1, L.ny, (L.nz + SMZ - 1) / SMZ); }
+dim3 coarse_grid(const MGLevel& C) { return grid3(C.nx, C.ny, C.nz); }
+void launch_smooth_batch(const BatchMap& m, const LevelBatch& L, int color, cudaStream_t st) {
+  launch_pdl(k_smooth_b, dim3(m.prefix[m.n]), kBlock, 0, st, m, L, color);
+}
+void launch_restrict_batch(const BatchMap& m, const LevelBatch& F, const LevelBatch& C, cudaStream_t st) {
+  launch_pdl(k_restrict_b, dim3(m.prefix[m.n]), kBlock, 0, st, m, F, C);
+}
+void launch_prolong_batch(const BatchMap& m, const LevelBatch& F, const LevelBatch& C, cudaStream_t st) {
+  launch_pdl(k_prolong_b, dim3(m.prefix[m.n]), kBlock, 0, st, m, F, C);
+}
+int tail_kind(const MGLevel* levels, int first, int n) { return tail_dist_levels(levels, first, n) > 0 ? 1 : 0; }
+size_t tail_desc_size(int kind) { return kind ? sizeof(CTailLevels) : sizeof(TailLevels); }
+void tail_desc_fill(const MGLevel* levels, int first, int n, int coarse, void* out) {
+  const int nd = tail_dist_levels(levels, first, n);
+  if (nd == 0) {
+    TailLevels T = make_tail_levels(levels, first, n, 0, false, nullptr);
+    T.coarse = coarse;
+    std::memcpy(out, &T, sizeof T);
+  } else {
+    CTailLevels T = make_ctail_levels(levels, first, n, nd, false, nullptr);
+    T.G.coarse = coarse;
+    std::memcpy(out, &T, sizeof T);
+  }
+}
+void launch_tail_batch(int kind, const void* dev_descs, int count, size_t smem, int pre, int post, int* err, cudaStream_t st) {
+  if (count <= 0) return;
+  if (kind == 0) {
+    launch_pdl(k_tail_b, dim3(count), dim3(TAIL_THREADS), smem, st, (const TailLevels*)dev_descs, pre, post, err);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CTAIL_CLUSTER * count);
+  cfg.blockDim = dim3(TAIL_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CTAIL_CLUSTER;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 2;
+  cudaLaunchKernelEx(&cfg, k_ctail_b, (const CTailLevels*)dev_descs, pre, post);
 }
 static dim3 residual_grid(const MGLevel& L) { return grid3(L.nx, L.ny, (L.nz + RZ - 1) / RZ); }
 int residual_partials_count(const MGLevel& L) {

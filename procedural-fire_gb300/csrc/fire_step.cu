@@ -21,16 +21,19 @@ constexpr int BX = 32, BY = 4, BZ = 2;
 struct CellId { int i, j, k; bool ok; };
 // Every stencil kernel starts here: wait for the predecessor grid (programmatic dependent launch), let the
 // successor's launch begin, and locate this thread's cell.
-__device__ __forceinline__ CellId cell_id(Dims d) {
+// `blk` is the CTA's position in the simulation's grid: blockIdx for a per-simulation launch, or the
+// position a batched launch derived from its flat block index (BatchMap).
+__device__ __forceinline__ CellId cell_id(Dims d, uint3 blk) {
   pdl_wait();
   pdl_trigger();
   CellId c;
-  c.i = blockIdx.x * BX + threadIdx.x;
-  c.j = blockIdx.y * BY + threadIdx.y;
-  c.k = blockIdx.z * BZ + threadIdx.z;
+  c.i = blk.x * BX + threadIdx.x;
+  c.j = blk.y * BY + threadIdx.y;
+  c.k = blk.z * BZ + threadIdx.z;
   c.ok = c.i < d.nx && c.j < d.ny && c.k < d.nz;
   return c;
 }
+__device__ __forceinline__ CellId cell_id(Dims d) { return cell_id(d, blockIdx); }
 static dim3 grid_for(Dims d) { return dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, (d.nz + BZ - 1) / BZ); }
 static dim3 block_shape() { return dim3(BX, BY, BZ); }
 
@@ -49,8 +52,8 @@ __device__ __forceinline__ f3 backtrace(const float4* __restrict__ vel, f3 c, f3
 }
 
 // ---------------- adv1 (src/sim.js:142-157) ----------------
-__global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv1(const float* __restrict__ P, Fields f, Dims d) {
-  CellId id = cell_id(d);
+__device__ __forceinline__ void adv1_body(const float* __restrict__ P, const Fields& f, Dims d, uint3 blk) {
+  CellId id = cell_id(d, blk);
   if (!id.ok) return;
   const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx);
   const size_t ci = cell(id.i, id.j, id.k, d.nx, d.ny);
@@ -67,8 +70,8 @@ __global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv1(const float* __
 }
 
 // ---------------- adv2 (src/sim.js:159-197) ----------------
-__global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv2(const float* __restrict__ P, Fields f, Dims d) {
-  CellId id = cell_id(d);
+__device__ __forceinline__ void adv2_body(const float* __restrict__ P, const Fields& f, Dims d, uint3 blk) {
+  CellId id = cell_id(d, blk);
   if (!id.ok) return;
   const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx);
   const size_t ci = cell(id.i, id.j, id.k, d.nx, d.ny);
@@ -416,14 +419,13 @@ __device__ __forceinline__ void curl_plane(float4* dst, float4* vbuf, int zlog, 
     dst[t] = make_float4(w.x, w.y, w.z, len3(w));
   }
 }
-__global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_tiled(const float* __restrict__ P, Fields f, const uint2* __restrict__ noiseT,
-                                                              const uint2* __restrict__ curlT, Dims d) {
-  extern __shared__ float4 fsm[];
+__device__ __forceinline__ void forces_tiled_body(const float* __restrict__ P, const Fields& f, const uint2* __restrict__ noiseT,
+                                                  const uint2* __restrict__ curlT, Dims d, uint3 blk, float4* fsm) {
   pdl_wait();
   pdl_trigger();
   float4* vbuf = fsm;                    // 5 * VX * VY
   float4* wbuf = fsm + 5 * VX * VY;      // 3 * WX * WY
-  const int x0 = blockIdx.x * FT_X, y0 = blockIdx.y * FT_Y, z0 = blockIdx.z * FZ;
+  const int x0 = blk.x * FT_X, y0 = blk.y * FT_Y, z0 = blk.z * FZ;
   const int z1 = min(z0 + FZ, d.nz);
   for (int z = z0 - 2; z <= z0 + 2; ++z) load_vplane(vslot(vbuf, z), f.velY, x0, y0, z, d);
   __syncthreads();
@@ -463,9 +465,9 @@ __global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_ti
 constexpr size_t FORCES_TILED_SMEM = sizeof(float4) * (5 * VX * VY + 3 * WX * WY);
 
 // ---------------- divergence minus the expansion target (src/sim.js:399-413) ----------------
-__global__ void __launch_bounds__(256) k_div(const float* __restrict__ P, const float4* __restrict__ velX,
-                                             float* __restrict__ b0, Dims d) {
-  CellId id = cell_id(d);
+__device__ __forceinline__ void div_body(const float* __restrict__ P, const float4* __restrict__ velX, float* __restrict__ b0, Dims d,
+                                         uint3 blk) {
+  CellId id = cell_id(d, blk);
   if (!id.ok) return;
   const int i = id.i, j = id.j, k = id.k;
   const size_t ci = cell(i, j, k, d.nx, d.ny);
@@ -484,10 +486,9 @@ __device__ __forceinline__ float pr(const float* __restrict__ p, int x, int y, i
   if (y < 0) return me;                                                    // floor: Neumann
   return __ldg(p + cell(x, y, z, d.nx, d.ny));
 }
-__global__ void __launch_bounds__(256) k_project(const float* __restrict__ P, const float4* __restrict__ velX,
-                                                 const float* __restrict__ p0, const unsigned char* __restrict__ solid,
-                                                 float4* __restrict__ vel, Dims d) {
-  CellId id = cell_id(d);
+__device__ __forceinline__ void project_body(const float* __restrict__ P, const float4* __restrict__ velX, const float* __restrict__ p0,
+                                             const unsigned char* __restrict__ solid, float4* __restrict__ vel, Dims d, uint3 blk) {
+  CellId id = cell_id(d, blk);
   if (!id.ok) return;
   const int i = id.i, j = id.j, k = id.k;
   const size_t ci = cell(i, j, k, d.nx, d.ny);
@@ -504,6 +505,55 @@ __global__ void __launch_bounds__(256) k_project(const float* __restrict__ P, co
   vel[ci] = make_float4(v.x, v.y, v.z, 0.0f);
 }
 
+// ---------------- per-simulation kernels ----------------
+__global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv1(const float* __restrict__ P, Fields f, Dims d) { adv1_body(P, f, d, blockIdx); }
+__global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv2(const float* __restrict__ P, Fields f, Dims d) { adv2_body(P, f, d, blockIdx); }
+__global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_tiled(const float* __restrict__ P, Fields f,
+                                                                                     const uint2* __restrict__ noiseT,
+                                                                                     const uint2* __restrict__ curlT, Dims d) {
+  extern __shared__ float4 fsm[];
+  forces_tiled_body(P, f, noiseT, curlT, d, blockIdx, fsm);
+}
+__global__ void __launch_bounds__(256) k_div(const float* __restrict__ P, const float4* __restrict__ velX, float* __restrict__ b0, Dims d) {
+  div_body(P, velX, b0, d, blockIdx);
+}
+__global__ void __launch_bounds__(256) k_project(const float* __restrict__ P, const float4* __restrict__ velX, const float* __restrict__ p0,
+                                                 const unsigned char* __restrict__ solid, float4* __restrict__ vel, Dims d) {
+  project_body(P, velX, p0, solid, vel, d, blockIdx);
+}
+
+// ---------------- batched kernels: one grid over many independent simulations ----------------
+// Each CTA finds its simulation and its position in that simulation's grid from the flat block index
+// (BatchMap), then runs the same body as the per-simulation kernel: the arithmetic, and so the results,
+// are those of stepping each simulation alone.
+__global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv1_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I) {
+  uint3 blk; int i;
+  batch_locate(m, blk, i);
+  adv1_body(I.s[i].P, I.s[i].f, I.s[i].d, blk);
+}
+__global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv2_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I) {
+  uint3 blk; int i;
+  batch_locate(m, blk, i);
+  adv2_body(I.s[i].P, I.s[i].f, I.s[i].d, blk);
+}
+__global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I,
+                                                                                 const uint2* __restrict__ noiseT, const uint2* __restrict__ curlT) {
+  extern __shared__ float4 fsm[];
+  uint3 blk; int i;
+  batch_locate(m, blk, i);
+  forces_tiled_body(I.s[i].P, I.s[i].f, noiseT, curlT, I.s[i].d, blk, fsm);
+}
+__global__ void __launch_bounds__(256) k_div_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I) {
+  uint3 blk; int i;
+  batch_locate(m, blk, i);
+  div_body(I.s[i].P, I.s[i].f.velX, I.s[i].b0, I.s[i].d, blk);
+}
+__global__ void __launch_bounds__(256) k_project_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I) {
+  uint3 blk; int i;
+  batch_locate(m, blk, i);
+  project_body(I.s[i].P, I.s[i].f.velX, I.s[i].p0, I.s[i].f.solid, I.s[i].f.vel, I.s[i].d, blk);
+}
+
 // ---------------- launchers ----------------
 void launch_adv1(const float* P, Fields f, Dims d, cudaStream_t st) { launch_pdl(k_adv1, grid_for(d), block_shape(), 0, st, P, f, d); }
 void launch_adv2(const float* P, Fields f, Dims d, cudaStream_t st) { launch_pdl(k_adv2, grid_for(d), block_shape(), 0, st, P, f, d); }
@@ -516,7 +566,27 @@ void launch_forces_recompute(const float* P, Fields f, const uint2* noise, const
   launch_pdl(k_forces<true>, grid_for(d), block_shape(), 0, st, P, f, noise, curl, d);
 }
 cudaError_t step_configure() {
-  return cudaFuncSetAttribute(k_forces_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
+  cudaError_t e = cudaFuncSetAttribute(k_forces_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_forces_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
+}
+// Block grids of the batched stages for a simulation of dims d.
+dim3 step_grid(Dims d) { return grid_for(d); }
+dim3 forces_grid(Dims d) { return dim3((d.nx + FT_X - 1) / FT_X, (d.ny + FT_Y - 1) / FT_Y, (d.nz + FZ - 1) / FZ); }
+void launch_adv1_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st) {
+  launch_pdl(k_adv1_b, dim3(m.prefix[m.n]), block_shape(), 0, st, m, I);
+}
+void launch_adv2_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st) {
+  launch_pdl(k_adv2_b, dim3(m.prefix[m.n]), block_shape(), 0, st, m, I);
+}
+void launch_forces_batch(const BatchMap& m, const StepBatch& I, const uint2* noise, const uint2* curl, cudaStream_t st) {
+  launch_pdl(k_forces_b, dim3(m.prefix[m.n]), dim3(FT_X, FT_Y), FORCES_TILED_SMEM, st, m, I, noise, curl);
+}
+void launch_div_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st) {
+  launch_pdl(k_div_b, dim3(m.prefix[m.n]), block_shape(), 0, st, m, I);
+}
+void launch_project_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st) {
+  launch_pdl(k_project_b, dim3(m.prefix[m.n]), block_shape(), 0, st, m, I);
 }
 void launch_forces_unfused(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
   launch_pdl(k_forces<false>, grid_for(d), block_shape(), 0, st, P, f, noise, curl, d);

@@ -105,6 +105,13 @@ _SIGS = {
     "fire_build_campfire": (_ip, [ctypes.c_uint32, _vp, _ip]),
     "fire_make_spots": (_ip, [ctypes.c_uint32, _ip, _fp, _fp, _fp, _fp, _vp]),
     "fire_poisson_vcycles_noalloc": (_ip, [_vp, _vp, _ip, _ip, _ip, _fp, _ip, _vp]),
+    "fire_ensemble_create": (_ip, [ctypes.POINTER(FireConfig), _ip, ctypes.POINTER(_vp)]),
+    "fire_ensemble_destroy": (_ip, [_vp]),
+    "fire_ensemble_size": (_ip, [_vp]),
+    "fire_ensemble_sim": (_ip, [_vp, _ip, ctypes.POINTER(_vp)]),
+    "fire_ensemble_step": (_ip, [_vp, _fp, _ip, _vp]),
+    "fire_ensemble_sync": (_ip, [_vp]),
+    "fire_ensemble_last_error": (ctypes.c_char_p, [_vp]),
     "fire_poisson_create": (_ip, [_vp, _fp, _ip, _ip, ctypes.POINTER(_vp)]),
     "fire_poisson_destroy": (_ip, [_vp]),
     "fire_poisson_solve": (_ip, [_vp, _vp, _vp, _vp, _dp, _ip, _ip, _vp]),
@@ -208,9 +215,23 @@ class FireSim:
         if rc:
             raise FireError(rc, "fire_sim_create")
         self._h = h
-        self.res = tuple(int(r) for r in res)
-        self.size = tuple(float(s) for s in size)
+        self._owned = True
+        self._describe()
+
+    @classmethod
+    def _borrow(cls, handle: ctypes.c_void_p):
+        """A view of a simulation owned elsewhere (an ensemble member): never destroyed by this object."""
+        self = cls.__new__(cls)
+        self._lib = load_library()
+        self._h = handle
+        self._owned = False
+        self._describe()
+        return self
+
+    def _describe(self):
         info = self.info()
+        self.res = tuple(int(r) for r in info.res)
+        self.size = tuple(float(s) for s in info.size)
         self.dx = info.dx
         self.origin = tuple(info.origin)
         self.coarse_iters = info.coarse_iters
@@ -225,7 +246,8 @@ class FireSim:
     # ---- lifetime ----
     def close(self):
         if self._h is not None:
-            self._lib.fire_sim_destroy(self._h)
+            if getattr(self, "_owned", True):
+                self._lib.fire_sim_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -388,6 +410,60 @@ class FireSim:
     def stats_async(self, out_ptr: int, stream=None):
         """Queues S stats + heat release into a pinned host buffer of 17 doubles (no wait)."""
         self._check(self._lib.fire_sim_stats_async(self._h, ctypes.c_void_p(out_ptr), _stream_handle(stream)), "stats_async")
+
+
+# ---------------------------------------------------------------------------------------------------
+class Ensemble:
+    """Independent simulations of possibly different grids stepped together (one launch per stage over all
+    members).  `members[i]` is a FireSim view for configuring and reading member i; step with `step`."""
+
+    def __init__(self, configs: Sequence[dict], vcycles: int = 4, device: int = 0, noise_seed: int = 1):
+        self._lib = load_library()
+        self._h = None
+        n = len(configs)
+        arr = (FireConfig * n)()
+        for i, c in enumerate(configs):
+            arr[i].res[:] = [int(r) for r in c["res"]]
+            arr[i].size[:] = [float(s) for s in c["size"]]
+            arr[i].vcycles = int(vcycles)
+            arr[i].device = int(device)
+            arr[i].noise_seed = int(noise_seed)
+            arr[i].mg_max_cycles = 0
+            arr[i].mg_tol = 0.0
+        h = ctypes.c_void_p()
+        rc = self._lib.fire_ensemble_create(arr, n, ctypes.byref(h))
+        if rc:
+            raise FireError(rc, "fire_ensemble_create")
+        self._h = h
+        self.members = []
+        for i in range(n):
+            s = ctypes.c_void_p()
+            self._check(self._lib.fire_ensemble_sim(self._h, i, ctypes.byref(s)), "fire_ensemble_sim")
+            self.members.append(FireSim._borrow(s))
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            msg = self._lib.fire_ensemble_last_error(self._h) if self._h else b""
+            raise FireError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def step(self, dt: float, n: int = 1, stream=None):
+        self._check(self._lib.fire_ensemble_step(self._h, float(dt), int(n), _stream_handle(stream)), "fire_ensemble_step")
+
+    def sync(self):
+        self._check(self._lib.fire_ensemble_sync(self._h), "fire_ensemble_sync")
+
+    def close(self):
+        if self._h is not None:
+            for m in self.members:
+                m._h = None
+            self._lib.fire_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------------------------------

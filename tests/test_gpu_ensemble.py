@@ -1,0 +1,75 @@
+"""Ensembles (fire_ensemble_*): members of different grids stepped by batched launches must give the fields
+each member gives when stepped alone.  The batched kernels run the same kernel bodies; the first step is
+bit-identical, later steps agree to FP32 rounding (the compiler may contract a*b+c into FMA differently in
+the batched and per-simulation instantiations), so the bound is relative L2 1e-4 after 6 steps."""
+import numpy as np
+import pytest
+
+import fire_cases as FC
+
+pytestmark = pytest.mark.gpu
+
+# grids chosen to cover every batched path: levels outside the tail (48x96x48: two; 64x128x64: one), the
+# single-CTA tail (48x96x48 from level 2, 24x48x24 from level 0) and the cluster tail (32x64x32 from level
+# 0, 64x128x64 from level 1)
+MEMBERS = [
+    dict(res=(48, 96, 48), size=(0.6, 1.2, 0.6), seed=11, spots=5),
+    dict(res=(32, 64, 32), size=(0.4, 0.8, 0.4), seed=12, spots=2),
+    dict(res=(24, 48, 24), size=(0.3, 0.6, 0.3), seed=13, spots=3),
+    dict(res=(64, 128, 64), size=(0.8, 1.6, 0.8), seed=14, spots=8),
+    dict(res=(32, 64, 32), size=(0.4, 0.8, 0.4), seed=15, spots=4),
+]
+DT = 1.0 / 120.0
+
+
+def _configure(sim, m):
+    import fire_sim as F
+    sim.set_spots(F.make_spots(m["seed"], m["spots"], 1.0, 4.0, 0.0125 * 1.6, 0.3 * m["size"][0]))
+    sim.set_params({"seed": float(m["seed"]), "vortEps": 0.3, "turbAmp": 0.2})
+    sim.set_soot_age(0.02, 0.06)
+    sim.set_bed_gain(0.0)
+
+
+def test_ensemble_equals_members_alone():
+    import fire_sim as F
+    ens = F.Ensemble(MEMBERS, vcycles=4)
+    for sim, m in zip(ens.members, MEMBERS):
+        _configure(sim, m)
+    alone = []
+    for m in MEMBERS:
+        s = F.FireSim(res=m["res"], size=m["size"], vcycles=4)
+        _configure(s, m)
+        alone.append(s)
+    ens.step(DT, 1)
+    ens.sync()
+    for s in alone:
+        s.step(DT, 1)
+        s.sync()
+    for k, (a, b) in enumerate(zip(ens.members, alone)):   # one step from rest: bit-identical
+        for name in ("vel", "S", "S2"):
+            assert np.array_equal(a.download(name), b.download(name)), (k, name)
+    ens.step(DT, 5)
+    ens.sync()
+    for s in alone:
+        s.step(DT, 5)
+        s.sync()
+    for k, (a, b) in enumerate(zip(ens.members, alone)):
+        for name in ("vel", "S", "S2"):
+            x, y = a.download(name), b.download(name)
+            assert np.isfinite(x).all()
+            assert FC.rel_l2(x, y) < 1e-4, (k, name, FC.rel_l2(x, y))
+        assert FC.rel_l2(a.level(0, "p"), b.level(0, "p")) < 1e-4, k
+        assert a.info().frame == b.info().frame == 6
+    # the fire has started in every member
+    assert all(float(m.download("S")[..., 0].max()) > 0.05 for m in ens.members)
+    for s in alone:
+        s.close()
+    ens.close()
+
+
+def test_ensemble_rejects_bad_configs():
+    import fire_sim as F
+    with pytest.raises(F.FireError):
+        F.Ensemble([dict(res=(32, 64, 32), size=(0.4, 0.8, 0.4))] * 65)
+    with pytest.raises(F.FireError):
+        F.Ensemble([])
