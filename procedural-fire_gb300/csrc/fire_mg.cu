@@ -844,11 +844,14 @@ __device__ __forceinline__ void residual_column(const float* __restrict__ p, con
     }
   }
 }
+// gate (residual-driven loop only, else null): the loop's counters; the norm is skipped while the cycle
+// about to complete (gate[0] + 1) is below gate[3], the first cycle at which this step tests convergence.
 __global__ void __launch_bounds__(RB) k_residual(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
-                                                 float ih2, float4* __restrict__ partials) {
+                                                 float ih2, float4* __restrict__ partials, const int* __restrict__ gate) {
   __shared__ df64 sr[RB / 32], sb[RB / 32];
   pdl_wait();
   pdl_trigger();
+  if (gate && gate[0] + 1 < gate[3]) return;   // uniform over the grid
   const int x = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y;
   const int z0 = (blockIdx.z * GZ + threadIdx.z) * RZ;
   const int tid = threadIdx.x + GX * (threadIdx.y + GY * threadIdx.z);
@@ -882,8 +885,23 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
                                                    double tol, int max_cycles, int* __restrict__ counter,
                                                    double* __restrict__ rel_out, cudaGraphConditionalHandle h) {
   __shared__ df64 sa[SUMV / 32], sb[SUMV / 32];
+  __shared__ int skip;
   pdl_wait();
   pdl_trigger();
+  // Cycles before counter[3] (one less than the previous step needed, kept below max_cycles) run without a
+  // convergence test: the previous step's count is a good predictor, and each skipped test saves the
+  // norm's pass over level 0.  The solve still stops only on a tested residual <= tol (or max_cycles).
+  if (threadIdx.x == 0) {
+    const int c = counter[0] + 1;
+    skip = c < counter[3];
+    if (skip) {
+      counter[0] = c;
+      counter[1] += 1;   // cumulative cycles since creation
+      cudaGraphSetConditional(h, 1u);
+    }
+  }
+  __syncthreads();
+  if (skip) return;
   df64 A, B;
   sum_pairs_fixed<RB>(partials, count, threadIdx.x, sa, sb, A, B);
   if (threadIdx.x == 0) {
@@ -892,10 +910,12 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
     sums2[1] = s1;
     const int c = counter[0] + 1;
     counter[0] = c;
-    counter[1] += 1;   // cumulative cycles since creation
+    counter[1] += 1;
     const double rel = s1 > 0.0 ? sqrt(s0 / s1) : 0.0;
     rel_out[0] = rel;
-    cudaGraphSetConditional(h, (rel > tol && c < max_cycles) ? 1u : 0u);
+    const bool more = rel > tol && c < max_cycles;
+    if (!more) counter[3] = min(max(1, c - 1), max_cycles - 1);
+    cudaGraphSetConditional(h, more ? 1u : 0u);
   }
 }
 
@@ -1072,14 +1092,14 @@ int residual_partials_count(const MGLevel& L) {
 void launch_residual(const MGLevel& L, double* partials, double* out2, cudaStream_t st) {
   float4* part4 = reinterpret_cast<float4*>(partials);   // 16 bytes per CTA (the buffer holds 128 per CTA)
   launch_pdl(k_residual, residual_grid(L), kBlock, 0, st, (const float*)L.p, (const float*)L.b, L.nx, L.ny, L.nz,
-             1.0f / (L.h * L.h), part4);
+             1.0f / (L.h * L.h), part4, (const int*)nullptr);
   launch_pdl(k_sum_pairs, dim3(1), dim3(RB), 0, st, (const float4*)part4, residual_partials_count(L), out2);
 }
 void launch_residual_decide(const MGLevel& L, double* partials, double* sums2, double tol, int max_cycles, int* counter,
                             double* rel_out, cudaGraphConditionalHandle h, cudaStream_t st) {
   float4* part4 = reinterpret_cast<float4*>(partials);
   launch_pdl(k_residual, residual_grid(L), kBlock, 0, st, (const float*)L.p, (const float*)L.b, L.nx, L.ny, L.nz,
-             1.0f / (L.h * L.h), part4);
+             1.0f / (L.h * L.h), part4, (const int*)counter);
   launch_pdl(k_sum_decide, dim3(1), dim3(RB), 0, st, (const float4*)part4, residual_partials_count(L), sums2, tol, max_cycles,
              counter, rel_out, h);
 }
