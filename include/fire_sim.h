@@ -271,6 +271,27 @@ int fire_ensemble_step(FireEnsemble* e, float dt, int n_steps, void* stream);
 int fire_ensemble_sync(FireEnsemble* e);
 const char* fire_ensemble_last_error(FireEnsemble* e);
 
+/* ---- sparks (src/sparks.js) ---------------------------------------------------------------------
+ * Burning sparks carried by a simulation's velocity field: the particle update of Sparks.step
+ * (src/sparks.js:55-142, 250-274).  A spark is 16 floats: position+age, velocity+burn time left,
+ * previous position+temperature (K), diameter (mm)+seed+alive+flicker (Hz).  fire_sparks_step reads the
+ * simulation's velocity: queue it after fire_sim_step on the same stream.  The drawing of the streaks
+ * (src/sparks.js:146-221) is a rasterisation pass and is not part of this library.                   */
+typedef struct FireSparks FireSparks;
+int fire_sparks_create(FireSim* sim, int count, FireSparks** out);        /* Sparks constructor (count)  */
+int fire_sparks_destroy(FireSparks* s);
+int fire_sparks_reset(FireSparks* s);                                      /* src/sparks.js:38-41       */
+/* burst({n, pos, speed, radius, dur, fan, size, aim}) (src/sparks.js:44-46); aim3 may be NULL.      */
+int fire_sparks_burst(FireSparks* s, int n, const float pos[3], float speed, float radius, float dur, float fan, float size,
+                      const float* aim3);
+/* rate (sparks/s, the page sets 1 x intensity) and params.turb / lifeK / sizeK / upK.               */
+int fire_sparks_set(FireSparks* s, float rate, float turb, float lifeK, float sizeK, float upK);
+int fire_sparks_step(FireSparks* s, float dt, void* stream);               /* src/sparks.js:250-274     */
+/* The 27 uniforms (SPARK_FIELDS order) the next step would use, without advancing anything.         */
+int fire_sparks_peek(FireSparks* s, float dt, float* out27);
+int fire_sparks_buffer(FireSparks* s, void** dev_ptr, int* count);          /* zero-copy device view     */
+int fire_sparks_io(FireSparks* s, float* host, size_t bytes, int to_device);   /* count * 16 floats, sync */
+
 /* ---- standalone pressure Poisson solver --------------------------------------------------------
  * The step's pressure equation (src/sim.js:415-495, 576-599: cell-centred 7-point Laplacian, p = 0 on the
  * side and top faces, zero gradient at the floor, levels halved while every dimension is even and the

@@ -1126,6 +1126,86 @@ double orc_poisson_study(int N, int face, int mode, double omega, int pre, int p
 }
 void orc_poisson_rhs(int N, float* out) { std::vector<float> b = krhs(N); std::memcpy(out, b.data(), b.size() * 4); }
 
+// ---- one spark update (src/sparks.js:55-142) over `count` sparks of 16 floats, FP32.  U: the 27 uniforms in
+// SPARK_FIELDS order.  Spawn slots go to dead sparks in index order (one of the orders the reference's
+// atomic counter can produce).  vel: the simulation's velocity field (float4 per cell); curl: the 128^3
+// curl table as float4. ----
+void orc_sparks_step(float* sp, int count, const float* U, const float* vel, int nx, int ny, int nz, const float* curl, int N) {
+  enum { dt_, time_, frame_, count_, nBase_, nBurst_, bX_, bY_, bZ_, bSpeed_, bRad_, ox_, oy_, oz_, sx_, sy_, sz_, turb_, lifeK_,
+         bedR_, seed_, sizeK_, upK_, bFan_, bSize_, aimX_, aimZ_ };
+  const std::vector<float> vf(vel, vel + 4 * (size_t)nx * ny * nz);
+  const uint32_t seed = (uint32_t)U[seed_], frame = (uint32_t)U[frame_];
+  auto r = [&](uint32_t slot, uint32_t k) { return rand2(slot * 7919u + k * 104729u + seed, frame); };
+  auto gauss = [&](uint32_t slot, uint32_t k) {
+    const float u1 = std::fmax(r(slot, k), 1e-6f), u2 = r(slot, k + 1u);
+    return std::sqrt(-2.0f * std::log(u1)) * std::cos(6.2831853f * u2);
+  };
+  auto normalize = [](V3<float> v) { return v / std::sqrt(dot3(v, v)); };
+  auto fluidVel = [&](V3<float> p) {   // sparks.js:70-78
+    const V3<float> g((p.x - U[ox_]) / U[sx_], (p.y - U[oy_]) / U[sy_], (p.z - U[oz_]) / U[sz_]);
+    if (g.x < 0.0f || g.y < 0.0f || g.z < 0.0f || g.x > 1.0f || g.y > 1.0f || g.z > 1.0f) {
+      if (g.y > 1.0f && std::sqrt(p.x * p.x + p.z * p.z) < 0.5f) return V3<float>(0.0f, 1.6f / (1.0f + (g.y - 1.0f) * 1.5f), 0.0f);
+      return V3<float>();
+    }
+    return sample_clamp(vf, nx, ny, nz, V3<float>(g.x * (float)nx, g.y * (float)ny, g.z * (float)nz)).xyz();
+  };
+  const uint32_t want = (uint32_t)(U[nBase_] + U[nBurst_]);
+  uint32_t deadSeen = 0;
+  for (int i = 0; i < count; ++i) {
+    float* s = sp + 16 * (size_t)i;
+    if (s[14] < 0.5f) {   // dead: spawn (sparks.js:82-111)
+      const uint32_t slot = deadSeen++;
+      if (want == 0u || slot >= want) continue;
+      const bool burst = slot >= (uint32_t)U[nBase_];
+      V3<float> p, v;
+      if (burst) {
+        p = V3<float>(U[bX_], U[bY_], U[bZ_]) + (V3<float>(r(slot, 7u), r(slot, 8u), r(slot, 9u)) - V3<float>(0.5f, 0.5f, 0.5f)) * U[bRad_] * 2.0f;
+        V3<float> radial(p.x, 0.0f, p.z);
+        radial = len3(radial) > 1e-3f ? normalize(radial) : V3<float>();
+        const V3<float> aim(U[aimX_], 0.0f, U[aimZ_]);
+        const V3<float> dir = normalize(V3<float>(gauss(slot, 1u), std::fabs(gauss(slot, 3u)) * 1.2f + 0.7f, gauss(slot, 5u)) + (radial + aim) * U[bFan_]);
+        v = dir * U[bSpeed_] * (0.5f + 0.8f * r(slot, 10u));
+      } else {
+        const float a = r(slot, 1u) * 6.2831853f, rr = std::sqrt(r(slot, 2u)) * U[bedR_];
+        p = V3<float>(std::cos(a) * rr, 0.05f + r(slot, 3u) * 0.12f, std::sin(a) * rr);
+        v = V3<float>(gauss(slot, 4u) * 0.4f, 0.6f + r(slot, 6u) * 1.8f, gauss(slot, 11u) * 0.4f);
+      }
+      const float dmm = clampf(0.5f * std::exp(0.55f * gauss(slot, 13u)) * U[sizeK_] * (burst ? U[bSize_] : 1.0f), 0.15f, 2.5f);
+      const float tb = (0.25f + 2.0f * dmm * dmm) * (0.6f + 0.8f * r(slot, 15u)) * U[lifeK_];
+      const float T0 = 1230.0f + 70.0f * gauss(slot, 16u) + (burst ? 80.0f : 0.0f);
+      const float fl = r(slot, 20u) < 0.45f ? 5.0f + 15.0f * r(slot, 18u) : 0.0f;
+      const float o[16] = {p.x, p.y, p.z, 0.0f, v.x, v.y, v.z, tb, p.x, p.y, p.z, T0, dmm, r(slot, 19u), 1.0f, fl};
+      std::memcpy(s, o, sizeof o);
+      continue;
+    }
+    // alive: integrate (sparks.js:113-141)
+    const float dt = U[dt_], dmm = s[12];
+    V3<float> p(s[0], s[1], s[2]), v(s[4], s[5], s[6]);
+    const float tau = std::fmax(0.4f * dmm * dmm, 0.01f);
+    V3<float> u = fluidVel(p) * U[upK_];
+    const V3<float> tq = p * 0.9f + V3<float>(0.0f, -U[time_] * 0.5f, U[time_] * 0.13f + s[13] * 3.0f);
+    const float turbAmp = U[turb_] * (0.3f + 3.0f * smoothstep(0.4f, 1.2f, p.y)) / 12.0f;
+    u = u + sample_repeat(curl, N, tq).xyz() * turbAmp;
+    const float k = 1.0f - std::exp(-dt / tau);
+    v = V3<float>(mixf(v.x, u.x, k), mixf(v.y, u.y, k), mixf(v.z, u.z, k));
+    v.y -= 9.81f * (1.0f - 0.004f) * dt * (dmm < 0.3f ? 0.2f : 1.0f);
+    const float qx = p.x, qy = p.y, qz = p.z;
+    p = p + v * dt;
+    float T = s[11];
+    const float tb = s[7] - dt;
+    if (tb > 0.0f) {
+      const float rel = len3(u - v);
+      T = mixf(T, 1180.0f + 60.0f * std::fmin(rel, 3.0f) + 60.0f * (s[13] - 0.5f), 1.0f - std::exp(-dt / 0.3f));
+    } else {
+      T = 293.0f + (T - 293.0f) * std::exp(-dt / (0.06f + 0.08f * dmm));
+    }
+    const float age = s[3] + dt;
+    const float alive = (T < 760.0f || p.y < 0.0f || p.y > 4.5f || std::sqrt(p.x * p.x + p.z * p.z) > 3.0f || age > 12.0f) ? 0.0f : 1.0f;
+    const float o[16] = {p.x, p.y, p.z, age, v.x, v.y, v.z, tb, qx, qy, qz, T, s[12], s[13], alive, s[15]};
+    std::memcpy(s, o, sizeof o);
+  }
+}
+
 // ---- FP64 reference solution of the step's pressure equation (the operator of k_smooth / k_restrict:
 // sum of the six ghost-ruled neighbours minus 6 p, over h^2; p = 0 on sides and top, zero gradient at the
 // floor, src/sim.js:417-466).  -A is symmetric positive definite, so conjugate gradients apply. ----

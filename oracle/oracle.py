@@ -62,6 +62,7 @@ def lib():
             "orc_pressure_apply": (None, [ip, ip, ip, dp, vp, vp]),
             "orc_pressure_rel_residual": (dp, [ip, ip, ip, dp, vp, vp]),
             "orc_pressure_cg": (ip, [ip, ip, ip, dp, vp, vp, dp, ip, vp]),
+            "orc_sparks_step": (None, [vp, ip, vp, vp, ip, ip, ip, vp, ip]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -105,6 +106,17 @@ def poisson_study(N: int, face: bool, mode: int, omega: float = 1.0, pre: int = 
     r0 = lib().orc_poisson_study(N, int(face), mode, omega, pre, post, coarse, cycles, _ptr(hist))
     n = 6 if mode in (0, 1) else cycles
     return r0, hist[:n]
+
+
+def sparks_step(sparks: np.ndarray, uniforms: np.ndarray, vel: np.ndarray, curl: np.ndarray) -> np.ndarray:
+    """One spark update (src/sparks.js:55-142) of a (count, 16) array; vel is (nz, ny, nx, 4), curl (N, N, N, 4)."""
+    s = np.ascontiguousarray(sparks, np.float32).copy()
+    U = np.ascontiguousarray(uniforms, np.float32)
+    v = np.ascontiguousarray(vel, np.float32)
+    c = np.ascontiguousarray(curl, np.float32)
+    nz, ny, nx = v.shape[:3]
+    lib().orc_sparks_step(_ptr(s), s.shape[0], _ptr(U), _ptr(v), nx, ny, nz, _ptr(c), c.shape[0])
+    return s
 
 
 def pressure_apply(x: np.ndarray, h: float) -> np.ndarray:

@@ -1162,3 +1162,154 @@ int fire_ensemble_sync(FireEnsemble* e) {
 const char* fire_ensemble_last_error(FireEnsemble* e) { return e ? e->err.c_str() : "null ensemble"; }
 
 }  // extern "C"
+
+// ==================================================================================================
+// Sparks (src/sparks.js): particles carried by a simulation's velocity field.  The host keeps the spawn
+// bookkeeping of Sparks.step (src/sparks.js:250-274) in doubles as the page does; the device runs the
+// particle update (fire_sparks.cu).
+struct SparkBurstRec {
+  double t0;
+  int n, emitted;
+  float pos[3], speed, radius, dur, fan, size, aim[3];
+  bool hasAim;
+};
+struct FireSparks {
+  FireSim* sim = nullptr;
+  int count = 0;
+  float4* dSp = nullptr;
+  int* dDead = nullptr;
+  double rate = 3.0, carry = 0.0, time = 0.0;   // src/sparks.js:24-28
+  long long frame = 0;
+  float turb = 1.0f, lifeK = 1.0f, sizeK = 1.0f, upK = 1.0f;
+  std::vector<SparkBurstRec> bursts;
+};
+
+namespace {
+// The uniforms of the next step (src/sparks.js:250-270); with commit, the bookkeeping advances too.
+SparkU spark_uniforms(FireSparks* s, float dt, bool commit) {
+  double carry = s->carry + s->rate * (double)dt;
+  const double nBase = std::floor(carry);
+  carry -= nBase;
+  std::vector<SparkBurstRec> bursts = s->bursts;
+  int nBurst = 0;
+  const SparkBurstRec* B = nullptr;
+  for (SparkBurstRec& b : bursts) {
+    const double frac = std::min((s->time + (double)dt - b.t0) / (double)b.dur, 1.0);
+    const int due = std::min(b.n, (int)std::floor((double)b.n * frac + 0.5));   // Math.round
+    const int k = due - b.emitted;
+    if (k > 0 && !B) { B = &b; nBurst = k; b.emitted += k; }
+  }
+  SparkU U;
+  U.dt = dt; U.time = (float)s->time; U.frame = (float)s->frame; U.count = (float)s->count;
+  U.nBase = (float)nBase; U.nBurst = (float)nBurst;
+  U.burstX = B ? B->pos[0] : 0.0f; U.burstY = B ? B->pos[1] : 0.0f; U.burstZ = B ? B->pos[2] : 0.0f;
+  U.burstSpeed = B ? B->speed : 0.0f; U.burstRadius = B ? B->radius : 0.0f;
+  U.ox = s->sim->origin[0]; U.oy = s->sim->origin[1]; U.oz = s->sim->origin[2];
+  U.sx = s->sim->size[0]; U.sy = s->sim->size[1]; U.sz = s->sim->size[2];
+  U.turb = s->turb; U.lifeK = s->lifeK; U.bedRadius = 0.2f; U.seed = 1234.0f; U.sizeK = s->sizeK; U.upK = s->upK;
+  U.burstFan = B ? B->fan : 0.0f; U.burstSize = B ? B->size : 1.0f;
+  U.aimX = (B && B->hasAim) ? B->aim[0] : 0.0f; U.aimZ = (B && B->hasAim) ? B->aim[2] : 0.0f;
+  if (commit) {
+    s->carry = carry;
+    bursts.erase(std::remove_if(bursts.begin(), bursts.end(), [](const SparkBurstRec& b) { return b.emitted >= b.n; }), bursts.end());
+    s->bursts = bursts;
+  }
+  return U;
+}
+}  // namespace
+
+extern "C" {
+
+int fire_sparks_create(FireSim* sim, int count, FireSparks** out) {
+  if (!sim || !out || count < 1 || count > (1 << 24)) return FIRE_ERR_BAD_ARG;
+  *out = nullptr;
+  CK(cudaSetDevice(sim->device));
+  FireSparks* s = new FireSparks();
+  s->sim = sim;
+  s->count = count;
+  if (cudaMalloc((void**)&s->dSp, sizeof(float4) * 4 * (size_t)count) != cudaSuccess ||
+      cudaMalloc((void**)&s->dDead, sizeof(int) * (size_t)spark_blocks(count)) != cudaSuccess ||
+      cudaMemset(s->dSp, 0, sizeof(float4) * 4 * (size_t)count) != cudaSuccess) {
+    if (s->dSp) cudaFree(s->dSp);
+    if (s->dDead) cudaFree(s->dDead);
+    delete s;
+    return FIRE_ERR_OOM;
+  }
+  *out = s;
+  return FIRE_OK;
+}
+
+int fire_sparks_destroy(FireSparks* s) {
+  if (!s) return FIRE_ERR_BAD_ARG;
+  cudaSetDevice(s->sim->device);
+  cudaDeviceSynchronize();
+  cudaFree(s->dSp);
+  cudaFree(s->dDead);
+  delete s;
+  return FIRE_OK;
+}
+
+int fire_sparks_reset(FireSparks* s) {   // src/sparks.js:38-41
+  if (!s) return FIRE_ERR_BAD_ARG;
+  if (cudaSetDevice(s->sim->device) != cudaSuccess || cudaMemset(s->dSp, 0, sizeof(float4) * 4 * (size_t)s->count) != cudaSuccess)
+    return FIRE_ERR_CUDA;
+  s->carry = 0.0;
+  s->bursts.clear();
+  s->time = 0.0;
+  s->frame = 0;
+  return FIRE_OK;
+}
+
+int fire_sparks_burst(FireSparks* s, int n, const float pos[3], float speed, float radius, float dur, float fan, float size,
+                      const float* aim3) {   // src/sparks.js:44-46
+  if (!s || !pos || n < 0 || !(dur > 0.0f)) return FIRE_ERR_BAD_ARG;
+  SparkBurstRec b;
+  b.t0 = s->time;
+  b.n = n;
+  b.emitted = 0;
+  for (int i = 0; i < 3; ++i) { b.pos[i] = pos[i]; b.aim[i] = aim3 ? aim3[i] : 0.0f; }
+  b.speed = speed; b.radius = radius; b.dur = dur; b.fan = fan; b.size = size;
+  b.hasAim = aim3 != nullptr;
+  s->bursts.push_back(b);
+  return FIRE_OK;
+}
+
+int fire_sparks_set(FireSparks* s, float rate, float turb, float lifeK, float sizeK, float upK) {
+  if (!s || !(rate >= 0.0f)) return FIRE_ERR_BAD_ARG;
+  s->rate = rate; s->turb = turb; s->lifeK = lifeK; s->sizeK = sizeK; s->upK = upK;
+  return FIRE_OK;
+}
+
+int fire_sparks_peek(FireSparks* s, float dt, float* out27) {
+  if (!s || !out27) return FIRE_ERR_BAD_ARG;
+  const SparkU U = spark_uniforms(s, dt, false);
+  std::memcpy(out27, &U, sizeof U);
+  return FIRE_OK;
+}
+
+// One spark step after the simulation's step on the same stream (it reads the simulation's velocity).
+int fire_sparks_step(FireSparks* s, float dt, void* stream) {
+  if (!s || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
+  if (cudaSetDevice(s->sim->device) != cudaSuccess) return FIRE_ERR_CUDA;
+  const SparkU U = spark_uniforms(s, dt, true);
+  launch_sparks(s->dSp, U, s->dDead, s->sim->f.vel, s->sim->d, s->sim->curl, as_stream(stream));
+  s->time += dt;
+  s->frame += 1;
+  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+}
+
+int fire_sparks_buffer(FireSparks* s, void** dev_ptr, int* count) {
+  if (!s || !dev_ptr || !count) return FIRE_ERR_BAD_ARG;
+  *dev_ptr = s->dSp;
+  *count = s->count;
+  return FIRE_OK;
+}
+
+int fire_sparks_io(FireSparks* s, float* host, size_t bytes, int to_device) {
+  if (!s || !host || bytes != sizeof(float4) * 4 * (size_t)s->count) return FIRE_ERR_BAD_ARG;
+  if (cudaSetDevice(s->sim->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return FIRE_ERR_CUDA;
+  const cudaError_t e = to_device ? cudaMemcpy(s->dSp, host, bytes, cudaMemcpyHostToDevice) : cudaMemcpy(host, s->dSp, bytes, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+}
+
+}  // extern "C"

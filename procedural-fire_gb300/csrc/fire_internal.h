@@ -80,6 +80,17 @@ struct StepBatch { StepInst s[BATCH_MAX]; };
 // One multigrid level of each simulation of a batch, by simulation index (kernel parameter).
 struct LevelBatch { MGLevel l[BATCH_MAX]; };
 
+// Uniforms of one spark update (SPARK_FIELDS order, src/sparks.js:9-13), all f32 as the reference uploads them.
+struct SparkU {
+  float dt, time, frame, count, nBase, nBurst, burstX, burstY, burstZ, burstSpeed, burstRadius;
+  float ox, oy, oz, sx, sy, sz, turb, lifeK, bedRadius, seed, sizeK, upK, burstFan, burstSize, aimX, aimZ;
+};
+static_assert(sizeof(SparkU) == 27 * sizeof(float), "27 spark uniforms");
+// ---- kernel launchers (fire_sparks.cu) ----
+int spark_blocks(int count);
+// One spark step (dead-count pass + update); `dead` holds spark_blocks(count) ints.
+void launch_sparks(float4* sp, const SparkU& S, int* dead, const float4* vel, Dims d, const uint2* curl, cudaStream_t st);
+
 // ---- kernel launchers (fire_tables.cu) ----
 void launch_noise_table(uint2* noise, int N, int seed, cudaStream_t st);
 void launch_curl_table(const uint2* noise, uint2* curl, int N, cudaStream_t st);

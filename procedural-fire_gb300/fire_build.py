@@ -26,6 +26,7 @@ SOURCES = {
     "fire_api.cu": [],
     "fire_noalloc.cu": [],
     "fire_poisson.cu": [],
+    "fire_sparks.cu": [],
     "fire_scene.cpp": [],
 }
 

@@ -105,6 +105,15 @@ _SIGS = {
     "fire_build_campfire": (_ip, [ctypes.c_uint32, _vp, _ip]),
     "fire_make_spots": (_ip, [ctypes.c_uint32, _ip, _fp, _fp, _fp, _fp, _vp]),
     "fire_poisson_vcycles_noalloc": (_ip, [_vp, _vp, _ip, _ip, _ip, _fp, _ip, _vp]),
+    "fire_sparks_create": (_ip, [_vp, _ip, ctypes.POINTER(_vp)]),
+    "fire_sparks_destroy": (_ip, [_vp]),
+    "fire_sparks_reset": (_ip, [_vp]),
+    "fire_sparks_burst": (_ip, [_vp, _ip, _vp, _fp, _fp, _fp, _fp, _fp, _vp]),
+    "fire_sparks_set": (_ip, [_vp, _fp, _fp, _fp, _fp, _fp]),
+    "fire_sparks_step": (_ip, [_vp, _fp, _vp]),
+    "fire_sparks_peek": (_ip, [_vp, _fp, _vp]),
+    "fire_sparks_buffer": (_ip, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_ip)]),
+    "fire_sparks_io": (_ip, [_vp, _vp, _sz, _ip]),
     "fire_ensemble_create": (_ip, [ctypes.POINTER(FireConfig), _ip, ctypes.POINTER(_vp)]),
     "fire_ensemble_destroy": (_ip, [_vp]),
     "fire_ensemble_size": (_ip, [_vp]),
@@ -410,6 +419,71 @@ class FireSim:
     def stats_async(self, out_ptr: int, stream=None):
         """Queues S stats + heat release into a pinned host buffer of 17 doubles (no wait)."""
         self._check(self._lib.fire_sim_stats_async(self._h, ctypes.c_void_p(out_ptr), _stream_handle(stream)), "stats_async")
+
+
+# ---------------------------------------------------------------------------------------------------
+SPARK_FIELDS = ("dt", "time", "frame", "count", "nBase", "nBurst", "burstX", "burstY", "burstZ", "burstSpeed", "burstRadius",
+                "ox", "oy", "oz", "sx", "sy", "sz", "turb", "lifeK", "bedRadius", "seed", "sizeK", "upK",
+                "burstFan", "burstSize", "aimX", "aimZ")   # src/sparks.js:9-13
+
+
+class Sparks:
+    """Sparks carried by `sim`'s velocity field (src/sparks.js: Sparks)."""
+
+    def __init__(self, sim: "FireSim", count: int = 8192):
+        self._lib = load_library()
+        self.sim = sim
+        self.count = int(count)
+        h = ctypes.c_void_p()
+        rc = self._lib.fire_sparks_create(sim._h, self.count, ctypes.byref(h))
+        if rc:
+            raise FireError(rc, "fire_sparks_create")
+        self._h = h
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            raise FireError(rc, what)
+
+    def close(self):
+        if self._h is not None:
+            self._lib.fire_sparks_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self):
+        self._check(self._lib.fire_sparks_reset(self._h), "fire_sparks_reset")
+
+    def burst(self, n: int = 60, pos=(0.0, 0.1, 0.0), speed: float = 3.0, radius: float = 0.05, dur: float = 0.12,
+              fan: float = 0.6, size: float = 1.3, aim=None):
+        p = np.ascontiguousarray(pos, np.float32)
+        a = np.ascontiguousarray(aim, np.float32) if aim is not None else None
+        self._check(self._lib.fire_sparks_burst(self._h, int(n), _ptr(p), speed, radius, dur, fan, size,
+                                                _ptr(a) if a is not None else None), "fire_sparks_burst")
+
+    def set(self, rate: float = 3.0, turb: float = 1.0, lifeK: float = 1.0, sizeK: float = 1.0, upK: float = 1.0):
+        self._check(self._lib.fire_sparks_set(self._h, rate, turb, lifeK, sizeK, upK), "fire_sparks_set")
+
+    def step(self, dt: float, stream=None):
+        self._check(self._lib.fire_sparks_step(self._h, float(dt), _stream_handle(stream)), "fire_sparks_step")
+
+    def peek(self, dt: float) -> np.ndarray:
+        out = np.zeros(27, np.float32)
+        self._check(self._lib.fire_sparks_peek(self._h, float(dt), _ptr(out)), "fire_sparks_peek")
+        return out
+
+    def download(self) -> np.ndarray:
+        out = np.zeros((self.count, 16), np.float32)
+        self._check(self._lib.fire_sparks_io(self._h, _ptr(out), out.nbytes, 0), "fire_sparks_io")
+        return out
+
+    def upload(self, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, np.float32)
+        self._check(self._lib.fire_sparks_io(self._h, _ptr(a), a.nbytes, 1), "fire_sparks_io")
 
 
 # ---------------------------------------------------------------------------------------------------
