@@ -291,6 +291,43 @@ int fire_sparks_step(FireSparks* s, float dt, void* stream);               /* sr
 int fire_sparks_peek(FireSparks* s, float dt, float* out27);
 int fire_sparks_buffer(FireSparks* s, void** dev_ptr, int* count);          /* zero-copy device view     */
 int fire_sparks_io(FireSparks* s, float* host, size_t bytes, int to_device);   /* count * 16 floats, sync */
+int fire_sparks_set_rate(FireSparks* s, float rate);                        /* sparks.rate alone         */
+
+/* ---- the cinematic's timeline (src/timeline.js) and its capture-mode driver (src/main.js:128-160) ----
+ * Host-only and deterministic.  Events: the scripted cue sheet plus the seeded background pops, sorted by
+ * time.  fire_timeline_step(j) is capStep(j): the simulation's parameters (simAt) and log offsets
+ * (logOffsetsAt, applied to the base logs and re-uploaded when they change) at t = j / (30 n), the spark
+ * bursts of the events in [t, t + 1/(30 n)), then one fire_sim_step and one fire_sparks_step (sparks may
+ * be NULL) of 1 / (30 n) seconds.  No GPU work of its own.                                              */
+enum { FIRE_EVENT_POP = 0, FIRE_EVENT_CRACKLE_BURST = 1, FIRE_EVENT_LOG_SHIFT = 2, FIRE_EVENT_GUST = 3, FIRE_EVENT_IGNITE = 4 };
+typedef struct {
+  double t;                 /* seconds                                                                */
+  int type;                 /* FIRE_EVENT_*                                                           */
+  double strength;
+  double pos[3];
+  int has_aim;
+  double aim[3];
+  int log;                  /* log-shift: the log that moves                                          */
+  double dur;               /* gust: duration (s)                                                     */
+} FireTimelineEvent;
+int fire_timeline_event_count(void);
+int fire_timeline_events(FireTimelineEvent* out, int max);                 /* returns the number written */
+double fire_timeline_intensity_at(double t);                               /* src/timeline.js:118-129   */
+/* simAt (src/timeline.js:147-170): intensity, burstAmt, burstX, burstY, burstZ, windX, windZ.          */
+int fire_timeline_sim_at(double t, double* out7);
+/* logOffsetsAt (src/timeline.js:136-144): returns 1 and the offsets after the log shift, else 0.       */
+int fire_timeline_log_offsets_at(double t, int* index, double* s, double* foot_out, double* top_drop, double* top_out);
+int fire_timeline_camera_at(double t, double* pos3, double* target3, double* fov_deg);   /* cameraAt    */
+int fire_timeline_lens_at(double t, double* focus, double* aperture, double* fmm, double* fnum);   /* lensAt */
+double fire_timeline_exposure_at(double t);                                /* exposureAt                */
+double fire_timeline_preroll(void);                                        /* PREROLL (s)               */
+typedef struct FireTimeline FireTimeline;
+/* base_logs: the campfire's packed logs (8 floats each); steps_per_frame: n (dt = 1 / (30 n)).          */
+int fire_timeline_create(const float* base_logs, int n_logs, int steps_per_frame, FireTimeline** out);
+int fire_timeline_destroy(FireTimeline* tl);
+double fire_timeline_step_dt(FireTimeline* tl);
+double fire_timeline_step_time(FireTimeline* tl, long long j);
+int fire_timeline_step(FireTimeline* tl, FireSim* sim, FireSparks* sparks, long long j, void* stream);
 
 /* ---- standalone pressure Poisson solver --------------------------------------------------------
  * The step's pressure equation (src/sim.js:415-495, 576-599: cell-centred 7-point Laplacian, p = 0 on the

@@ -1280,6 +1280,12 @@ int fire_sparks_set(FireSparks* s, float rate, float turb, float lifeK, float si
   return FIRE_OK;
 }
 
+int fire_sparks_set_rate(FireSparks* s, float rate) {   // simStep: sparks.rate = 1.0 * intensity
+  if (!s || !(rate >= 0.0f)) return FIRE_ERR_BAD_ARG;
+  s->rate = rate;
+  return FIRE_OK;
+}
+
 int fire_sparks_peek(FireSparks* s, float dt, float* out27) {
   if (!s || !out27) return FIRE_ERR_BAD_ARG;
   const SparkU U = spark_uniforms(s, dt, false);

@@ -28,6 +28,7 @@ SOURCES = {
     "fire_poisson.cu": [],
     "fire_sparks.cu": [],
     "fire_scene.cpp": [],
+    "fire_timeline.cpp": [],
 }
 
 

@@ -114,6 +114,22 @@ _SIGS = {
     "fire_sparks_peek": (_ip, [_vp, _fp, _vp]),
     "fire_sparks_buffer": (_ip, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_ip)]),
     "fire_sparks_io": (_ip, [_vp, _vp, _sz, _ip]),
+    "fire_sparks_set_rate": (_ip, [_vp, _fp]),
+    "fire_timeline_event_count": (_ip, []),
+    "fire_timeline_events": (_ip, [_vp, _ip]),
+    "fire_timeline_intensity_at": (_dp, [_dp]),
+    "fire_timeline_sim_at": (_ip, [_dp, _vp]),
+    "fire_timeline_log_offsets_at": (_ip, [_dp, ctypes.POINTER(_ip), ctypes.POINTER(_dp), ctypes.POINTER(_dp),
+                                            ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "fire_timeline_camera_at": (_ip, [_dp, _vp, _vp, ctypes.POINTER(_dp)]),
+    "fire_timeline_lens_at": (_ip, [_dp, ctypes.POINTER(_dp), ctypes.POINTER(_dp), ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "fire_timeline_exposure_at": (_dp, [_dp]),
+    "fire_timeline_preroll": (_dp, []),
+    "fire_timeline_create": (_ip, [_vp, _ip, _ip, ctypes.POINTER(_vp)]),
+    "fire_timeline_destroy": (_ip, [_vp]),
+    "fire_timeline_step_dt": (_dp, [_vp]),
+    "fire_timeline_step_time": (_dp, [_vp, ctypes.c_longlong]),
+    "fire_timeline_step": (_ip, [_vp, _vp, _vp, ctypes.c_longlong, _vp]),
     "fire_ensemble_create": (_ip, [ctypes.POINTER(FireConfig), _ip, ctypes.POINTER(_vp)]),
     "fire_ensemble_destroy": (_ip, [_vp]),
     "fire_ensemble_size": (_ip, [_vp]),
@@ -484,6 +500,89 @@ class Sparks:
     def upload(self, arr: np.ndarray):
         a = np.ascontiguousarray(arr, np.float32)
         self._check(self._lib.fire_sparks_io(self._h, _ptr(a), a.nbytes, 1), "fire_sparks_io")
+
+
+# ---------------------------------------------------------------------------------------------------
+# The cinematic's timeline (src/timeline.js) and its capture-mode driver (src/main.js:128-160).
+EVENT_TYPES = {0: "pop", 1: "crackle-burst", 2: "log-shift", 3: "gust", 4: "ignite"}
+
+
+class FireTimelineEvent(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_double), ("type", ctypes.c_int), ("strength", ctypes.c_double), ("pos", ctypes.c_double * 3),
+                ("has_aim", ctypes.c_int), ("aim", ctypes.c_double * 3), ("log", ctypes.c_int), ("dur", ctypes.c_double)]
+
+
+def timeline_events():
+    L = load_library()
+    n = L.fire_timeline_event_count()
+    arr = (FireTimelineEvent * n)()
+    L.fire_timeline_events(arr, n)
+    return [{"t": e.t, "type": EVENT_TYPES[e.type], "strength": e.strength, "pos": tuple(e.pos),
+             "aim": tuple(e.aim) if e.has_aim else None, "log": e.log, "dur": e.dur} for e in arr]
+
+
+def timeline_sim_at(t: float) -> Dict[str, float]:
+    out = np.zeros(7, np.float64)
+    load_library().fire_timeline_sim_at(float(t), _ptr(out))
+    return dict(zip(("intensity", "burstAmt", "burstX", "burstY", "burstZ", "windX", "windZ"), map(float, out)))
+
+
+def timeline_intensity_at(t: float) -> float:
+    return float(load_library().fire_timeline_intensity_at(float(t)))
+
+
+def timeline_log_offsets_at(t: float):
+    i, s, a, b, c = ctypes.c_int(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    if not load_library().fire_timeline_log_offsets_at(float(t), ctypes.byref(i), ctypes.byref(s), ctypes.byref(a),
+                                                       ctypes.byref(b), ctypes.byref(c)):
+        return None
+    return {"index": i.value, "s": s.value, "footOut": a.value, "topDrop": b.value, "topOut": c.value}
+
+
+def timeline_camera_at(t: float):
+    pos, tgt, fov = np.zeros(3), np.zeros(3), ctypes.c_double()
+    load_library().fire_timeline_camera_at(float(t), _ptr(pos), _ptr(tgt), ctypes.byref(fov))
+    return {"pos": tuple(pos), "target": tuple(tgt), "fov": fov.value}
+
+
+def timeline_lens_at(t: float):
+    f, a, m, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    load_library().fire_timeline_lens_at(float(t), ctypes.byref(f), ctypes.byref(a), ctypes.byref(m), ctypes.byref(n))
+    return {"focus": f.value, "aperture": a.value, "fmm": m.value, "N": n.value}
+
+
+class Timeline:
+    """capStep driver: `step(j)` sets sim params and log offsets for t = j / (30 n), throws the event bursts
+    and steps the simulation (and the sparks, if given) by 1 / (30 n)."""
+
+    def __init__(self, base_logs: np.ndarray, steps_per_frame: int = 8):
+        self._lib = load_library()
+        lg = np.ascontiguousarray(base_logs, np.float32).reshape(-1)
+        h = ctypes.c_void_p()
+        rc = self._lib.fire_timeline_create(_ptr(lg) if lg.size else None, lg.size // 8, int(steps_per_frame), ctypes.byref(h))
+        if rc:
+            raise FireError(rc, "fire_timeline_create")
+        self._h = h
+        self.dt = float(self._lib.fire_timeline_step_dt(self._h))
+
+    def time(self, j: int) -> float:
+        return float(self._lib.fire_timeline_step_time(self._h, int(j)))
+
+    def step(self, sim: "FireSim", j: int, sparks: Optional["Sparks"] = None, stream=None):
+        rc = self._lib.fire_timeline_step(self._h, sim._h, sparks._h if sparks is not None else None, int(j), _stream_handle(stream))
+        if rc:
+            raise FireError(rc, "fire_timeline_step")
+
+    def close(self):
+        if self._h is not None:
+            self._lib.fire_timeline_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------------------------------
