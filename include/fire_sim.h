@@ -293,6 +293,34 @@ int fire_sparks_buffer(FireSparks* s, void** dev_ptr, int* count);          /* z
 int fire_sparks_io(FireSparks* s, float* host, size_t bytes, int to_device);   /* count * 16 floats, sync */
 int fire_sparks_set_rate(FireSparks* s, float rate);                        /* sparks.rate alone         */
 
+/* ---- volume rendering of the fire (src/renderer.js pLights, pSharpen, pVolume) -------------------
+ * The renderer's fire light extraction (8 temporally filtered point lights, one per height band), the
+ * optional flame prefilter and the emission-absorption ray march of S (soot, temperature, heat release)
+ * and S2 (smoke) with single scattering of the lights, into a headless image of vw x vh pixels
+ * (vw = max(8, round(width * vol_scale))): per pixel radiance rgb and transmittance, plus haze and depth.
+ * The page's surfaces (logs, stones, ground), composite, bloom and tone map are rasterisation and display
+ * and are not part of this library; a caller may give the depth the march stops at.                    */
+typedef struct FireVolume FireVolume;
+/* white_balance_k: the camera white balance (the renderer uses 5000 K; 0 = none).                       */
+int fire_volume_create(FireSim* sim, int width, int height, float vol_scale, float white_balance_k, FireVolume** out);
+int fire_volume_destroy(FireVolume* v);
+int fire_volume_size(FireVolume* v, int* vw, int* vh);
+/* Renderer parameters (RP_FIELDS names): stepMul sootAbs sootEmit emitK blueK smokeScat smokeG detailAmt
+ * detailFreq detailSpeed lightK tempScale emitTempLo sootScat sootEdge cubic flameSharp flickerK lensX
+ * lensY focus.  Unknown names: FIRE_ERR_BAD_PARAM.                                                       */
+int fire_volume_set_params(FireVolume* v, const char* const* names, const float* values, int n);
+/* lookAt (src/camera.js:6-17); jitter in full-resolution pixels.                                        */
+int fire_volume_set_camera(FireVolume* v, const double pos[3], const double target[3], double fov_deg, float jit_x, float jit_y);
+int fire_volume_set_depth(FireVolume* v, const float* depth_dev, int width, int height);   /* NULL: none */
+/* The f32 uniforms the next render would use (returns their count, at most 64).                         */
+int fire_volume_uniforms(FireVolume* v, double time, int frame, float* out, int n);
+int fire_volume_render(FireVolume* v, double time, int frame, void* stream);
+/* which: 0 image (vw*vh*4 floats), 1 aux (vw*vh*2: haze, depth), 2 lights (8 * 8: pos+power,
+ * colour+spread), 3 blackbody LUT (2 * 1024 * 4).  Synchronous.                                          */
+int fire_volume_download(FireVolume* v, int which, float* host, size_t bytes);
+/* blackbodyLUT (src/blackbody.js:78-93): 2 rows (blackbody, soot) x n x (r, g, b, Y) over [tmin, tmax].   */
+int fire_blackbody_lut(int n, float tmin, float tmax, float white_balance_k, float* out);
+
 /* ---- the cinematic's timeline (src/timeline.js) and its capture-mode driver (src/main.js:128-160) ----
  * Host-only and deterministic.  Events: the scripted cue sheet plus the seeded background pops, sorted by
  * time.  fire_timeline_step(j) is capStep(j): the simulation's parameters (simAt) and log offsets

@@ -1206,6 +1206,174 @@ void orc_sparks_step(float* sp, int count, const float* U, const float* vel, int
   }
 }
 
+// ---- the renderer's fire passes (src/renderer.js:104-165 pLights, 194-326 pVolume), FP32.  U: the 60
+// uniforms in the library's order (fire_volume_uniforms); S, S2: float4 fields; lut: 2 x n x 4 blackbody
+// LUT; lights: 8 x (pos+power, colour+spread) as 16 float4. ----
+enum VolIdx {
+  V_width, V_height, V_vw, V_vh, V_time, V_frame, V_camX, V_camY, V_camZ, V_tanFov, V_fwdX, V_fwdY, V_fwdZ, V_aspect, V_rgtX, V_rgtY,
+  V_rgtZ, V_jitX, V_upX, V_upY, V_upZ, V_jitY, V_ox, V_oy, V_oz, V_dx, V_sx, V_sy, V_sz, V_tempScale, V_nx, V_ny, V_nz, V_nLights,
+  V_stepMul, V_sootAbs, V_sootEmit, V_emitK, V_blueK, V_smokeScat, V_smokeG, V_detailAmt, V_detailFreq, V_detailSpeed, V_lightK,
+  V_bbTmin, V_bbTmax, V_bbN, V_emitTempLo, V_sootScat, V_sootEdge, V_cubic, V_flameSharp, V_lightDt, V_flickerK, V_lensX, V_lensY,
+  V_focus, V_depthW, V_depthH, V_COUNT
+};
+static V3<float> bb_row(const float* U, const float* lut, float T, int row) {   // renderer.js:74-80
+  const float x = clampf((T - U[V_bbTmin]) / (U[V_bbTmax] - U[V_bbTmin]), 0.0f, 1.0f) * (U[V_bbN] - 1.0f);
+  const unsigned i = (unsigned)std::floor(x), n = (unsigned)U[V_bbN];
+  const float f = x - std::floor(x);
+  const float* a = lut + 4 * ((size_t)row * n + i);
+  const float* b = lut + 4 * ((size_t)row * n + std::min(i + 1u, n - 1u));
+  return V3<float>(mixf(a[0], b[0], f), mixf(a[1], b[1], f), mixf(a[2], b[2], f));
+}
+static float lumf(const V3<float>& c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
+
+void orc_volume_lights(const float* U, const float* S, int nx_, int ny_, int nz_, const float* lut, float* lstate, float* lights) {
+  const unsigned nx = nx_, ny = ny_, nz = nz_, NL = 8, bandH = ny / NL, hx = nx / 2, hb = bandH / 2, total = hx * hb * (nz / 2);
+  for (unsigned wg = 0; wg < NL; ++wg) {
+    const unsigned y0 = wg * bandH;
+    float P[256][4] = {}, C[256][4] = {};
+    for (unsigned li = 0; li < 256; ++li)   // the 256 lanes of the band's workgroup, each in its own order
+      for (unsigned i = li; i < total; i += 256) {
+        const unsigned ix = (i % hx) * 2, iy = ((i / hx) % hb) * 2 + y0, iz = (i / (hx * hb)) * 2;
+        const float* s = S + 4 * ((size_t)ix + (size_t)nx * (iy + (size_t)ny * iz));
+        const float T = 293.0f + s[0] * U[V_tempScale];
+        if (T < 700.0f) continue;
+        const V3<float> e = bb_row(U, lut, T, 1) * (s[2] * U[V_sootEmit]) * U[V_emitK];
+        const float w = lumf(e);
+        const V3<float> pos = V3<float>(U[V_ox], U[V_oy], U[V_oz]) + (V3<float>((float)ix, (float)iy, (float)iz) + V3<float>(1, 1, 1)) * U[V_dx];
+        P[li][0] += pos.x * w; P[li][1] += pos.y * w; P[li][2] += pos.z * w; P[li][3] += w;
+        C[li][0] += e.x; C[li][1] += e.y; C[li][2] += e.z; C[li][3] += dot3(pos, pos) * w;
+      }
+    for (unsigned s = 128; s > 0; s >>= 1)   // the workgroup's tree
+      for (unsigned li = 0; li < s; ++li)
+        for (int k = 0; k < 4; ++k) { P[li][k] += P[li + s][k]; C[li][k] += C[li + s][k]; }
+    const float w = P[0][3];
+    const V3<float> cen = w > 1e-6f ? V3<float>(P[0][0], P[0][1], P[0][2]) / w : V3<float>(0.0f, ((float)y0 + (float)bandH * 0.5f) * U[V_dx], 0.0f);
+    const float spread = w > 1e-6f ? std::fmax(C[0][3] / w - dot3(cen, cen), 0.0f) : 0.04f;
+    const V3<float> J = V3<float>(C[0][0], C[0][1], C[0][2]) * ((float)(nx * bandH * nz) / (float)total) * U[V_dx] * U[V_dx] * U[V_dx];
+    float* sp = lstate + 4 * wg;
+    float* sc = lstate + 4 * (NL + wg);
+    float* sm = lstate + 4 * (2 * NL + wg);
+    if (U[V_lightDt] < 0.0f || sm[3] <= 0.0f) {
+      const float a[4] = {cen.x, cen.y, cen.z, spread}, b[4] = {J.x, J.y, J.z, 0.0f}, c[4] = {J.x, J.y, J.z, 1.0f};
+      std::memcpy(sp, a, 16); std::memcpy(sc, b, 16); std::memcpy(sm, c, 16);
+    } else {
+      const float dtl = U[V_lightDt];
+      const float a = 1.0f - std::exp(-dtl / 0.08f), ap = 1.0f - std::exp(-dtl / 0.15f), am = 1.0f - std::exp(-dtl / 1.5f);
+      const float tgt[4] = {cen.x, cen.y, cen.z, spread};
+      for (int k = 0; k < 4; ++k) sp[k] = mixf(sp[k], tgt[k], ap);
+      const float Jv[3] = {J.x, J.y, J.z};
+      for (int k = 0; k < 3; ++k) { sc[k] = mixf(sc[k], Jv[k], a); sm[k] = mixf(sm[k], Jv[k], am); }
+      sc[3] = 0.0f; sm[3] = 1.0f;
+    }
+    const float ratio = lumf(V3<float>(sc[0], sc[1], sc[2])) / std::fmax(lumf(V3<float>(sm[0], sm[1], sm[2])), 1e-9f);
+    const V3<float> Jc = V3<float>(sc[0], sc[1], sc[2]) * std::pow(std::fmax(ratio, 1e-4f), U[V_flickerK] - 1.0f);
+    const float wl = lumf(Jc);
+    const bool on = wl > 1e-3f * lumf(V3<float>(sm[0], sm[1], sm[2])) && wl > 0.0f;
+    const float L[8] = {sp[0], sp[1], sp[2], on ? wl : 0.0f, on ? Jc.x : 0.0f, on ? Jc.y : 0.0f, on ? Jc.z : 0.0f, sp[3]};
+    std::memcpy(lights + 8 * wg, L, sizeof L);
+  }
+}
+
+void orc_volume_render(const float* U, const float* S, const float* S2, int nx, int ny, int nz, const float* curl, int N, const float* lut,
+                       const float* lights, float* vol, float* aux) {
+  const std::vector<float> sv(S, S + 4 * (size_t)nx * ny * nz), s2v(S2, S2 + 4 * (size_t)nx * ny * nz);
+  const int vw = (int)U[V_vw], vh = (int)U[V_vh];
+  auto smooth = [](float e0, float e1, float x) { return smoothstep(e0, e1, x); };
+  auto fract = [](float x) { return x - std::floor(x); };
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int iy = 0; iy < vh; ++iy)
+    for (int ix = 0; ix < vw; ++ix) {
+      const float pxx = (float)ix + 0.5f + U[V_jitX] * (U[V_vw] / U[V_width]), pxy = (float)iy + 0.5f + U[V_jitY] * (U[V_vw] / U[V_width]);
+      const float ndx = pxx / U[V_vw] * 2.0f - 1.0f, ndy = 1.0f - pxy / U[V_vh] * 2.0f;
+      const V3<float> fwd(U[V_fwdX], U[V_fwdY], U[V_fwdZ]), rgt(U[V_rgtX], U[V_rgtY], U[V_rgtZ]), up(U[V_upX], U[V_upY], U[V_upZ]);
+      V3<float> dPin = fwd + rgt * ndx * U[V_tanFov] * U[V_aspect] + up * ndy * U[V_tanFov];
+      dPin = dPin / std::sqrt(dot3(dPin, dPin));
+      V3<float> ro(U[V_camX], U[V_camY], U[V_camZ]), rd = dPin;
+      if (U[V_focus] > 0.0f) {
+        const V3<float> o = ro + rgt * U[V_lensX] + up * U[V_lensY];
+        const V3<float> q = ro + dPin * (U[V_focus] / dot3(dPin, fwd));
+        const V3<float> dq = q - o;
+        ro = o;
+        rd = dq / std::sqrt(dot3(dq, dq));
+      }
+      const float sd = 1e9f;
+      const V3<float> bmin(U[V_ox], U[V_oy], U[V_oz]), bmax = bmin + V3<float>(U[V_sx], U[V_sy], U[V_sz]);
+      const V3<float> inv(1.0f / rd.x, 1.0f / rd.y, 1.0f / rd.z);
+      const V3<float> t0 = (bmin - ro) * inv, t1 = (bmax - ro) * inv;
+      const float tn = std::fmax(std::fmax(std::fmax(std::fmin(t0.x, t1.x), std::fmin(t0.y, t1.y)), std::fmin(t0.z, t1.z)), 0.0f);
+      const float tf = std::fmin(std::fmin(std::fmin(std::fmax(t0.x, t1.x), std::fmax(t0.y, t1.y)), std::fmax(t0.z, t1.z)), sd);
+      V3<float> L;
+      float Tr = 1.0f, haze = 0.0f;
+      if (tf > tn) {
+        const float ds = U[V_dx] * U[V_stepMul];
+        const float fm = std::fmod(U[V_frame], 64.0f);
+        const float ipx = (float)ix + 5.588238f * fm, ipy = (float)iy + 5.588238f * fm;
+        const float jit = fract(52.9829189f * fract(ipx * 0.06711056f + ipy * 0.00583715f));
+        float t = tn + ds * jit;
+        const V3<float> dims(U[V_nx], U[V_ny], U[V_nz]);
+        for (int it = 0; it < 1200; ++it) {
+          if (t > tf || Tr < 0.003f) break;
+          const V3<float> p = ro + rd * t;
+          V3<float> g = (p - bmin) / U[V_dx];
+          float mottle = 0.0f;
+          if (U[V_detailAmt] > 0.0f) {
+            const float rise = U[V_detailSpeed] * (0.5f + 1.5f * smooth(0.0f, 1.0f, p.y));
+            const float ph = U[V_time] / 0.7f;
+            const float f0 = fract(ph), f1 = fract(ph + 0.5f);
+            const float w0 = 1.0f - std::fabs(2.0f * f0 - 1.0f);
+            const V3<float> o0 = V3<float>(0.37f, 0.0f, 0.61f) * std::floor(ph), o1 = V3<float>(0.71f, 0.0f, 0.29f) * std::floor(ph + 0.5f);
+            const V3<float> q0 = (p - V3<float>(0.0f, rise * f0 * 0.7f, 0.0f)) * U[V_detailFreq] * 0.25f + o0;
+            const V3<float> q1 = (p - V3<float>(0.0f, rise * f1 * 0.7f, 0.0f)) * U[V_detailFreq] * 0.25f + o1;
+            const V4<float> c0 = sample_repeat(curl, N, q0), c1 = sample_repeat(curl, N, q1);
+            const V4<float> cw = c0 * w0 + c1 * (1.0f - w0);
+            g = g + (cw.xyz() * (U[V_detailAmt] * 0.12f)) * V3<float>(1.0f, 0.6f, 1.0f);
+            mottle = cw.w * 0.08f - 0.6f;
+          }
+          V4<float> s = sample_clamp(sv, nx, ny, nz, g);   // the cubic option is not restated
+          const float edge = std::fmin(std::fmin(g.x, dims.x - g.x), std::fmin(g.z, dims.z - g.z));
+          const float fade = smooth(0.02f, 0.15f, edge * U[V_dx]) * smooth(0.0f, 0.4f, (dims.y - g.y) * U[V_dx]);
+          s = s * fade;
+          const float T = 293.0f + s.x * U[V_tempScale] + mottle * 60.0f * U[V_detailAmt] * (s.x >= 0.3f ? 1.0f : 0.0f);
+          float soot = s.z;
+          if (U[V_sootEdge] > 0.0f) soot *= smooth(0.6f * U[V_sootEdge], 1.4f * U[V_sootEdge], soot);
+          float smoke = 0.0f;
+          if (U[V_smokeScat] > 0.0f) smoke = sample_clamp(s2v, nx, ny, nz, g).z * fade;
+          if (soot > 1e-4f || s.w > 1e-3f || smoke > 1e-4f) {
+            const float sigSoot = soot * U[V_sootAbs];
+            const float sigS = sigSoot * U[V_sootScat] + smoke * U[V_smokeScat];
+            const float sigT = sigSoot + smoke * U[V_smokeScat] * 1.1f + 1e-6f;
+            V3<float> e;
+            if (T > U[V_emitTempLo]) e = bb_row(U, lut, T, 1) * (soot * U[V_sootEmit]) * U[V_emitK];
+            e = e + V3<float>(0.15f, 0.3f, 1.0f) * std::pow(s.w, 1.6f) * (U[V_blueK] / 3.0f) * std::exp(-soot * 2.0f);
+            V3<float> ins;
+            if (sigS * Tr > 1e-6f) {
+              for (int k = 0; k < (int)U[V_nLights]; ++k) {
+                const float* Lk = lights + 8 * k;
+                const V3<float> toL = V3<float>(Lk[0], Lk[1], Lk[2]) - p;
+                const float r2 = dot3(toL, toL) + Lk[7] * 0.6f + 0.004f;
+                const float c = dot3(rd, toL * (1.0f / std::sqrt(r2)));
+                const float g2 = U[V_smokeG] * U[V_smokeG];
+                const float hgv = (1.0f - g2) / (4.0f * 3.14159265f * std::pow(1.0f + g2 - 2.0f * U[V_smokeG] * c, 1.5f));
+                ins = ins + V3<float>(Lk[4], Lk[5], Lk[6]) * hgv / r2;
+              }
+              ins = ins * (sigS * U[V_lightK]);
+            }
+            const float a = std::exp(-sigT * ds);
+            const float w = sigT * ds < 1e-4f ? ds : (1.0f - a) / sigT;
+            L = L + (e + ins) * Tr * w;
+            Tr *= a;
+          }
+          haze += std::fmax(s.x - 0.05f, 0.0f) * ds;
+          t += ds;
+        }
+      }
+      float* o = vol + 4 * ((size_t)ix + (size_t)vw * iy);
+      o[0] = L.x; o[1] = L.y; o[2] = L.z; o[3] = Tr;
+      aux[2 * ((size_t)ix + (size_t)vw * iy)] = haze;
+      aux[2 * ((size_t)ix + (size_t)vw * iy) + 1] = sd;
+    }
+}
+
 // ---- FP64 reference solution of the step's pressure equation (the operator of k_smooth / k_restrict:
 // sum of the six ghost-ruled neighbours minus 6 p, over h^2; p = 0 on sides and top, zero gradient at the
 // floor, src/sim.js:417-466).  -A is symmetric positive definite, so conjugate gradients apply. ----

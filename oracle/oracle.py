@@ -63,6 +63,8 @@ def lib():
             "orc_pressure_rel_residual": (dp, [ip, ip, ip, dp, vp, vp]),
             "orc_pressure_cg": (ip, [ip, ip, ip, dp, vp, vp, dp, ip, vp]),
             "orc_sparks_step": (None, [vp, ip, vp, vp, ip, ip, ip, vp, ip]),
+            "orc_volume_lights": (None, [vp, vp, ip, ip, ip, vp, vp, vp]),
+            "orc_volume_render": (None, [vp, vp, vp, ip, ip, ip, vp, ip, vp, vp, vp, vp]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -117,6 +119,30 @@ def sparks_step(sparks: np.ndarray, uniforms: np.ndarray, vel: np.ndarray, curl:
     nz, ny, nx = v.shape[:3]
     lib().orc_sparks_step(_ptr(s), s.shape[0], _ptr(U), _ptr(v), nx, ny, nz, _ptr(c), c.shape[0])
     return s
+
+
+def volume_lights(uniforms, S, lut, lstate):
+    """pLights (src/renderer.js:104-165): returns (lights (8, 8), new lstate (24, 4))."""
+    U = np.ascontiguousarray(uniforms, np.float32)
+    s = np.ascontiguousarray(S, np.float32)
+    L = np.ascontiguousarray(lut, np.float32)
+    st = np.ascontiguousarray(lstate, np.float32).copy()
+    out = np.zeros((8, 8), np.float32)
+    nz, ny, nx = s.shape[:3]
+    lib().orc_volume_lights(_ptr(U), _ptr(s), nx, ny, nz, _ptr(L), _ptr(st), _ptr(out))
+    return out, st
+
+
+def volume_render(uniforms, S, S2, curl, lut, lights):
+    """pVolume (src/renderer.js:194-326) without a depth buffer: returns (image (vh, vw, 4), aux (vh, vw, 2))."""
+    U = np.ascontiguousarray(uniforms, np.float32)
+    s, s2 = np.ascontiguousarray(S, np.float32), np.ascontiguousarray(S2, np.float32)
+    c, L, li = np.ascontiguousarray(curl, np.float32), np.ascontiguousarray(lut, np.float32), np.ascontiguousarray(lights, np.float32)
+    vw, vh = int(U[2]), int(U[3])
+    img, aux = np.zeros((vh, vw, 4), np.float32), np.zeros((vh, vw, 2), np.float32)
+    nz, ny, nx = s.shape[:3]
+    lib().orc_volume_render(_ptr(U), _ptr(s), _ptr(s2), nx, ny, nz, _ptr(c), c.shape[0], _ptr(L), _ptr(li), _ptr(img), _ptr(aux))
+    return img, aux
 
 
 def pressure_apply(x: np.ndarray, h: float) -> np.ndarray:

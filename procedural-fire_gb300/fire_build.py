@@ -27,6 +27,8 @@ SOURCES = {
     "fire_noalloc.cu": [],
     "fire_poisson.cu": [],
     "fire_sparks.cu": [],
+    "fire_volume.cu": [],
+    "fire_blackbody.cpp": [],
     "fire_scene.cpp": [],
     "fire_timeline.cpp": [],
 }

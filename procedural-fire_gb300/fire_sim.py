@@ -115,6 +115,16 @@ _SIGS = {
     "fire_sparks_buffer": (_ip, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_ip)]),
     "fire_sparks_io": (_ip, [_vp, _vp, _sz, _ip]),
     "fire_sparks_set_rate": (_ip, [_vp, _fp]),
+    "fire_volume_create": (_ip, [_vp, _ip, _ip, _fp, _fp, ctypes.POINTER(_vp)]),
+    "fire_volume_destroy": (_ip, [_vp]),
+    "fire_volume_size": (_ip, [_vp, ctypes.POINTER(_ip), ctypes.POINTER(_ip)]),
+    "fire_volume_set_params": (_ip, [_vp, ctypes.POINTER(ctypes.c_char_p), _vp, _ip]),
+    "fire_volume_set_camera": (_ip, [_vp, _vp, _vp, _dp, _fp, _fp]),
+    "fire_volume_set_depth": (_ip, [_vp, _vp, _ip, _ip]),
+    "fire_volume_uniforms": (_ip, [_vp, _dp, _ip, _vp, _ip]),
+    "fire_volume_render": (_ip, [_vp, _dp, _ip, _vp]),
+    "fire_volume_download": (_ip, [_vp, _ip, _vp, _sz]),
+    "fire_blackbody_lut": (_ip, [_ip, _fp, _fp, _fp, _vp]),
     "fire_timeline_event_count": (_ip, []),
     "fire_timeline_events": (_ip, [_vp, _ip]),
     "fire_timeline_intensity_at": (_dp, [_dp]),
@@ -500,6 +510,81 @@ class Sparks:
     def upload(self, arr: np.ndarray):
         a = np.ascontiguousarray(arr, np.float32)
         self._check(self._lib.fire_sparks_io(self._h, _ptr(a), a.nbytes, 1), "fire_sparks_io")
+
+
+# ---------------------------------------------------------------------------------------------------
+def blackbody_lut(n: int = 1024, tmin: float = 400.0, tmax: float = 3000.0, white_balance: float = 5000.0) -> np.ndarray:
+    """blackbodyLUT (src/blackbody.js:78-93) as (2, n, 4): rows blackbody and soot, (r, g, b, Y)."""
+    out = np.zeros((2, n, 4), np.float32)
+    rc = load_library().fire_blackbody_lut(n, tmin, tmax, white_balance, _ptr(out))
+    if rc:
+        raise FireError(rc, "fire_blackbody_lut")
+    return out
+
+
+class Volume:
+    """The renderer's fire passes (lights, prefilter, ray march) into a vw x vh image of `sim`."""
+
+    def __init__(self, sim: "FireSim", width: int = 540, height: int = 960, vol_scale: float = 0.5, white_balance: float = 5000.0):
+        self._lib = load_library()
+        self.sim = sim
+        h = ctypes.c_void_p()
+        rc = self._lib.fire_volume_create(sim._h, int(width), int(height), float(vol_scale), float(white_balance), ctypes.byref(h))
+        if rc:
+            raise FireError(rc, "fire_volume_create")
+        self._h = h
+        a, b = ctypes.c_int(), ctypes.c_int()
+        self._lib.fire_volume_size(self._h, ctypes.byref(a), ctypes.byref(b))
+        self.vw, self.vh = a.value, b.value
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            raise FireError(rc, what)
+
+    def close(self):
+        if self._h is not None:
+            self._lib.fire_volume_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params: Dict[str, float]):
+        names = (ctypes.c_char_p * len(params))(*[k.encode() for k in params])
+        vals = np.array(list(params.values()), np.float32)
+        self._check(self._lib.fire_volume_set_params(self._h, names, _ptr(vals), len(params)), "fire_volume_set_params")
+
+    def set_camera(self, pos, target, fov: float = 40.0, jitter=(0.0, 0.0)):
+        p, t = np.asarray(pos, np.float64), np.asarray(target, np.float64)
+        self._check(self._lib.fire_volume_set_camera(self._h, _ptr(p), _ptr(t), float(fov), float(jitter[0]), float(jitter[1])),
+                    "fire_volume_set_camera")
+
+    def uniforms(self, time: float, frame: int) -> np.ndarray:
+        out = np.zeros(64, np.float32)
+        n = self._lib.fire_volume_uniforms(self._h, float(time), int(frame), _ptr(out), 64)
+        if n < 0:
+            raise FireError(n, "fire_volume_uniforms")
+        return out[:n]
+
+    def render(self, time: float, frame: int, stream=None):
+        self._check(self._lib.fire_volume_render(self._h, float(time), int(frame), _stream_handle(stream)), "fire_volume_render")
+
+    def _get(self, which: int, shape) -> np.ndarray:
+        out = np.zeros(shape, np.float32)
+        self._check(self._lib.fire_volume_download(self._h, which, _ptr(out), out.nbytes), "fire_volume_download")
+        return out
+
+    def image(self) -> np.ndarray:
+        return self._get(0, (self.vh, self.vw, 4))
+
+    def aux(self) -> np.ndarray:
+        return self._get(1, (self.vh, self.vw, 2))
+
+    def lights(self) -> np.ndarray:
+        return self._get(2, (8, 8))
 
 
 # ---------------------------------------------------------------------------------------------------
