@@ -343,6 +343,85 @@ def run_ensemble(dev: int, steps: int = 20):
             "speedup": ms_single / ms_batched}
 
 
+# Inverse source fit through the discrete adjoint: 64x128x64 cells at 1 cm, dt = 1/120, 120 steps from rest,
+# 8 floor spots.  The target is the final temperature and soot of a run with seed-A fluxes; the fit starts
+# from seed-B fluxes at the same positions; checkpoints every 10 steps.
+ADJOINT = dict(name="adjoint-fit-64x128x64", res=(64, 128, 64), size=(0.64, 1.28, 0.64), dt=1.0 / 120.0, steps=120,
+               checkpoint=10, spots=8, seed_a=11, seed_b=12, sigma=0.02, radius=0.12, mg_tol=1e-5, mg_max_cycles=8,
+               iterations=3)
+
+
+def run_adjoint(dev: int):
+    """Forward and adjoint time per step of the source fit, and a few gradient steps on the fluxes."""
+    import torch
+    import fire_sim as F
+    A = ADJOINT
+    st = torch.cuda.current_stream(dev)
+    spots_a = F.make_spots(A["seed_a"], A["spots"], 1.0, 4.0, A["sigma"], A["radius"])
+    spots_b = spots_a.copy()
+    spots_b[:, 4] = F.make_spots(A["seed_b"], A["spots"], 1.0, 4.0, A["sigma"], A["radius"])[:, 4]
+
+    def make(spots):
+        s = F.FireSim(res=A["res"], size=A["size"], vcycles=4, device=dev, mg_max_cycles=A["mg_max_cycles"], mg_tol=A["mg_tol"])
+        s.set_params({"vortEps": 0.3, "turbAmp": 0.2})
+        s.set_soot_age(0.02, 0.06)
+        s.set_bed_gain(0.0)
+        s.set_spots(spots)
+        return s
+
+    # the target, and the plain forward's time per step (the step graph, same solve)
+    sim = make(spots_a)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    sim.step(A["dt"], A["steps"], stream=st.cuda_stream)
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms_plain = e0.elapsed_time(e1) / A["steps"]
+    target = sim.download("S").astype(np.float32)
+    sim.close()
+    sim = make(spots_b)
+    adj = F.Adjoint(sim, A["steps"], A["checkpoint"])
+    flux = spots_b[:, 4].astype(np.float64)
+    hist, fwd, bwd = [], [], []
+    for it in range(A["iterations"] + 1):
+        sim.reset()
+        sp = spots_b.copy()
+        sp[:, 4] = flux
+        sim.set_spots(sp)
+        adj.forward(A["dt"], stream=st.cuda_stream)
+        loss = adj.loss(target)
+        adj.backward(stream=st.cuda_stream)
+        g = adj.grad_spots(A["spots"])
+        f_ms, b_ms = adj.timing()
+        fwd.append(f_ms / A["steps"])
+        bwd.append(b_ms / A["steps"])
+        hist.append({"loss": loss, "flux_err_gps": float(np.abs(flux - spots_a[:, 4]).max()), "grad_norm": float(np.linalg.norm(g))})
+        if it == A["iterations"]:
+            break
+        # a projected gradient step on the fluxes along -g, backtracking from 0.5 g/s until the loss drops
+        step = 0.5
+        for _ in range(4):
+            trial = np.clip(flux - step * g / max(np.linalg.norm(g), 1e-30), 0.0, 8.0)
+            sim.reset()
+            sp = spots_b.copy()
+            sp[:, 4] = trial
+            sim.set_spots(sp)
+            adj.forward(A["dt"], stream=st.cuda_stream)
+            if adj.loss(target) < loss:
+                break
+            step *= 0.5
+        flux = trial
+    adj.close()
+    sim.close()
+    fwd_ms, bwd_ms = float(np.median(fwd[1:] or fwd)), float(np.median(bwd[1:] or bwd))
+    return {"workload": A["name"], "steps": A["steps"], "checkpoint_every": A["checkpoint"],
+            "mg": f"V(2,2) to {A['mg_tol']} rel. residual, max {A['mg_max_cycles']}",
+            "ms_per_step_forward_plain": ms_plain, "ms_per_step_forward_taped": fwd_ms,
+            "ms_per_step_backward": bwd_ms, "adjoint_over_forward": bwd_ms / ms_plain,
+            "backward_includes": "recompute of every segment but the last from its checkpoint, then the reverse steps",
+            "fit": hist}
+
+
 # ------------------------------------------------------------------------------------------ arms
 def run_ours(args):
     import torch
@@ -456,12 +535,15 @@ def run_ours(args):
         "poisson": None,
     }
     out["ensemble"] = None
-    if world == 1 and not (args.no_poisson and args.no_ensemble):
+    out["adjoint"] = None
+    if world == 1 and not (args.no_poisson and args.no_ensemble and args.no_adjoint):
         sim.close()   # frees the step's arena before the standalone workloads
         if not args.no_poisson:
             out["poisson"] = run_poisson(dev)
         if not args.no_ensemble:
             out["ensemble"] = run_ensemble(dev)
+        if not args.no_adjoint:
+            out["adjoint"] = run_adjoint(dev)
     return out
 
 
@@ -520,6 +602,7 @@ def main(argv=None):
     ap.add_argument("--preroll", type=int, default=WORKLOAD["preroll"], help="untimed steps that develop the fire")
     ap.add_argument("--no-poisson", action="store_true", help="skip the standalone 256x512x256 pressure-solve timings")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-fire ensemble timings")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint source-fit timings")
     ap.add_argument("--mg-fixed", type=int, default=0,
                     help="profiling aid: N fixed V-cycles per step instead of the residual-driven solve")
     args = ap.parse_args(argv)

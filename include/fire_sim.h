@@ -406,6 +406,59 @@ int fire_poisson_make_rhs(FirePoisson* ps, float* b, unsigned seed, int n_source
  * amplitude); host only.                                                                                */
 int fire_poisson_sources(unsigned seed, int n_sources, const int res[3], float* out);
 
+/* ---- discrete adjoint of the step and checkpointed rollouts -----------------------------------------
+ * Reverse-mode derivatives of FireSim.step (src/sim.js:627-648) over a rollout of n steps: the adjoint of
+ * each stage (advect, sources, projection) linearised at the branch the forward took (every min / max /
+ * clamp, the MacCormack limiter, the speed clamps), the pressure solve treated as p = A^-1 b with A the
+ * multigrid's symmetric operator (so its adjoint is the same solve).  The rollout keeps the state every
+ * `checkpoint_every` steps; the backward recomputes one segment at a time into a tape and runs the
+ * adjoint steps over it.  No counterpart in the reference (it has no derivatives).
+ *
+ *   fire_adjoint_forward   n steps of dt from the simulation's current state (per-step parameter blocks
+ *                          and event envelopes as fire_sim_step), leaving the simulation in the final state.
+ *   fire_adjoint_loss      L = sum over cells (1000 (S.x - T.x))^2 + (S.z - T.z)^2 (temperature in kelvin,
+ *                          soot) against a target S field; seeds the final-state cotangents with dL.
+ *   fire_adjoint_seed      or seeds arbitrary final-state cotangents (vel, S, S2; NULL = zero).
+ *   fire_adjoint_backward  the reverse sweep: afterwards FIRE_ADJ_VEL / S / S2 hold the cotangents of the
+ *                          rollout's initial state and fire_adjoint_grad_spots the spot-flux gradients.
+ * Cotangent buffers (float4 per cell unless noted), read and written with fire_adjoint_io:                */
+enum {
+  FIRE_ADJ_VEL = 0, FIRE_ADJ_S = 1, FIRE_ADJ_S2 = 2,            /* state                                  */
+  FIRE_ADJ_VELX = 3, FIRE_ADJ_SX = 4, FIRE_ADJ_S2X = 5,         /* advection hats                          */
+  FIRE_ADJ_VELY = 6, FIRE_ADJ_SY = 7, FIRE_ADJ_S2Y = 8,         /* advected fields                         */
+  FIRE_ADJ_F = 9,                                               /* forces output velocity (xyz), phi (w)   */
+  FIRE_ADJ_W = 10,                                              /* vorticity (xyz) and its magnitude (w)   */
+  FIRE_ADJ_G = 11,                                              /* projection scratch                      */
+  FIRE_ADJ_P = 12, FIRE_ADJ_B = 13,                             /* pressure p, divergence b (1 float)      */
+  FIRE_ADJ_COUNT = 14
+};
+typedef struct FireAdjoint FireAdjoint;
+/* n_steps >= 1, 1 <= checkpoint_every <= 64.  Device memory: (k + 1) * 3 + k * 7 + 12 float4 fields plus
+ * (n_steps / k + 1) * 3 checkpoint fields.  The solve mode (fixed V-cycles or residual-driven) is the
+ * simulation's at creation.                                                                             */
+int fire_adjoint_create(FireSim* sim, int n_steps, int checkpoint_every, FireAdjoint** out);
+int fire_adjoint_destroy(FireAdjoint* adj);
+int fire_adjoint_forward(FireAdjoint* adj, float dt, void* stream);
+/* target_S: host float4 field (x fastest); loss: out, synchronous.                                       */
+int fire_adjoint_loss(FireAdjoint* adj, const float* target_S, double* loss);
+int fire_adjoint_seed(FireAdjoint* adj, const float* d_vel, const float* d_S, const float* d_S2);
+int fire_adjoint_backward(FireAdjoint* adj, void* stream);
+/* dL/d(flux) of each spot in g/s (n <= the simulation's spot count), synchronous.                         */
+int fire_adjoint_grad_spots(FireAdjoint* adj, double* out, int n);
+/* dir 0: device -> host, 1: host -> device; bytes must be the buffer's size.                              */
+int fire_adjoint_io(FireAdjoint* adj, int which, void* host, size_t bytes, int dir);
+/* Zeroes every cotangent buffer and the spot gradients.                                                   */
+int fire_adjoint_clear(FireAdjoint* adj);
+/* One stage's adjoint at the simulation's own current fields (the stage-level counterpart of
+ * fire_sim_run_stage), with parameter block for dt: FIRE_STAGE_ADV1 / ADV2 / FORCES (with the curl) / DIV /
+ * PROJECT, or FIRE_STAGE_VCYCLE: `arg` V-cycles of the pressure solve on FIRE_ADJ_P into FIRE_ADJ_B.
+ * Each reads the cotangents of the stage's outputs and adds into those of its inputs: ADV1 velX,SX,S2X ->
+ * vel,S,S2; ADV2 velY,SY,S2Y -> vel,S,S2 and the hats; FORCES F,S,S2 -> velY (added), SY,S2Y (written),
+ * spot gradients; DIV B -> F (added); PROJECT vel -> F (written), P.                                         */
+int fire_adjoint_stage(FireAdjoint* adj, int stage, float dt, int arg, void* stream);
+/* Timing of the last forward / backward (GPU milliseconds, CUDA events on the call's stream).              */
+int fire_adjoint_timing(FireAdjoint* adj, float* forward_ms, float* backward_ms);
+
 /* ---- library ----------------------------------------------------------------------------------- */
 /* 1 if the library's kernels were built for the current device's architecture, else 0.             */
 int fire_device_ok(int device);

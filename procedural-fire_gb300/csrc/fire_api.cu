@@ -58,80 +58,14 @@ void launch_mg_counter_reset(int* counter, cudaStream_t st);
 using namespace fire;
 
 namespace {
-constexpr int RING_SLOTS = 256;
-constexpr int SLOT_FLOATS = BLOCK_FLOATS + MAX_LOGS * 8;   // param block + log buffer (1312 bytes)
 constexpr size_t ALIGN = 256;
 size_t align_up(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
 }  // namespace
 
-struct FireSim {
-  int device = 0;
-  int res[3] = {0, 0, 0};
-  float size[3] = {0, 0, 0};
-  double dx = 0;
-  float origin[3] = {0, 0, 0};
-  int vcycles = 2;
-  int mg_max_cycles = 0;
-  double mg_tol = 0;
-  double time = 0;
-  long long frame = 0;
-  float params[P_STRIDE];
-  float ext[E_COUNT];
-  float logs[MAX_LOGS * 8];
-  int nLogs = 0;
-  bool geoReady = false;
-  bool logsDirty = true;
+#include "fire_simobj.h"
 
-  // device
-  void* arena = nullptr;
-  size_t arenaBytes = 0;
-  Fields f{};
-  Dims d{};
-  std::vector<MGLevel> levels;
-  int coarseIters = 8;
-  int tailFirst = 0;
-  uint2* noise = nullptr;
-  uint2* curl = nullptr;
-  float* dBlock = nullptr;
-  float* dLogs = nullptr;
-  double* dPartials = nullptr;
-  int partialsCount = 0;
-  double* dSmall = nullptr;     // [0..1] residual sums, [2..17] stats, [18] hrr, [19] rel residual
-  int* dCounter = nullptr;      // V-cycles run by the residual-driven loop
-
-  // host staging
-  float* hRing = nullptr;
-  cudaEvent_t ringEv[RING_SLOTS];
-  bool ringUsed[RING_SLOTS];
-  int ringPos = 0;
-  double* hSmall = nullptr;     // pinned mirror of dSmall
-  int* hCounter = nullptr;
-
-  cudaStream_t capStream = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  bool graphProfiled = false;
-  bool profiling = false;
-  cudaEvent_t stageEv[FIRE_STAGE_COUNT + 1];
-  cudaEvent_t doneEv = nullptr;
-  bool profiledStepPending = false;
-
-  // events (src/main.js:401-407, 456-461)
-  double burstUntil = -1;
-  float burstAmt = 0;
-  bool burstActive = false;
-  double gustLeft = 0, gustDur = 2.4;
-  float gustStrength = 1;
-  bool gustActive = false;
-  float windBase[2] = {0, 0};
-
-  int lastCycles = 0;
-  double lastRel = -1;
-  long long stepsRun = 0;
-  std::string err;
-};
-
-namespace {
+namespace fire {
+namespace rt {
 
 int set_err(FireSim* s, int code, const char* fmt, ...) {
   char buf[512];
@@ -355,7 +289,9 @@ int ensure_geo(FireSim* sim, cudaStream_t st) {
   return FIRE_OK;
 }
 
-}  // namespace
+}  // namespace rt
+}  // namespace fire
+using namespace fire::rt;
 
 // =====================================================================================================
 extern "C" {

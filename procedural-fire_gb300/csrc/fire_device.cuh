@@ -214,4 +214,34 @@ __device__ __forceinline__ float4 sample_table(const uint2* __restrict__ tab, f3
   return lerp4(lerp4(c00, c10, fy), lerp4(c01, c11, fy), fz);
 }
 
+
+// ---- shared by the step kernels (fire_step.cu) and their adjoints (fire_adjoint.cu) ----
+// Scalars entering from outside the domain are ambient (src/sim.js:137-140)
+__device__ __forceinline__ float outside_fade(f3 c, Dims d) {
+  float lo = fminf(c.x, c.z);
+  float hi = fmaxf(c.x - (float)d.nx, fmaxf(c.y - (float)d.ny, c.z - (float)d.nz));
+  return clampf(1.0f - fmaxf(-lo, hi), 0.0f, 1.0f);
+}
+// RK2 midpoint back-trace in cells (src/sim.js:129-135).  The first velocity sample sits exactly on the
+// cell centre, where the trilinear weights are (1, 0) on every axis, so it equals the cell's own value.
+__device__ __forceinline__ f3 backtrace(const float4* __restrict__ vel, f3 c, f3 v0, float dt, float dx, Dims d) {
+  f3 mid = c - v0 * (0.5f * dt) / dx;
+  f3 v1 = xyz(sample(vel, make_tap(mid, d), d));
+  return c - v1 * dt / dx;
+}
+
+// Vorticity at cell (x, y, z) (already inside the domain), from clamped velY neighbours.
+__device__ __forceinline__ float4 curl_at(const float4* __restrict__ v, int x, int y, int z, Dims d) {
+  f3 L = xyz(ldc(v, x - 1, y, z, d)), R = xyz(ldc(v, x + 1, y, z, d));
+  f3 B = xyz(ldc(v, x, y - 1, z, d)), T = xyz(ldc(v, x, y + 1, z, d));
+  f3 K = xyz(ldc(v, x, y, z - 1, d)), F = xyz(ldc(v, x, y, z + 1, d));
+  f3 w = mk3((T.z - B.z) - (F.y - K.y), (F.x - K.x) - (R.z - L.z), (R.y - L.y) - (T.x - B.x)) * 0.5f;
+  return make_float4(w.x, w.y, w.z, len3(w));
+}
+
+__device__ __forceinline__ float4 noise4(const uint2* __restrict__ tab, f3 q) {    // src/sim.js:228
+  float4 t = sample_table(tab, q);
+  return make_float4(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f, t.w * 2.0f - 1.0f);
+}
+
 }  // namespace fire

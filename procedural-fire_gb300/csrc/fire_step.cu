@@ -37,19 +37,6 @@ __device__ __forceinline__ CellId cell_id(Dims d) { return cell_id(d, blockIdx);
 static dim3 grid_for(Dims d) { return dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, (d.nz + BZ - 1) / BZ); }
 static dim3 block_shape() { return dim3(BX, BY, BZ); }
 
-// Scalars entering from outside the domain are ambient (src/sim.js:137-140)
-__device__ __forceinline__ float outside_fade(f3 c, Dims d) {
-  float lo = fminf(c.x, c.z);
-  float hi = fmaxf(c.x - (float)d.nx, fmaxf(c.y - (float)d.ny, c.z - (float)d.nz));
-  return clampf(1.0f - fmaxf(-lo, hi), 0.0f, 1.0f);
-}
-// RK2 midpoint back-trace in cells (src/sim.js:129-135).  The first velocity sample sits exactly on the
-// cell centre, where the trilinear weights are (1, 0) on every axis, so it equals the cell's own value.
-__device__ __forceinline__ f3 backtrace(const float4* __restrict__ vel, f3 c, f3 v0, float dt, float dx, Dims d) {
-  f3 mid = c - v0 * (0.5f * dt) / dx;
-  f3 v1 = xyz(sample(vel, make_tap(mid, d), d));
-  return c - v1 * dt / dx;
-}
 
 // ---------------- adv1 (src/sim.js:142-157) ----------------
 __device__ __forceinline__ void adv1_body(const float* __restrict__ P, const Fields& f, Dims d, uint3 blk) {
@@ -116,14 +103,6 @@ __device__ __forceinline__ void adv2_body(const float* __restrict__ P, const Fie
 }
 
 // ---------------- curl (src/sim.js:200-211) ----------------
-// Vorticity at cell (x, y, z) (already inside the domain), from clamped velY neighbours.
-__device__ __forceinline__ float4 curl_at(const float4* __restrict__ v, int x, int y, int z, Dims d) {
-  f3 L = xyz(ldc(v, x - 1, y, z, d)), R = xyz(ldc(v, x + 1, y, z, d));
-  f3 B = xyz(ldc(v, x, y - 1, z, d)), T = xyz(ldc(v, x, y + 1, z, d));
-  f3 K = xyz(ldc(v, x, y, z - 1, d)), F = xyz(ldc(v, x, y, z + 1, d));
-  f3 w = mk3((T.z - B.z) - (F.y - K.y), (F.x - K.x) - (R.z - L.z), (R.y - L.y) - (T.x - B.x)) * 0.5f;
-  return make_float4(w.x, w.y, w.z, len3(w));
-}
 __global__ void __launch_bounds__(256) k_curl(Fields f, Dims d) {
   CellId id = cell_id(d);
   if (!id.ok) return;
@@ -134,10 +113,6 @@ __global__ void __launch_bounds__(256) k_curl(Fields f, Dims d) {
 // The reference runs a separate curl dispatch into a vorticity texture and reads 7 taps of it here.
 // This kernel computes those 7 vorticity values from velY directly (the taps are clamped to the
 // domain exactly as `ld` clamps them), so the vorticity field never round-trips through HBM.
-__device__ __forceinline__ float4 noise4(const uint2* __restrict__ tab, f3 q) {    // src/sim.js:228
-  float4 t = sample_table(tab, q);
-  return make_float4(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f, t.w * 2.0f - 1.0f);
-}
 // Per-cell physics of the forces kernel.  `nb` supplies the velY/vorticity neighbourhood: the centre
 // velY value, the centre vorticity, the gradient of |w| from the 6 clamped vorticity taps, and the
 // velY Laplacian (only evaluated when visc > 0).

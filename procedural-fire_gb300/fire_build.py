@@ -28,6 +28,7 @@ SOURCES = {
     "fire_poisson.cu": [],
     "fire_sparks.cu": [],
     "fire_volume.cu": [],
+    "fire_adjoint.cu": [],
     "fire_blackbody.cpp": [],
     "fire_scene.cpp": [],
     "fire_timeline.cpp": [],

@@ -154,6 +154,17 @@ _SIGS = {
     "fire_poisson_residual": (_ip, [_vp, _vp, _vp, _vp, ctypes.POINTER(_dp)]),
     "fire_poisson_make_rhs": (_ip, [_vp, _vp, ctypes.c_uint, _ip, _fp, _vp]),
     "fire_poisson_sources": (_ip, [ctypes.c_uint, _ip, _vp, _vp]),
+    "fire_adjoint_create": (_ip, [_vp, _ip, _ip, ctypes.POINTER(_vp)]),
+    "fire_adjoint_destroy": (_ip, [_vp]),
+    "fire_adjoint_forward": (_ip, [_vp, _fp, _vp]),
+    "fire_adjoint_loss": (_ip, [_vp, _vp, ctypes.POINTER(_dp)]),
+    "fire_adjoint_seed": (_ip, [_vp, _vp, _vp, _vp]),
+    "fire_adjoint_backward": (_ip, [_vp, _vp]),
+    "fire_adjoint_grad_spots": (_ip, [_vp, _vp, _ip]),
+    "fire_adjoint_io": (_ip, [_vp, _ip, _vp, ctypes.c_size_t, _ip]),
+    "fire_adjoint_clear": (_ip, [_vp]),
+    "fire_adjoint_stage": (_ip, [_vp, _ip, _fp, _ip, _vp]),
+    "fire_adjoint_timing": (_ip, [_vp, ctypes.POINTER(_fp), ctypes.POINTER(_fp)]),
     "fire_device_ok": (_ip, [_ip]),
     "fire_version": (ctypes.c_char_p, []),
 }
@@ -585,6 +596,123 @@ class Volume:
 
     def lights(self) -> np.ndarray:
         return self._get(2, (8, 8))
+
+
+# ---------------------------------------------------------------------------------------------------
+# Discrete adjoint of the step over checkpointed rollouts (reverse-mode derivatives; no counterpart in
+# the reference).
+ADJ_BUFFERS = {"vel": 0, "S": 1, "S2": 2, "velX": 3, "SX": 4, "S2X": 5, "velY": 6, "SY": 7, "S2Y": 8,
+               "F": 9, "W": 10, "G": 11, "p": 12, "b": 13}
+
+
+class Adjoint:
+    """Reverse-mode derivatives of `n_steps` steps of `sim`, keeping the state every `checkpoint_every`
+    steps.  forward() runs the rollout from the simulation's current state (leaving it in the final state);
+    loss() or seed() sets the final-state cotangents; backward() leaves the initial-state cotangents in
+    get("vel" / "S" / "S2") and the spot-flux gradients in grad_spots()."""
+
+    def __init__(self, sim: "FireSim", n_steps: int, checkpoint_every: int = 10):
+        self._lib = load_library()
+        self.sim = sim
+        self.n_steps = int(n_steps)
+        h = ctypes.c_void_p()
+        rc = self._lib.fire_adjoint_create(sim._h, self.n_steps, int(checkpoint_every), ctypes.byref(h))
+        if rc:
+            raise FireError(rc, "fire_adjoint_create")
+        self._h = h
+
+    def _check(self, rc: int, what: str):
+        self.sim._check(rc, what)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            self._lib.fire_adjoint_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, dt: float, stream=None):
+        self._check(self._lib.fire_adjoint_forward(self._h, float(dt), _stream_handle(stream)), "fire_adjoint_forward")
+
+    def loss(self, target_S: np.ndarray) -> float:
+        t = np.ascontiguousarray(target_S, np.float32)
+        out = ctypes.c_double()
+        self._check(self._lib.fire_adjoint_loss(self._h, _ptr(t), ctypes.byref(out)), "fire_adjoint_loss")
+        return out.value
+
+    def seed(self, vel=None, S=None, S2=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (vel, S, S2)]
+        self._check(self._lib.fire_adjoint_seed(self._h, *[None if a is None else _ptr(a) for a in arrs]), "fire_adjoint_seed")
+
+    def backward(self, stream=None):
+        self._check(self._lib.fire_adjoint_backward(self._h, _stream_handle(stream)), "fire_adjoint_backward")
+
+    def grad_spots(self, n: int) -> np.ndarray:
+        out = np.zeros(int(n), np.float64)
+        self._check(self._lib.fire_adjoint_grad_spots(self._h, _ptr(out), int(n)), "fire_adjoint_grad_spots")
+        return out
+
+    def _shape(self, name: str):
+        nx, ny, nz = self.sim.res
+        return (nz, ny, nx) + (() if ADJ_BUFFERS[name] >= 12 else (4,))
+
+    def get(self, name: str) -> np.ndarray:
+        out = np.zeros(self._shape(name), np.float32)
+        self._check(self._lib.fire_adjoint_io(self._h, ADJ_BUFFERS[name], _ptr(out), out.nbytes, 0), f"adjoint get {name}")
+        return out
+
+    def put(self, name: str, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, np.float32).reshape(self._shape(name))
+        self._check(self._lib.fire_adjoint_io(self._h, ADJ_BUFFERS[name], _ptr(a), a.nbytes, 1), f"adjoint put {name}")
+
+    def clear(self):
+        self._check(self._lib.fire_adjoint_clear(self._h), "fire_adjoint_clear")
+
+    def stage(self, name: str, dt: float, arg: int = 0, stream=None):
+        self._check(self._lib.fire_adjoint_stage(self._h, STAGES[name], float(dt), int(arg), _stream_handle(stream)),
+                    f"fire_adjoint_stage {name}")
+
+    def timing(self):
+        f, b = ctypes.c_float(), ctypes.c_float()
+        self._check(self._lib.fire_adjoint_timing(self._h, ctypes.byref(f), ctypes.byref(b)), "fire_adjoint_timing")
+        return f.value, b.value
+
+
+def rollout_function():
+    """A torch.autograd.Function over an Adjoint:  FireRollout.apply(adj, dt, spots, vel0, S0, S2_0, fluxes)
+    sets the simulation's state and spot fluxes (spots: (n, 5) records whose flux column is replaced by
+    `fluxes`), runs the rollout and returns the final (vel, S, S2); its backward runs the reverse sweep and
+    returns the gradients of vel0, S0, S2_0 and the fluxes.  Tensors live on the host (float32 fields,
+    float64 fluxes); the rollout itself runs on the device through the C ABI."""
+    import torch
+
+    class FireRollout(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, adj, dt, spots, vel0, S0, S2_0, fluxes):
+            sim = adj.sim
+            sp = np.array(spots, np.float32).reshape(-1, 5)
+            sp[:, 4] = fluxes.detach().cpu().numpy().astype(np.float32)
+            sim.set_spots(sp)
+            for name, a in (("vel", vel0), ("S", S0), ("S2", S2_0)):
+                sim.upload(name, a.detach().cpu().numpy())
+            adj.forward(dt)
+            sim.sync()
+            ctx.adj, ctx.n = adj, len(sp)
+            return tuple(torch.from_numpy(sim.download(n).astype(np.float32)) for n in ("vel", "S", "S2"))
+
+        @staticmethod
+        def backward(ctx, gvel, gS, gS2):
+            adj = ctx.adj
+            adj.seed(*[None if g is None else g.detach().cpu().numpy() for g in (gvel, gS, gS2)])
+            adj.backward()
+            grads = [torch.from_numpy(adj.get(n)) for n in ("vel", "S", "S2")]
+            return (None, None, None, *grads, torch.from_numpy(adj.grad_spots(ctx.n)))
+
+    return FireRollout
 
 
 # ---------------------------------------------------------------------------------------------------
