@@ -310,7 +310,7 @@ def run_ensemble(dev: int, steps: int = 20):
     ens = F.Ensemble(members, vcycles=E["vcycles"], device=dev)
     for s, m in zip(ens.members, members):
         _ensemble_configure(s, m, F)
-    ens.step(E["dt"], E["preroll"], stream=st.cuda_stream)
+    ens.step(E["dt"], E["preroll"], stream=st.cuda_stream)   # the autotuner runs on step 8 of these
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
@@ -318,6 +318,14 @@ def run_ensemble(dev: int, steps: int = 20):
     e1.record(st)
     torch.cuda.synchronize(dev)
     ms_batched = e0.elapsed_time(e1) / steps
+    tuned = ens.tiles()
+    ens.set_tiles([0, 0, 0, 0, 0])   # the same ensemble with the untuned (per-simulation) tiles
+    ens.step(E["dt"], 2, stream=st.cuda_stream)
+    e0.record(st)
+    ens.step(E["dt"], steps, stream=st.cuda_stream)
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms_untuned = e0.elapsed_time(e1) / steps
     ens.close()
     sims = []
     for m in members:
@@ -340,7 +348,12 @@ def run_ensemble(dev: int, steps: int = 20):
             "ms_per_step_batched": ms_batched, "ms_per_step_one_at_a_time": ms_single,
             "gcell_updates_per_s_batched": cells / (ms_batched * 1e-3) / 1e9,
             "gcell_updates_per_s_one_at_a_time": cells / (ms_single * 1e-3) / 1e9,
-            "speedup": ms_single / ms_batched}
+            "speedup": ms_single / ms_batched,
+            "tiles": {"stages": ["adv1", "adv2", "forces", "div", "project"],
+                      "chosen": tuned[0].tolist() if tuned else None,
+                      "candidate_ms": tuned[1].round(5).tolist() if tuned else None,
+                      "cell_tiles": ["32x4x2", "32x8x1", "32x2x4", "64x4x1"], "forces_depths": [16, 8, 32],
+                      "ms_per_step_untuned_tiles": ms_untuned}}
 
 
 # Inverse source fit through the discrete adjoint: 64x128x64 cells at 1 cm, dt = 1/120, 120 steps from rest,

@@ -266,10 +266,22 @@ int fire_ensemble_create(const FireConfig* cfgs, int n, FireEnsemble** out);
 int fire_ensemble_destroy(FireEnsemble* e);
 int fire_ensemble_size(FireEnsemble* e);
 int fire_ensemble_sim(FireEnsemble* e, int index, FireSim** out);
-/* n_steps steps of dt seconds for every member, asynchronous on `stream`.                              */
+/* n_steps steps of dt seconds for every member, asynchronous on `stream`.  Step number `at_step` of
+ * fire_ensemble_set_autotune (default 8, once the fires have developed) is the tuning step: it runs
+ * eagerly, times every tile candidate of every batched stage on the members' current state and keeps the
+ * fastest (the call waits for those timings); the step's results are those of any other step.  Steps
+ * before it use tile 0 everywhere.                                                                      */
 int fire_ensemble_step(FireEnsemble* e, float dt, int n_steps, void* stream);
 int fire_ensemble_sync(FireEnsemble* e);
 const char* fire_ensemble_last_error(FireEnsemble* e);
+/* Tile candidates of the batched stages (adv1, adv2, forces, div, project): cell tiles 0-3 (32x4x2, 32x8x1,
+ * 32x2x4, 64x4x1 threads) for the per-cell stages, z-march depths 0-2 (16, 8, 32 planes) for forces.
+ * fire_ensemble_tiles reports the chosen ones (FIRE_ERR_STATE before the tuning step) and, if ms is not
+ * NULL, the measured mean launch time of each candidate (5 x 4 floats, ms; unused entries 0).          */
+#define FIRE_ENSEMBLE_STAGES 5
+int fire_ensemble_set_autotune(FireEnsemble* e, int at_step);   /* -1: no tuning; re-arms a new tuning */
+int fire_ensemble_set_tiles(FireEnsemble* e, const int* tiles);
+int fire_ensemble_tiles(FireEnsemble* e, int* tiles, float* ms);
 
 /* ---- sparks (src/sparks.js) ---------------------------------------------------------------------
  * Burning sparks carried by a simulation's velocity field: the particle update of Sparks.step

@@ -861,6 +861,7 @@ int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream) {
 // launch per tail form; the whole step is one CUDA graph.  Members are ordinary FireSim handles (created
 // and owned by the ensemble) so their parameters, spots, events, fields and diagnostics use the FireSim
 // API; their parameter blocks are staged into one contiguous device array and copied with one copy.
+constexpr int ENS_STAGES = 5;   // adv1, adv2, forces, div, project
 struct FireEnsemble {
   int device = 0;
   std::vector<FireSim*> sims;
@@ -876,6 +877,12 @@ struct FireEnsemble {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   long long steps = 0;
+  // tile candidate per batched stage (adv1, adv2, forces, div, project), chosen by timing every candidate
+  // on the first step (autotune) or set by the caller
+  int tiles[ENS_STAGES] = {0, 0, 0, 0, 0};
+  float tileMs[ENS_STAGES][CELL_TILES] = {};
+  int tuneAt = 8;        // the step index that runs the tuning (-1: never)
+  bool tuned = false;
   std::string err;
 };
 
@@ -903,51 +910,112 @@ int ens_err(FireEnsemble* e, int code, const char* msg) {
 
 // Records one ensemble step (src/sim.js:633-644 for every member): adv1, adv2, curl + forces, div,
 // `vcycles` V(2,2) cycles, project.
-int record_ensemble_step(FireEnsemble* e, cudaStream_t st) {
-  const int n = (int)e->sims.size();
+// Launch descriptions of one ensemble step: the members' stage pointers, one BatchMap per tile candidate,
+// and the multigrid's per-level maps and level tables.
+struct EnsCtx {
   StepBatch SB;
-  std::memset(&SB, 0, sizeof SB);
-  BatchMap cellMap = map_empty(), forcesMap = map_empty();
+  BatchMap cell[CELL_TILES], forces[FORCES_TILES];
   int depth = 0;
+  std::vector<BatchMap> smoothMap, coarseMap;
+  std::vector<LevelBatch> LB;
+};
+void ens_context(FireEnsemble* e, EnsCtx& c) {
+  const int n = (int)e->sims.size();
+  std::memset(&c.SB, 0, sizeof c.SB);
+  for (auto& m : c.cell) m = map_empty();
+  for (auto& m : c.forces) m = map_empty();
+  c.depth = 0;
   for (int i = 0; i < n; ++i) {
     FireSim* s = e->sims[i];
-    SB.s[i] = StepInst{e->dBlocks + (size_t)i * BLOCK_FLOATS, s->f, s->d, s->levels[0].b, s->levels[0].p};
-    map_add(cellMap, i, step_grid(s->d));
-    map_add(forcesMap, i, forces_grid(s->d));
-    depth = std::max(depth, std::min(s->tailFirst, (int)s->levels.size() - 1));
+    c.SB.s[i] = StepInst{e->dBlocks + (size_t)i * BLOCK_FLOATS, s->f, s->d, s->levels[0].b, s->levels[0].p};
+    for (int v = 0; v < CELL_TILES; ++v) map_add(c.cell[v], i, step_grid(s->d, v));
+    for (int v = 0; v < FORCES_TILES; ++v) map_add(c.forces[v], i, forces_grid(s->d, v));
+    c.depth = std::max(c.depth, std::min(s->tailFirst, (int)s->levels.size() - 1));
   }
   // per level: the members that have it outside their tail, and every member's level l and l + 1
-  std::vector<BatchMap> smoothMap(depth, map_empty()), coarseMap(depth, map_empty());
-  std::vector<LevelBatch> LB(depth + 1);
-  for (int l = 0; l <= depth; ++l) std::memset(&LB[l], 0, sizeof(LevelBatch));
+  c.smoothMap.assign(c.depth, map_empty());
+  c.coarseMap.assign(c.depth, map_empty());
+  c.LB.assign(c.depth + 1, LevelBatch{});
+  for (int l = 0; l <= c.depth; ++l) std::memset(&c.LB[l], 0, sizeof(LevelBatch));
   for (int i = 0; i < n; ++i) {
     FireSim* s = e->sims[i];
     const int top = std::min(s->tailFirst, (int)s->levels.size() - 1);
-    for (int l = 0; l <= depth && l < (int)s->levels.size(); ++l) LB[l].l[i] = s->levels[l];
+    for (int l = 0; l <= c.depth && l < (int)s->levels.size(); ++l) c.LB[l].l[i] = s->levels[l];
     for (int l = 0; l < top; ++l) {
-      map_add(smoothMap[l], i, smooth_grid(s->levels[l]));
-      map_add(coarseMap[l], i, coarse_grid(s->levels[l + 1]));
+      map_add(c.smoothMap[l], i, smooth_grid(s->levels[l]));
+      map_add(c.coarseMap[l], i, coarse_grid(s->levels[l + 1]));
     }
   }
+}
+void ens_stage(FireEnsemble* e, const EnsCtx& c, int stage, int tile, cudaStream_t st) {
+  switch (stage) {
+    case 0: launch_adv1_batch(c.cell[tile], c.SB, tile, st); break;
+    case 1: launch_adv2_batch(c.cell[tile], c.SB, tile, st); break;
+    case 2: launch_forces_batch(c.forces[tile], c.SB, e->sims[0]->noise, e->sims[0]->curl, tile, st); break;
+    case 3: launch_div_batch(c.cell[tile], c.SB, tile, st); break;
+    default: launch_project_batch(c.cell[tile], c.SB, tile, st); break;
+  }
+}
+void ens_mg(FireEnsemble* e, const EnsCtx& c, cudaStream_t st) {
   const int V = e->sims[0]->vcycles;
-  launch_adv1_batch(cellMap, SB, st);
-  launch_adv2_batch(cellMap, SB, st);
-  launch_forces_batch(forcesMap, SB, e->sims[0]->noise, e->sims[0]->curl, st);
-  launch_div_batch(cellMap, SB, st);
-  for (int c = 0; c < V; ++c) {
-    for (int l = 0; l < depth; ++l) {
-      for (int k = 0; k < 2; ++k) { launch_smooth_batch(smoothMap[l], LB[l], 0, st); launch_smooth_batch(smoothMap[l], LB[l], 1, st); }
-      launch_restrict_batch(coarseMap[l], LB[l], LB[l + 1], st);
+  for (int cy = 0; cy < V; ++cy) {
+    for (int l = 0; l < c.depth; ++l) {
+      for (int k = 0; k < 2; ++k) { launch_smooth_batch(c.smoothMap[l], c.LB[l], 0, st); launch_smooth_batch(c.smoothMap[l], c.LB[l], 1, st); }
+      launch_restrict_batch(c.coarseMap[l], c.LB[l], c.LB[l + 1], st);
     }
     for (int kind = 0; kind < 2; ++kind)
       launch_tail_batch(kind, e->dTail[kind], e->tailCount[kind], e->tailSmem[kind], 2, 2, e->dErr, st);
-    for (int l = depth - 1; l >= 0; --l) {
-      launch_prolong_batch(coarseMap[l], LB[l], LB[l + 1], st);
-      for (int k = 0; k < 2; ++k) { launch_smooth_batch(smoothMap[l], LB[l], 0, st); launch_smooth_batch(smoothMap[l], LB[l], 1, st); }
+    for (int l = c.depth - 1; l >= 0; --l) {
+      launch_prolong_batch(c.coarseMap[l], c.LB[l], c.LB[l + 1], st);
+      for (int k = 0; k < 2; ++k) { launch_smooth_batch(c.smoothMap[l], c.LB[l], 0, st); launch_smooth_batch(c.smoothMap[l], c.LB[l], 1, st); }
     }
   }
-  launch_project_batch(cellMap, SB, st);
+}
+
+int record_ensemble_step(FireEnsemble* e, cudaStream_t st) {
+  EnsCtx c;
+  ens_context(e, c);
+  for (int s = 0; s < 4; ++s) ens_stage(e, c, s, e->tiles[s], st);
+  ens_mg(e, c, st);
+  ens_stage(e, c, 4, e->tiles[4], st);
   return cudaGetLastError() == cudaSuccess ? FIRE_OK : ens_err(e, FIRE_ERR_CUDA, "ensemble step launch failed");
+}
+
+// The autotuner: runs one step eagerly, timing every tile candidate of every batched stage (3 launches each,
+// CUDA events, the mean) and keeping the fastest.  Each stage reads only what the previous stages wrote and
+// every candidate computes the same per-cell arithmetic, so running all candidates of a stage back to back
+// leaves exactly the state one step leaves.
+int tune_ensemble(FireEnsemble* e, cudaStream_t st) {
+  EnsCtx c;
+  ens_context(e, c);
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+    if (a) cudaEventDestroy(a);
+    return ens_err(e, FIRE_ERR_CUDA, "autotune: event create failed");
+  }
+  constexpr int R = 3;
+  int rc = FIRE_OK;
+  for (int s = 0; s < ENS_STAGES && !rc; ++s) {
+    if (s == 4) ens_mg(e, c, st);
+    const int count = s == 2 ? FORCES_TILES : CELL_TILES;
+    int best = 0;
+    float bestMs = 1e30f;
+    for (int v = 0; v < count; ++v) {
+      float ms = 0.0f;
+      if (cudaEventRecord(a, st) != cudaSuccess) { rc = FIRE_ERR_CUDA; break; }
+      for (int r = 0; r < R; ++r) ens_stage(e, c, s, v, st);
+      if (cudaEventRecord(b, st) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, a, b) != cudaSuccess) { rc = FIRE_ERR_CUDA; break; }
+      e->tileMs[s][v] = ms / R;
+      if (ms < bestMs) { bestMs = ms; best = v; }
+    }
+    e->tiles[s] = best;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (!rc && cudaGetLastError() != cudaSuccess) rc = FIRE_ERR_CUDA;
+  e->tuned = true;
+  return rc ? ens_err(e, rc, "autotune step failed") : FIRE_OK;
 }
 
 int build_ensemble_graph(FireEnsemble* e) {
@@ -1049,10 +1117,6 @@ int fire_ensemble_step(FireEnsemble* e, float dt, int n_steps, void* stream) {
   if (!e || n_steps < 0 || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
   if (cudaSetDevice(e->device) != cudaSuccess) return FIRE_ERR_CUDA;
   cudaStream_t st = as_stream(stream);
-  if (!e->exec) {
-    const int rc = build_ensemble_graph(e);
-    if (rc) return rc;
-  }
   const int n = (int)e->sims.size();
   for (int step = 0; step < n_steps; ++step) {
     const int k = e->ringPos;
@@ -1071,8 +1135,19 @@ int fire_ensemble_step(FireEnsemble* e, float dt, int n_steps, void* stream) {
       }
     }
     if (cudaMemcpyAsync(e->dBlocks, slot, sizeof(float) * BLOCK_FLOATS * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaEventRecord(e->ringEv[k], st) != cudaSuccess || cudaGraphLaunch(e->exec, st) != cudaSuccess)
+        cudaEventRecord(e->ringEv[k], st) != cudaSuccess)
       return FIRE_ERR_CUDA;
+    if (e->tuneAt >= 0 && !e->tuned && e->steps >= e->tuneAt) {   // eager step that picks the graph's tiles
+      if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+      const int rc = tune_ensemble(e, st);
+      if (rc) return rc;
+    } else {
+      if (!e->exec) {
+        const int rc = build_ensemble_graph(e);
+        if (rc) return rc;
+      }
+      if (cudaGraphLaunch(e->exec, st) != cudaSuccess) return FIRE_ERR_CUDA;
+    }
     for (FireSim* s : e->sims) {                                               // src/sim.js:646-647
       s->time += dt;
       s->frame += 1;
@@ -1081,6 +1156,30 @@ int fire_ensemble_step(FireEnsemble* e, float dt, int n_steps, void* stream) {
     e->steps += 1;
   }
   return FIRE_OK;
+}
+
+int fire_ensemble_set_autotune(FireEnsemble* e, int at_step) {
+  if (!e || at_step < -1) return FIRE_ERR_BAD_ARG;
+  e->tuneAt = at_step;
+  e->tuned = false;
+  return FIRE_OK;
+}
+int fire_ensemble_set_tiles(FireEnsemble* e, const int* tiles) {
+  if (!e || !tiles) return FIRE_ERR_BAD_ARG;
+  for (int s = 0; s < ENS_STAGES; ++s)
+    if (tiles[s] < 0 || tiles[s] >= (s == 2 ? FORCES_TILES : CELL_TILES)) return FIRE_ERR_BAD_ARG;
+  if (cudaSetDevice(e->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return FIRE_ERR_CUDA;
+  std::memcpy(e->tiles, tiles, sizeof e->tiles);
+  e->tuned = true;
+  if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+  if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
+  return FIRE_OK;
+}
+int fire_ensemble_tiles(FireEnsemble* e, int* tiles, float* ms) {
+  if (!e || !tiles) return FIRE_ERR_BAD_ARG;
+  std::memcpy(tiles, e->tiles, sizeof e->tiles);
+  if (ms) std::memcpy(ms, e->tileMs, sizeof e->tileMs);
+  return e->tuned ? FIRE_OK : FIRE_ERR_STATE;
 }
 
 int fire_ensemble_sync(FireEnsemble* e) {

@@ -109,14 +109,18 @@ void launch_forces_recompute(const float* P, Fields f, const uint2* noise, const
 cudaError_t step_configure();
 void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st);
 void launch_project(const float* P, Fields f, const float* p0, Dims d, cudaStream_t st);
-// Block grids of the per-cell stages (adv1, adv2, div, project) and of the tiled forces stage.
-dim3 step_grid(Dims d);
-dim3 forces_grid(Dims d);
-void launch_adv1_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st);
-void launch_adv2_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st);
-void launch_forces_batch(const BatchMap& m, const StepBatch& I, const uint2* noise, const uint2* curl, cudaStream_t st);
-void launch_div_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st);
-void launch_project_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st);
+// Tile candidates of the batched stages: CELL_TILES cell tiles for adv1, adv2, div and project (0 is the
+// per-simulation kernels' 32x4x2; then 32x8x1, 32x2x4, 64x4x1) and FORCES_TILES z-march depths of the forces
+// tile (16, 8, 32).  Every candidate computes the same per-cell arithmetic.
+constexpr int CELL_TILES = 4, FORCES_TILES = 3;
+// Block grids of the per-cell stages (adv1, adv2, div, project) and of the tiled forces stage, per candidate.
+dim3 step_grid(Dims d, int tile = 0);
+dim3 forces_grid(Dims d, int tile = 0);
+void launch_adv1_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStream_t st);
+void launch_adv2_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStream_t st);
+void launch_forces_batch(const BatchMap& m, const StepBatch& I, const uint2* noise, const uint2* curl, int tile, cudaStream_t st);
+void launch_div_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStream_t st);
+void launch_project_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStream_t st);
 
 // ---- kernel launchers (fire_mg.cu) ----
 void launch_smooth(const MGLevel& L, int color, cudaStream_t st);

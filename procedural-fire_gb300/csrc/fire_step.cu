@@ -3,6 +3,7 @@
 // ranges are given per kernel.  One thread per cell; CTAs cover 32 x 4 x 2 bricks so the gathers of
 // the semi-Lagrangian back-trace and the 7-point stencils hit L1.  Fields are dense float4 arrays,
 // x fastest, so every warp reads and writes 512 contiguous bytes per field.
+#include <type_traits>
 #include "fire_device.cuh"
 #include "fire_launch.cuh"
 
@@ -23,24 +24,30 @@ struct CellId { int i, j, k; bool ok; };
 // successor's launch begin, and locate this thread's cell.
 // `blk` is the CTA's position in the simulation's grid: blockIdx for a per-simulation launch, or the
 // position a batched launch derived from its flat block index (BatchMap).
+// Cell tiles a stage can run with: the per-simulation kernels use Tile0; the batched (ensemble) kernels are
+// instantiated for every CELL_TILES entry and the ensemble's autotuner picks one per stage.
+template <int TX, int TY, int TZ> struct Tile { static constexpr int X = TX, Y = TY, Z = TZ; };
+using Tile0 = Tile<BX, BY, BZ>;
+template <class T = Tile0>
 __device__ __forceinline__ CellId cell_id(Dims d, uint3 blk) {
   pdl_wait();
   pdl_trigger();
   CellId c;
-  c.i = blk.x * BX + threadIdx.x;
-  c.j = blk.y * BY + threadIdx.y;
-  c.k = blk.z * BZ + threadIdx.z;
+  c.i = blk.x * T::X + threadIdx.x;
+  c.j = blk.y * T::Y + threadIdx.y;
+  c.k = blk.z * T::Z + threadIdx.z;
   c.ok = c.i < d.nx && c.j < d.ny && c.k < d.nz;
   return c;
 }
-__device__ __forceinline__ CellId cell_id(Dims d) { return cell_id(d, blockIdx); }
+__device__ __forceinline__ CellId cell_id(Dims d) { return cell_id<Tile0>(d, blockIdx); }
 static dim3 grid_for(Dims d) { return dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, (d.nz + BZ - 1) / BZ); }
 static dim3 block_shape() { return dim3(BX, BY, BZ); }
 
 
 // ---------------- adv1 (src/sim.js:142-157) ----------------
+template <class TileT = Tile0>
 __device__ __forceinline__ void adv1_body(const float* __restrict__ P, const Fields& f, Dims d, uint3 blk) {
-  CellId id = cell_id(d, blk);
+  CellId id = cell_id<TileT>(d, blk);
   if (!id.ok) return;
   const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx);
   const size_t ci = cell(id.i, id.j, id.k, d.nx, d.ny);
@@ -57,8 +64,9 @@ __device__ __forceinline__ void adv1_body(const float* __restrict__ P, const Fie
 }
 
 // ---------------- adv2 (src/sim.js:159-197) ----------------
+template <class TileT = Tile0>
 __device__ __forceinline__ void adv2_body(const float* __restrict__ P, const Fields& f, Dims d, uint3 blk) {
-  CellId id = cell_id(d, blk);
+  CellId id = cell_id<TileT>(d, blk);
   if (!id.ok) return;
   const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx);
   const size_t ci = cell(id.i, id.j, id.k, d.nx, d.ny);
@@ -394,14 +402,15 @@ __device__ __forceinline__ void curl_plane(float4* dst, float4* vbuf, int zlog, 
     dst[t] = make_float4(w.x, w.y, w.z, len3(w));
   }
 }
+template <int ZD = FZ>   // planes one CTA marches through
 __device__ __forceinline__ void forces_tiled_body(const float* __restrict__ P, const Fields& f, const uint2* __restrict__ noiseT,
                                                   const uint2* __restrict__ curlT, Dims d, uint3 blk, float4* fsm) {
   pdl_wait();
   pdl_trigger();
   float4* vbuf = fsm;                    // 5 * VX * VY
   float4* wbuf = fsm + 5 * VX * VY;      // 3 * WX * WY
-  const int x0 = blk.x * FT_X, y0 = blk.y * FT_Y, z0 = blk.z * FZ;
-  const int z1 = min(z0 + FZ, d.nz);
+  const int x0 = blk.x * FT_X, y0 = blk.y * FT_Y, z0 = blk.z * ZD;
+  const int z1 = min(z0 + ZD, d.nz);
   for (int z = z0 - 2; z <= z0 + 2; ++z) load_vplane(vslot(vbuf, z), f.velY, x0, y0, z, d);
   __syncthreads();
   for (int z = z0 - 1; z <= z0 + 1; ++z) curl_plane(wslot(wbuf, z), vbuf, z, x0, y0, d);
@@ -440,9 +449,10 @@ __device__ __forceinline__ void forces_tiled_body(const float* __restrict__ P, c
 constexpr size_t FORCES_TILED_SMEM = sizeof(float4) * (5 * VX * VY + 3 * WX * WY);
 
 // ---------------- divergence minus the expansion target (src/sim.js:399-413) ----------------
+template <class TileT = Tile0>
 __device__ __forceinline__ void div_body(const float* __restrict__ P, const float4* __restrict__ velX, float* __restrict__ b0, Dims d,
                                          uint3 blk) {
-  CellId id = cell_id(d, blk);
+  CellId id = cell_id<TileT>(d, blk);
   if (!id.ok) return;
   const int i = id.i, j = id.j, k = id.k;
   const size_t ci = cell(i, j, k, d.nx, d.ny);
@@ -461,9 +471,10 @@ __device__ __forceinline__ float pr(const float* __restrict__ p, int x, int y, i
   if (y < 0) return me;                                                    // floor: Neumann
   return __ldg(p + cell(x, y, z, d.nx, d.ny));
 }
+template <class TileT = Tile0>
 __device__ __forceinline__ void project_body(const float* __restrict__ P, const float4* __restrict__ velX, const float* __restrict__ p0,
                                              const unsigned char* __restrict__ solid, float4* __restrict__ vel, Dims d, uint3 blk) {
-  CellId id = cell_id(d, blk);
+  CellId id = cell_id<TileT>(d, blk);
   if (!id.ok) return;
   const int i = id.i, j = id.j, k = id.k;
   const size_t ci = cell(i, j, k, d.nx, d.ny);
@@ -501,32 +512,57 @@ __global__ void __launch_bounds__(256) k_project(const float* __restrict__ P, co
 // Each CTA finds its simulation and its position in that simulation's grid from the flat block index
 // (BatchMap), then runs the same body as the per-simulation kernel: the arithmetic, and so the results,
 // are those of stepping each simulation alone.
+template <class T>
 __global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv1_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I) {
   uint3 blk; int i;
   batch_locate(m, blk, i);
-  adv1_body(I.s[i].P, I.s[i].f, I.s[i].d, blk);
+  adv1_body<T>(I.s[i].P, I.s[i].f, I.s[i].d, blk);
 }
+template <class T>
 __global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv2_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I) {
   uint3 blk; int i;
   batch_locate(m, blk, i);
-  adv2_body(I.s[i].P, I.s[i].f, I.s[i].d, blk);
+  adv2_body<T>(I.s[i].P, I.s[i].f, I.s[i].d, blk);
 }
+template <int ZD>
 __global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I,
                                                                                  const uint2* __restrict__ noiseT, const uint2* __restrict__ curlT) {
   extern __shared__ float4 fsm[];
   uint3 blk; int i;
   batch_locate(m, blk, i);
-  forces_tiled_body(I.s[i].P, I.s[i].f, noiseT, curlT, I.s[i].d, blk, fsm);
+  forces_tiled_body<ZD>(I.s[i].P, I.s[i].f, noiseT, curlT, I.s[i].d, blk, fsm);
 }
+template <class T>
 __global__ void __launch_bounds__(256) k_div_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I) {
   uint3 blk; int i;
   batch_locate(m, blk, i);
-  div_body(I.s[i].P, I.s[i].f.velX, I.s[i].b0, I.s[i].d, blk);
+  div_body<T>(I.s[i].P, I.s[i].f.velX, I.s[i].b0, I.s[i].d, blk);
 }
+template <class T>
 __global__ void __launch_bounds__(256) k_project_b(const __grid_constant__ BatchMap m, const __grid_constant__ StepBatch I) {
   uint3 blk; int i;
   batch_locate(m, blk, i);
-  project_body(I.s[i].P, I.s[i].f.velX, I.s[i].p0, I.s[i].f.solid, I.s[i].f.vel, I.s[i].d, blk);
+  project_body<T>(I.s[i].P, I.s[i].f.velX, I.s[i].p0, I.s[i].f.solid, I.s[i].f.vel, I.s[i].d, blk);
+}
+
+// The tile candidates of the batched stages: CELL_TILES cell tiles (256 threads each; x stays 32 or 64 wide
+// for coalescing) and FORCES_TILES z-march depths of the forces tile.
+template <class F> void with_cell_tile(int v, F&& f) {
+  switch (v) {
+    case 1: f(Tile<32, 8, 1>{}); break;
+    case 2: f(Tile<32, 2, 4>{}); break;
+    case 3: f(Tile<64, 4, 1>{}); break;
+    default: f(Tile0{}); break;
+  }
+}
+static_assert(CELL_TILES == 4, "with_cell_tile lists every cell tile");
+constexpr int kForcesDepth[FORCES_TILES] = {FZ, 8, 32};
+template <class F> void with_forces_depth(int v, F&& f) {
+  switch (v) {
+    case 1: f(std::integral_constant<int, 8>{}); break;
+    case 2: f(std::integral_constant<int, 32>{}); break;
+    default: f(std::integral_constant<int, FZ>{}); break;
+  }
 }
 
 // ---------------- launchers ----------------
@@ -542,26 +578,53 @@ void launch_forces_recompute(const float* P, Fields f, const uint2* noise, const
 }
 cudaError_t step_configure() {
   cudaError_t e = cudaFuncSetAttribute(k_forces_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_forces_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
+  for (int v = 0; v < FORCES_TILES && e == cudaSuccess; ++v)
+    with_forces_depth(v, [&](auto z) {
+      e = cudaFuncSetAttribute(k_forces_b<decltype(z)::value>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
+    });
+  return e;
 }
-// Block grids of the batched stages for a simulation of dims d.
-dim3 step_grid(Dims d) { return grid_for(d); }
-dim3 forces_grid(Dims d) { return dim3((d.nx + FT_X - 1) / FT_X, (d.ny + FT_Y - 1) / FT_Y, (d.nz + FZ - 1) / FZ); }
-void launch_adv1_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st) {
-  launch_pdl(k_adv1_b, dim3(m.prefix[m.n]), block_shape(), 0, st, m, I);
+// Block grids of the batched stages for a simulation of dims d with tile candidate `tile`.
+dim3 step_grid(Dims d, int tile) {
+  dim3 g;
+  with_cell_tile(tile, [&](auto t) {
+    using T = decltype(t);
+    g = dim3((d.nx + T::X - 1) / T::X, (d.ny + T::Y - 1) / T::Y, (d.nz + T::Z - 1) / T::Z);
+  });
+  return g;
 }
-void launch_adv2_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st) {
-  launch_pdl(k_adv2_b, dim3(m.prefix[m.n]), block_shape(), 0, st, m, I);
+dim3 forces_grid(Dims d, int tile) {
+  const int zd = kForcesDepth[tile >= 0 && tile < FORCES_TILES ? tile : 0];
+  return dim3((d.nx + FT_X - 1) / FT_X, (d.ny + FT_Y - 1) / FT_Y, (d.nz + zd - 1) / zd);
 }
-void launch_forces_batch(const BatchMap& m, const StepBatch& I, const uint2* noise, const uint2* curl, cudaStream_t st) {
-  launch_pdl(k_forces_b, dim3(m.prefix[m.n]), dim3(FT_X, FT_Y), FORCES_TILED_SMEM, st, m, I, noise, curl);
+void launch_adv1_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStream_t st) {
+  with_cell_tile(tile, [&](auto t) {
+    using T = decltype(t);
+    launch_pdl(k_adv1_b<T>, dim3(m.prefix[m.n]), dim3(T::X, T::Y, T::Z), 0, st, m, I);
+  });
 }
-void launch_div_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st) {
-  launch_pdl(k_div_b, dim3(m.prefix[m.n]), block_shape(), 0, st, m, I);
+void launch_adv2_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStream_t st) {
+  with_cell_tile(tile, [&](auto t) {
+    using T = decltype(t);
+    launch_pdl(k_adv2_b<T>, dim3(m.prefix[m.n]), dim3(T::X, T::Y, T::Z), 0, st, m, I);
+  });
 }
-void launch_project_batch(const BatchMap& m, const StepBatch& I, cudaStream_t st) {
-  launch_pdl(k_project_b, dim3(m.prefix[m.n]), block_shape(), 0, st, m, I);
+void launch_forces_batch(const BatchMap& m, const StepBatch& I, const uint2* noise, const uint2* curl, int tile, cudaStream_t st) {
+  with_forces_depth(tile, [&](auto z) {
+    launch_pdl(k_forces_b<decltype(z)::value>, dim3(m.prefix[m.n]), dim3(FT_X, FT_Y), FORCES_TILED_SMEM, st, m, I, noise, curl);
+  });
+}
+void launch_div_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStream_t st) {
+  with_cell_tile(tile, [&](auto t) {
+    using T = decltype(t);
+    launch_pdl(k_div_b<T>, dim3(m.prefix[m.n]), dim3(T::X, T::Y, T::Z), 0, st, m, I);
+  });
+}
+void launch_project_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStream_t st) {
+  with_cell_tile(tile, [&](auto t) {
+    using T = decltype(t);
+    launch_pdl(k_project_b<T>, dim3(m.prefix[m.n]), dim3(T::X, T::Y, T::Z), 0, st, m, I);
+  });
 }
 void launch_forces_unfused(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
   launch_pdl(k_forces<false>, grid_for(d), block_shape(), 0, st, P, f, noise, curl, d);

@@ -147,6 +147,9 @@ _SIGS = {
     "fire_ensemble_step": (_ip, [_vp, _fp, _ip, _vp]),
     "fire_ensemble_sync": (_ip, [_vp]),
     "fire_ensemble_last_error": (ctypes.c_char_p, [_vp]),
+    "fire_ensemble_set_autotune": (_ip, [_vp, _ip]),
+    "fire_ensemble_set_tiles": (_ip, [_vp, _vp]),
+    "fire_ensemble_tiles": (_ip, [_vp, _vp, _vp]),
     "fire_poisson_create": (_ip, [_vp, _fp, _ip, _ip, ctypes.POINTER(_vp)]),
     "fire_poisson_destroy": (_ip, [_vp]),
     "fire_poisson_solve": (_ip, [_vp, _vp, _vp, _vp, _dp, _ip, _ip, _vp]),
@@ -837,6 +840,26 @@ class Ensemble:
 
     def sync(self):
         self._check(self._lib.fire_ensemble_sync(self._h), "fire_ensemble_sync")
+
+    # stage order of the tile choices: adv1, adv2, forces, div, project
+    def set_autotune(self, at_step: int):
+        """Tune the tiles on step number `at_step` from now on the ensemble's count (-1: never)."""
+        self._check(self._lib.fire_ensemble_set_autotune(self._h, int(at_step)), "fire_ensemble_set_autotune")
+
+    def set_tiles(self, tiles: Sequence[int]):
+        a = np.ascontiguousarray(tiles, np.int32)
+        self._check(self._lib.fire_ensemble_set_tiles(self._h, _ptr(a)), "fire_ensemble_set_tiles")
+
+    def tiles(self):
+        """(chosen tile per stage, measured mean launch ms per stage and candidate (5 x 4)), or None before
+        the tuning step."""
+        a = np.zeros(5, np.int32)
+        ms = np.zeros((5, 4), np.float32)
+        rc = self._lib.fire_ensemble_tiles(self._h, _ptr(a), _ptr(ms))
+        if rc == 6:
+            return None
+        self._check(rc, "fire_ensemble_tiles")
+        return a, ms
 
     def close(self):
         if self._h is not None:

@@ -73,3 +73,39 @@ def test_ensemble_rejects_bad_configs():
         F.Ensemble([dict(res=(32, 64, 32), size=(0.4, 0.8, 0.4))] * 65)
     with pytest.raises(F.FireError):
         F.Ensemble([])
+
+
+def test_tile_candidates_agree_and_autotune_picks_one():
+    """Every tile candidate of the batched stages computes the same per-cell arithmetic: after 10 steps with
+    the default tiles, one more step with any candidate gives the default tiles' fields to FP32 rounding.
+    The autotuner's step gives the same fields as a plain step and reports a valid choice with its timings."""
+    import fire_sim as F
+    members = MEMBERS[:3]
+
+    def run(tiles=None, tune=False):
+        ens = F.Ensemble(members, vcycles=4)
+        ens.set_autotune(-1)
+        for sim, m in zip(ens.members, members):
+            _configure(sim, m)
+        ens.step(DT, 10)
+        if tiles is not None:
+            ens.set_tiles(tiles)
+        if tune:
+            ens.set_autotune(0)
+        ens.step(DT, 1)
+        ens.sync()
+        out = [{n: s.download(n) for n in ("vel", "S", "S2")} for s in ens.members]
+        chosen = ens.tiles()
+        ens.close()
+        return out, chosen
+
+    ref, _ = run()
+    variants = [[v, v, min(v, 2), v, v] for v in range(1, 4)] + [[0, 0, 1, 0, 0], [0, 0, 2, 0, 0]]
+    for tiles in variants + ["tune"]:
+        got, chosen = run(tune=True) if tiles == "tune" else run(tiles)
+        for k in range(len(members)):
+            for n in ("vel", "S", "S2"):
+                assert FC.rel_l2(got[k][n], ref[k][n]) < 1e-5, (tiles, k, n)
+    tiles, ms = chosen
+    assert all(0 <= t < (3 if i == 2 else 4) for i, t in enumerate(tiles))
+    assert (ms[[0, 1, 3, 4]] > 0).all() and (ms[2, :3] > 0).all()
