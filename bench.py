@@ -364,18 +364,24 @@ ADJOINT = dict(name="adjoint-fit-64x128x64", res=(64, 128, 64), size=(0.64, 1.28
                iterations=3)
 
 
-def run_adjoint(dev: int):
-    """Forward and adjoint time per step of the source fit, and a few gradient steps on the fluxes."""
+def run_adjoint(dev: int, steps: int = 0, iterations: int = -1, mg_fixed: int = 0):
+    """Forward and adjoint time per step of the source fit, and a few gradient steps on the fluxes
+    (steps / iterations override the workload's for profiling runs)."""
     import torch
     import fire_sim as F
-    A = ADJOINT
+    A = dict(ADJOINT)
+    if steps > 0:
+        A["steps"] = steps
+    if iterations >= 0:
+        A["iterations"] = iterations
     st = torch.cuda.current_stream(dev)
     spots_a = F.make_spots(A["seed_a"], A["spots"], 1.0, 4.0, A["sigma"], A["radius"])
     spots_b = spots_a.copy()
     spots_b[:, 4] = F.make_spots(A["seed_b"], A["spots"], 1.0, 4.0, A["sigma"], A["radius"])[:, 4]
 
     def make(spots):
-        s = F.FireSim(res=A["res"], size=A["size"], vcycles=4, device=dev, mg_max_cycles=A["mg_max_cycles"], mg_tol=A["mg_tol"])
+        s = F.FireSim(res=A["res"], size=A["size"], vcycles=mg_fixed or 4, device=dev,
+                      mg_max_cycles=0 if mg_fixed else A["mg_max_cycles"], mg_tol=A["mg_tol"])
         s.set_params({"vortEps": 0.3, "turbAmp": 0.2})
         s.set_soot_age(0.02, 0.06)
         s.set_bed_gain(0.0)
@@ -428,7 +434,7 @@ def run_adjoint(dev: int):
     sim.close()
     fwd_ms, bwd_ms = float(np.median(fwd[1:] or fwd)), float(np.median(bwd[1:] or bwd))
     return {"workload": A["name"], "steps": A["steps"], "checkpoint_every": A["checkpoint"],
-            "mg": f"V(2,2) to {A['mg_tol']} rel. residual, max {A['mg_max_cycles']}",
+            "mg": f"{mg_fixed} fixed V(2,2) cycles" if mg_fixed else f"V(2,2) to {A['mg_tol']} rel. residual, max {A['mg_max_cycles']}",
             "ms_per_step_forward_plain": ms_plain, "ms_per_step_forward_taped": fwd_ms,
             "ms_per_step_backward": bwd_ms, "adjoint_over_forward": bwd_ms / ms_plain,
             "backward_includes": "recompute of every segment but the last from its checkpoint, then the reverse steps",
@@ -616,10 +622,21 @@ def main(argv=None):
     ap.add_argument("--no-poisson", action="store_true", help="skip the standalone 256x512x256 pressure-solve timings")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-fire ensemble timings")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint source-fit timings")
+    ap.add_argument("--only", choices=["poisson", "ensemble", "adjoint"],
+                    help="run just one of the side workloads and print its block (profiling aid)")
+    ap.add_argument("--adjoint-steps", type=int, default=0, help="override the adjoint rollout length")
+    ap.add_argument("--adjoint-iters", type=int, default=-1, help="override the number of fit iterations")
     ap.add_argument("--mg-fixed", type=int, default=0,
                     help="profiling aid: N fixed V-cycles per step instead of the residual-driven solve")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
+    if args.only:
+        import torch
+        torch.cuda.init()
+        fn = {"poisson": lambda: run_poisson(0), "ensemble": lambda: run_ensemble(0),
+              "adjoint": lambda: run_adjoint(0, args.adjoint_steps, args.adjoint_iters, args.mg_fixed)}[args.only]
+        print(json.dumps({args.only: fn()}), flush=True)
+        return
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out is not None:
         print(json.dumps(out), flush=True)

@@ -964,9 +964,14 @@ bool tail_fits(const MGLevel* levels, int first, int n, bool coarse64) {
   return first >= 0 && first < n && n - first - tail_dist_levels(levels, first, n) <= TAIL_MAX_LEVELS &&
          tail_smem_bytes(levels, first, n, coarse64) <= TAIL_SMEM_BUDGET;
 }
-int tail_first(const MGLevel* levels, int n, bool coarse64) {
+// The step's V-cycle keeps its tail single-CTA: measured in CUDA graphs on GB300, a level of >= 32k cells
+// costs less as its 10 full-grid launches (~21 us) than inside the cluster tail (the 8-CTA tail from 32x64x32
+// takes 57 us against 21 + 31 us for that level separately plus the single-CTA tail below it).  The
+// standalone solver's tail (FP64 coarsest solve) still gains from the cluster form and asks for it.
+int tail_first(const MGLevel* levels, int n, bool coarse64, bool allow_cluster) {
   int first = n;
-  for (int l = n - 1; l >= 0 && tail_fits(levels, l, n, coarse64); --l) first = l;
+  for (int l = n - 1; l >= 0 && tail_fits(levels, l, n, coarse64) && (allow_cluster || tail_dist_levels(levels, l, n) == 0); --l)
+    first = l;
   return first;
 }
 // Levels [first, n) as a TailLevels block whose first level's p starts `off` floats into shared memory.

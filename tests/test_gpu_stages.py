@@ -154,9 +154,8 @@ def test_rb_sweeps(level, sweeps):
                                  (64, 128, 64)])
 def test_mg_vcycle_tail_shapes(res):
     """V-cycles whose shared-memory tail has only warp-sized levels (8x16x8), only CTA-sized levels (12x400x12:
-    coarsest 6x200x6), an odd coarsest level (20x30x20 -> 10x15x10), and cluster tails: one distributed
-    level over gathered levels (16x32x16), two distributed levels (32x64x32; 48x32x32 with nx not a power of
-    two), and two distributed levels below a launch-per-phase level (64x128x64)."""
+    coarsest 6x200x6), an odd coarsest level (20x30x20 -> 10x15x10), and launch-per-phase levels above the
+    tail (16x32x16 up to 64x128x64; 48x32x32 with nx not a power of two)."""
     cfg = dict(res=res, size=(0.02 * res[0], 0.02 * res[1], 0.02 * res[2]), dt=0.01, vcycles=2)
     sim, orc = FC.make_pair(cfg)
     rng = np.random.default_rng(sum(res))
@@ -171,6 +170,27 @@ def test_mg_vcycle_tail_shapes(res):
         orc.vcycle()
     sim.sync()
     FC.compare(sim.level(0, "p"), orc.get_level(0, "p"), 1e-4, 1e-5, 0, what=f"vcycle {res}")
+
+
+@pytest.mark.parametrize("res", [(16, 32, 16), (32, 64, 32), (48, 32, 32)])
+def test_mg_cluster_tail_whole_cycle(res):
+    """The 8-CTA cluster tail run over the whole hierarchy (fire_sim_run_mg from level 0): one distributed level
+    over gathered levels (16x32x16), two distributed levels (32x64x32; 48x32x32 with nx not a power of two)
+    equal the oracle's V-cycle."""
+    cfg = dict(res=res, size=(0.02 * res[0], 0.02 * res[1], 0.02 * res[2]), dt=0.01, vcycles=2)
+    sim, orc = FC.make_pair(cfg)
+    rng = np.random.default_rng(sum(res) + 1)
+    for l, L in enumerate(sim.levels):
+        nx, ny, nz = L["dims"]
+        for w, scale in (("p", 0.01), ("b", 50.0)):
+            a = (FC.smooth_noise((nz, ny, nx), rng, 1) * scale).astype(np.float32)
+            sim.set_level(l, w, a)
+            orc.put_level(l, w, a)
+    for _ in range(2):
+        sim.run_mg("tail", 0)
+        orc.vcycle()
+    sim.sync()
+    FC.compare(sim.level(0, "p"), orc.get_level(0, "p"), 1e-4, 1e-5, 0, what=f"cluster tail {res}")
 
 
 def test_mg_vcycle_parity():
