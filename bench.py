@@ -40,7 +40,7 @@ for p in (PKG, ROOT / "oracle"):
 WORKLOAD = dict(
     name="fire-step-128x256x128-fp32", res=(128, 256, 128), size=(0.64, 1.28, 0.64), dt=1.0 / 240.0,
     spots=6, spot_seed=2, flux=(1.0, 4.0), sigma=0.02, radius=0.2, vortEps=0.3, turbAmp=0.2,
-    soot_age=(0.02, 0.06), mg_tol=1e-5, mg_max_cycles=8, preroll=60,
+    soot_age=(0.02, 0.06), mg_tol=1e-5, mg_max_cycles=8, mg_omega=1.2, preroll=60,
 )
 METRIC = "steps/s, full-physics fire step at 128x256x128 (FP32)"
 
@@ -167,6 +167,8 @@ def make_sim(F, device: int, mg_fixed: int = 0):
     sim.set_soot_age(*W["soot_age"])
     sim.set_bed_gain(0.0)
     sim.set_spots(F.make_spots(W["spot_seed"], W["spots"], W["flux"][0], W["flux"][1], W["sigma"], W["radius"]))
+    if not mg_fixed:
+        sim.set_mg_omega(W["mg_omega"])   # over-relaxed fine-level smoothing: 3 cycles to 1e-5 instead of ~4.5
     return sim
 
 
@@ -361,7 +363,7 @@ def run_ensemble(dev: int, steps: int = 20):
 # from seed-B fluxes at the same positions; checkpoints every 10 steps.
 ADJOINT = dict(name="adjoint-fit-64x128x64", res=(64, 128, 64), size=(0.64, 1.28, 0.64), dt=1.0 / 120.0, steps=120,
                checkpoint=10, spots=8, seed_a=11, seed_b=12, sigma=0.02, radius=0.12, mg_tol=1e-5, mg_max_cycles=8,
-               iterations=3)
+               mg_omega=1.2, iterations=3)
 
 
 def run_adjoint(dev: int, steps: int = 0, iterations: int = -1, mg_fixed: int = 0):
@@ -386,6 +388,8 @@ def run_adjoint(dev: int, steps: int = 0, iterations: int = -1, mg_fixed: int = 
         s.set_soot_age(0.02, 0.06)
         s.set_bed_gain(0.0)
         s.set_spots(spots)
+        if not mg_fixed:
+            s.set_mg_omega(A["mg_omega"])
         return s
 
     # the target, and the plain forward's time per step (the step graph, same solve)
@@ -417,9 +421,10 @@ def run_adjoint(dev: int, steps: int = 0, iterations: int = -1, mg_fixed: int = 
         hist.append({"loss": loss, "flux_err_gps": float(np.abs(flux - spots_a[:, 4]).max()), "grad_norm": float(np.linalg.norm(g))})
         if it == A["iterations"]:
             break
-        # a projected gradient step on the fluxes along -g, backtracking from 0.5 g/s until the loss drops
-        step = 0.5
-        for _ in range(4):
+        # a projected gradient step on the fluxes along -g, backtracking from 0.2 g/s until the loss drops
+        # (the rollout is chaotic: the gradient describes the loss only over small flux changes)
+        step = 0.2
+        for _ in range(6):
             trial = np.clip(flux - step * g / max(np.linalg.norm(g), 1e-30), 0.0, 8.0)
             sim.reset()
             sp = spots_b.copy()
@@ -427,14 +432,15 @@ def run_adjoint(dev: int, steps: int = 0, iterations: int = -1, mg_fixed: int = 
             sim.set_spots(sp)
             adj.forward(A["dt"], stream=st.cuda_stream)
             if adj.loss(target) < loss:
+                flux = trial
                 break
-            step *= 0.5
-        flux = trial
+            step *= 0.25
     adj.close()
     sim.close()
     fwd_ms, bwd_ms = float(np.median(fwd[1:] or fwd)), float(np.median(bwd[1:] or bwd))
     return {"workload": A["name"], "steps": A["steps"], "checkpoint_every": A["checkpoint"],
-            "mg": f"{mg_fixed} fixed V(2,2) cycles" if mg_fixed else f"V(2,2) to {A['mg_tol']} rel. residual, max {A['mg_max_cycles']}",
+            "mg": f"{mg_fixed} fixed V(2,2) cycles" if mg_fixed else
+                  f"V(2,2), omega {A['mg_omega']}, to {A['mg_tol']} rel. residual, max {A['mg_max_cycles']}",
             "ms_per_step_forward_plain": ms_plain, "ms_per_step_forward_taped": fwd_ms,
             "ms_per_step_backward": bwd_ms, "adjoint_over_forward": bwd_ms / ms_plain,
             "backward_includes": "recompute of every segment but the last from its checkpoint, then the reverse steps",
@@ -536,7 +542,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": W["name"], "grid": list(W["res"]), "cell_m": 0.005, "dt": W["dt"],
-                   "spots": W["spots"], "mg": f"V(2,2) to {W['mg_tol']} rel. residual, max {W['mg_max_cycles']}",
+                   "spots": W["spots"], "mg": f"V(2,2), fine-level smoothing over-relaxed (omega {W['mg_omega']}), to {W['mg_tol']} rel. residual, max {W['mg_max_cycles']}",
                    "mean_vcycles_per_step": cycles, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (fields ~740 MB vs 129 MB L2)"},
         "gcell_updates_per_s": value * cells / 1e9,
@@ -603,7 +609,7 @@ def run_reference(args):
         "ms_per_step": 1e3 * el / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic", "impl": "reference",
         "config": {"workload": W["name"], "grid": list(W["res"]), "cell_m": 0.005, "dt": W["dt"],
-                   "spots": W["spots"], "mg": f"V(2,2) to {W['mg_tol']} rel. residual, max {W['mg_max_cycles']}"},
+                   "spots": W["spots"], "mg": f"the reference's Gauss-Seidel V(2,2) to {W['mg_tol']} rel. residual, max {W['mg_max_cycles']}"},
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
                          "sample": f"{k} timed steps after {max(args.warmup, 1)} warm-up steps from rest "
                                    f"(the reference's WebGPU step needs a browser GPU stack, unavailable on this box)"},

@@ -565,6 +565,13 @@ int fire_sim_set_bed_gain(FireSim* sim, float gain) {
   sim->geoReady = false;
   return FIRE_OK;
 }
+int fire_sim_set_mg_omega(FireSim* sim, float omega) {
+  if (!sim || !(omega > 0.0f && omega < 2.0f)) return FIRE_ERR_BAD_ARG;
+  for (MGLevel& L : sim->levels) L.omega = omega;
+  drop_graph(sim);   // the smoother launches carry omega as an argument
+  return FIRE_OK;
+}
+
 int fire_sim_set_spots(FireSim* sim, const float* spots, int n) {
   if (!sim || n < 0 || n > MAX_SPOTS || (n > 0 && !spots)) return FIRE_ERR_BAD_ARG;
   for (int i = 0; i < n; ++i)

@@ -54,6 +54,7 @@ struct MGLevel {
   float h;
   float* p;
   float* b;
+  float omega = 1.0f;   // over-relaxation of the launch-per-sweep smoother (1: Gauss-Seidel, the reference's)
 };
 
 // ---- batched launches over many independent simulations ----

@@ -47,8 +47,10 @@ __device__ __forceinline__ float rb_update(const float* p, const float* b, int x
 #define FIRE_SMOOTH_Z 2
 #endif
 constexpr int SMZ = FIRE_SMOOTH_Z;
+// omega != 1 over-relaxes the update (p + omega (p_gs - p)); omega == 1 is the reference's Gauss-Seidel
+// update bit for bit.
 __device__ __forceinline__ void smooth_body(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz, float h, int color,
-                                            uint3 blk) {
+                                            uint3 blk, float omega = 1.0f) {
   pdl_wait();
   pdl_trigger();
   const int gx = blk.x * GX + threadIdx.x, y = blk.y * GY + threadIdx.y;
@@ -60,7 +62,13 @@ __device__ __forceinline__ void smooth_body(float* __restrict__ p, const float* 
   for (int k = 0; k < SMZ; ++k) {   // all reads first (a colour's cells never read each other) ...
     const int z = zb + k;
     const int x = gx * 2 + ((y + z + color) & 1);
-    if (z < nz && x < nx) v[k] = rb_update(p, b, x, y, z, nx, ny, nz, h2);
+    if (z < nz && x < nx) {
+      v[k] = rb_update(p, b, x, y, z, nx, ny, nz, h2);
+      if (omega != 1.0f) {
+        const float old = p[x + nx * (y + ny * z)];
+        v[k] = fmaf(omega, v[k] - old, old);
+      }
+    }
   }
 #pragma unroll
   for (int k = 0; k < SMZ; ++k) {   // ... then the writes
@@ -169,8 +177,8 @@ __device__ __forceinline__ void prolong_body(float* __restrict__ p, const float*
 // Per-level kernels of one simulation, and their batched forms over many simulations (one grid; each CTA
 // finds its simulation's level from the BatchMap and runs the same body).
 __global__ void __launch_bounds__(GX * GY * GZ) k_smooth(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz, float h,
-                                                         int color) {
-  smooth_body(p, b, nx, ny, nz, h, color, blockIdx);
+                                                         int color, float omega) {
+  smooth_body(p, b, nx, ny, nz, h, color, blockIdx, omega);
 }
 __global__ void __launch_bounds__(GX * GY * GZ) k_restrict(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
                                                            float h, float* __restrict__ bc, float* __restrict__ pc) {
@@ -183,7 +191,7 @@ __global__ void __launch_bounds__(GX * GY * GZ) k_smooth_b(const __grid_constant
   uint3 blk; int i;
   batch_locate(m, blk, i);
   const MGLevel& v = L.l[i];
-  smooth_body(v.p, v.b, v.nx, v.ny, v.nz, v.h, color, blk);
+  smooth_body(v.p, v.b, v.nx, v.ny, v.nz, v.h, color, blk, v.omega);
 }
 __global__ void __launch_bounds__(GX * GY * GZ) k_restrict_b(const __grid_constant__ BatchMap m, const __grid_constant__ LevelBatch F,
                                                              const __grid_constant__ LevelBatch C) {
@@ -925,7 +933,7 @@ static const dim3 kBlock(GX, GY, GZ);
 
 void launch_smooth(const MGLevel& L, int color, cudaStream_t st) {
   launch_pdl(k_smooth, grid3((L.nx + 1) >> 1, L.ny, (L.nz + SMZ - 1) / SMZ), kBlock, 0, st, L.p, (const float*)L.b, L.nx, L.ny,
-             L.nz, L.h, color);
+             L.nz, L.h, color, L.omega);
 }
 void launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
   launch_pdl(k_restrict, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (const float*)F.p, (const float*)F.b, F.nx, F.ny, F.nz, F.h, C.b, C.p);

@@ -168,6 +168,7 @@ _SIGS = {
     "fire_adjoint_clear": (_ip, [_vp]),
     "fire_adjoint_stage": (_ip, [_vp, _ip, _fp, _ip, _vp]),
     "fire_adjoint_timing": (_ip, [_vp, ctypes.POINTER(_fp), ctypes.POINTER(_fp)]),
+    "fire_sim_set_mg_omega": (_ip, [_vp, _fp]),
     "fire_device_ok": (_ip, [_ip]),
     "fire_version": (ctypes.c_char_p, []),
 }
@@ -352,6 +353,10 @@ class FireSim:
 
     def set_bed_gain(self, gain: float):
         self._check(self._lib.fire_sim_set_bed_gain(self._h, gain), "set_bed_gain")
+
+    def set_mg_omega(self, omega: float):
+        """Over-relaxation of the V-cycle's fine-level smoothing (1 = the reference's Gauss-Seidel)."""
+        self._check(self._lib.fire_sim_set_mg_omega(self._h, float(omega)), "set_mg_omega")
 
     def set_spots(self, spots: np.ndarray):
         s = np.ascontiguousarray(spots, np.float32).reshape(-1, 5)

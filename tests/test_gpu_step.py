@@ -188,3 +188,31 @@ def test_residual_driven_solve(campfire):
     assert 1 <= info.last_cycles <= 12
     assert info.last_rel_residual <= 1e-4 or info.last_cycles == 12
     assert sim.residual() == pytest.approx(info.last_rel_residual, rel=1e-6)
+
+
+def test_over_relaxed_smoothing(campfire):
+    """The over-relaxed fine-level smoothing (omega = 1.2) still converges: every step ends at or below the
+    tolerance, in no more cycles than Gauss-Seidel; omega = 1 stays the reference's smoother bit for bit."""
+    cfg = dict(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=4, mg_max_cycles=12, mg_tol=1e-5)
+    runs = {}
+    for omega in (1.0, 1.2):
+        sim = F.FireSim(**cfg)
+        sim.set_mg_omega(omega)
+        c0 = None
+        for k in range(30):
+            sim.step(FC.C1["dt"], 1)
+            sim.sync()
+            info = sim.info()
+            assert info.last_rel_residual <= 1e-5 or info.last_cycles == 12
+            if k == 9:
+                c0 = info.total_cycles
+        runs[omega] = (sim.info().total_cycles - c0) / 20
+        sim.close()
+    assert runs[1.2] <= runs[1.0], runs
+    a, b = (F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=4) for _ in range(2))
+    b.set_mg_omega(1.0)
+    a.step(FC.C1["dt"], 5)
+    b.step(FC.C1["dt"], 5)
+    a.sync(); b.sync()
+    assert np.array_equal(a.download("vel"), b.download("vel"))
+    a.close(); b.close()
