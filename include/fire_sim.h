@@ -158,10 +158,10 @@ int fire_sim_set_bed_gain(FireSim* sim, float gain);
  * source of peak weight flux / ref_flux (ref_flux = 4 g/s) with a Gaussian profile of width sigma;
  * it feeds the same source path as the log pyrolysis band (src/sim.js:246-284).                    */
 int fire_sim_set_spots(FireSim* sim, const float* spots, int n);
-/* Over-relaxation factor of the V-cycle's launch-per-sweep smoothing (levels above the shared-memory tail):
- * p += omega (p_GS - p), 0 < omega < 2.  1 (default) is the reference's Gauss-Seidel (src/sim.js:417-437)
- * bit for bit; a larger value can cut the cycles a residual-driven solve needs (no counterpart in the
- * reference).                                                                                        */
+/* Over-relaxation factor of every red-black sweep of the step's V-cycle (pre/post smoothing and the
+ * coarsest-level sweeps): p += omega (p_GS - p), 0 < omega < 2.  1 (default) is the reference's
+ * Gauss-Seidel (src/sim.js:417-437) bit for bit; a larger value can cut the cycles a residual-driven solve
+ * needs (no counterpart in the reference).                                                            */
 int fire_sim_set_mg_omega(FireSim* sim, float omega);
 
 /* ---- events (src/main.js:401-407, 456-461; src/timeline.js:126-157) ---------------------------- */

@@ -222,6 +222,7 @@ struct TailLevels {
   float* gp[TAIL_MAX_LEVELS];  // global copies (written back at the end)
   float* gb[TAIL_MAX_LEVELS];
   int coarse;                  // coarsest-level sweeps (used by the batched tails; per-simulation launches pass it)
+  float omega;                 // over-relaxation of the sweeps (1: Gauss-Seidel)
   int coarse64;                // 1: the coarsest level is solved in FP64: p = cinv b with the dense inverse
   int doff;                    //    (transposed, global memory) if cinv is set, else `coarse` FP64 sweeps on a
   const double* cinv;          //    double copy at float offset doff
@@ -261,7 +262,7 @@ struct Box3 {
   }
 };
 template <bool kWarp>
-__device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters) {
+__device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters, float omega) {
   const int hx = (nx + 1) >> 1;
   const float h2 = h * h;
   const Box3 bx(tm.size, tm.rank, hx, ny, nz);
@@ -271,7 +272,12 @@ __device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int
         for (int y = bx.y0; y < ny; y += bx.ty)
           for (int gx = bx.x0; gx < hx; gx += bx.tx) {
             const int x = gx * 2 + ((y + z + color) & 1);
-            if (x < nx) p[x + nx * (y + ny * z)] = rb_update(p, b, x, y, z, nx, ny, nz, h2);
+            if (x < nx) {
+              const int c = x + nx * (y + ny * z);
+              float v = rb_update(p, b, x, y, z, nx, ny, nz, h2);
+              if (omega != 1.0f) v = fmaf(omega, v - p[c], p[c]);
+              p[c] = v;
+            }
           }
       tm.sync();
     }
@@ -366,7 +372,7 @@ __device__ void tail_vcycle(const Team<kWarp>& tm, const TailLevels& T, float* s
   const int n = T.n;
   for (int l = from; l < n - 1; ++l) {
     float* p = sm + T.off[l];
-    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
+    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega);
     tail_restrict(tm, T, sm, l);
   }
   {
@@ -377,12 +383,12 @@ __device__ void tail_vcycle(const Team<kWarp>& tm, const TailLevels& T, float* s
       tail_smooth_fp64(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse,
                        reinterpret_cast<double*>(sm + T.doff));
     else
-      tail_smooth(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse);
+      tail_smooth(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse, T.omega);
   }
   for (int l = n - 2; l >= from; --l) {
     tail_prolong(tm, T, sm, l);
     float* p = sm + T.off[l];
-    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
+    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega);
   }
 }
 // The V-cycle over all levels of T with one CTA of TAIL_THREADS threads: levels above T.small with the
@@ -419,14 +425,14 @@ __device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre
     const int n = T.n, top = min(S, n - 1);
     for (int l = 0; l < top; ++l) {
       float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega);
       tail_restrict(cta, T, sm, l);
     }
     if (tid < 32) {
       const Team<true> wp{tid};
       for (int l = top; l < n - 1; ++l) {
         float* p = sm + T.off[l];
-        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
+        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega);
         tail_restrict(wp, T, sm, l);
       }
     }
@@ -441,14 +447,14 @@ __device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre
       for (int l = n - 2; l >= top; --l) {
         tail_prolong(wp, T, sm, l);
         float* p = sm + T.off[l];
-        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
+        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega);
       }
     }
     __syncthreads();
     for (int l = top - 1; l >= 0; --l) {
       tail_prolong(cta, T, sm, l);
       float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega);
     }
     return;
   }
@@ -461,7 +467,7 @@ __device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre
     // large levels [0, S) with the whole CTA; the V-cycle below S (levels S..n-1) on warp 0
     for (int l = 0; l < S; ++l) {
       float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre);
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega);
       tail_restrict(cta, T, sm, l);
     }
     if (tid < 32) tail_vcycle(Team<true>{tid}, T, sm, S, pre, post, coarse);
@@ -469,7 +475,7 @@ __device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre
     for (int l = S - 1; l >= 0; --l) {
       tail_prolong(cta, T, sm, l);
       float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post);
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega);
     }
   }
 }
@@ -996,6 +1002,7 @@ static TailLevels make_tail_levels(const MGLevel* levels, int first, int n, int 
     if (T.small == T.n && L.nx * L.ny * L.nz <= TAIL_WARP_CELLS) T.small = l;
   }
   T.coarse = 0;
+  T.omega = T.n > 0 ? levels[first].omega : 1.0f;
   T.coarse64 = coarse64 ? 1 : 0;
   T.doff = (int)tail_fp64_offset((size_t)off);
   T.cinv = coarse64 ? cinv : nullptr;
