@@ -1076,6 +1076,8 @@ int fire_ensemble_create(const FireConfig* cfgs, int n, FireEnsemble** out) {
     const int rc = fire_sim_create(&cfgs[i], nullptr, 0, &s);
     if (rc) { fire_ensemble_destroy(e); return rc; }
     e->sims.push_back(s);
+    // members' tails run side by side in one launch: let each start at the finest level that fits
+    s->tailFirst = tail_first(s->levels.data(), (int)s->levels.size(), false, 1L << 40);
     if (s->tailFirst >= (int)s->levels.size()) { fire_ensemble_destroy(e); return FIRE_ERR_BAD_ARG; }   // needs a tail
   }
   cudaSetDevice(e->device);

@@ -130,12 +130,13 @@ void launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st);
 // One launch runs the V-cycle over levels [first, n) out of shared memory: a single CTA when every level
 // fits in its shared memory, or a thread-block cluster whose CTAs each hold a z-slab of the finer tail
 // levels (distributed shared memory for the slab edges) with the coarsest levels gathered on CTA 0.
-// tail_fits: whether [first, n) can run as one tail launch; tail_first: the finest `first` that fits (n if
-// none), single-CTA forms only unless allow_cluster.
+// tail_fits: whether [first, n) can run as one tail launch; tail_first: the finest `first` that fits and has
+// at most max_cells cells (n if none) — for one simulation, larger levels are cheaper as their own launches.
 // coarse64: the coarsest level is solved in FP64: exactly with `cinv` (its dense inverse, transposed, in
 // global memory) when given, else by `coarse` FP64 sweeps on a double copy in shared memory.
 bool tail_fits(const MGLevel* levels, int first, int n, bool coarse64 = false);
-int tail_first(const MGLevel* levels, int n, bool coarse64 = false, bool allow_cluster = false);
+constexpr long TAIL_FIRST_CELLS = 8192;
+int tail_first(const MGLevel* levels, int n, bool coarse64 = false, long max_cells = TAIL_FIRST_CELLS);
 // Shared memory per CTA of the tail launch for [first, n).
 size_t tail_smem_bytes(const MGLevel* levels, int first, int n, bool coarse64 = false);
 // `err` receives 1 if the kernel's bounded wait for its bulk copies ran out (the kernel then returns early).

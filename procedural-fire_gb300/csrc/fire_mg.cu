@@ -619,7 +619,7 @@ __device__ __forceinline__ float rb_update_planes(const float* pl, const float* 
   if (y < ny - 1) sum += pm[c + nx]; else diag += 1.0f;
   return __fdividef(sum - h2 * bm[c], diag);
 }
-__device__ void ct_smooth(const cg::cluster_group& cl, const DSlab& s, unsigned r, int tid, int iters) {
+__device__ void ct_smooth(const cg::cluster_group& cl, const DSlab& s, unsigned r, int tid, int iters, float omega) {
   const int hx = (s.nx + 1) >> 1;
   const float h2 = s.h * s.h;
   const float* b = s.p + s.P * s.plane;
@@ -635,7 +635,11 @@ __device__ void ct_smooth(const cg::cluster_group& cl, const DSlab& s, unsigned 
         for (int y = bx.y0; y < s.ny; y += bx.ty)
           for (int gx = bx.x0; gx < hx; gx += bx.tx) {
             const int x = gx * 2 + ((y + z + color) & 1);
-            if (x < s.nx) pm[x + s.nx * y] = rb_update_planes(pl, pm, pu, bm, x, y, s.nx, s.ny, h2);
+            if (x < s.nx) {
+              float v = rb_update_planes(pl, pm, pu, bm, x, y, s.nx, s.ny, h2);
+              if (omega != 1.0f) v = fmaf(omega, v - pm[x + s.nx * y], pm[x + s.nx * y]);
+              pm[x + s.nx * y] = v;
+            }
           }
       }
       cl.sync();
@@ -766,7 +770,7 @@ __device__ __forceinline__ void ctail_body(const CTailLevels& T, int pre, int po
   const int gcells = gplane * T.G.nz[0];
   for (int l = 0; l < T.nd; ++l) {
     const DSlab s = make_slab(T, l, r, sm);
-    ct_smooth(cl, s, r, tid, pre);
+    ct_smooth(cl, s, r, tid, pre, T.G.omega);
     if (l + 1 < T.nd) {
       const DSlab c = make_slab(T, l + 1, r, sm);
       ct_restrict(cl, s, r, tid, c.p, c.P * c.plane);
@@ -786,7 +790,7 @@ __device__ __forceinline__ void ctail_body(const CTailLevels& T, int pre, int po
       src = CSrc{g0r, 0, T.G.nz[0], gplane, false};
     }
     ct_prolong(cl, s, src, r, tid);
-    ct_smooth(cl, s, r, tid, post);
+    ct_smooth(cl, s, r, tid, post, T.G.omega);
   }
   {  // the first tail level's p back to global memory (the next prolongation reads it)
     const DSlab s = make_slab(T, 0, r, sm);
@@ -978,13 +982,16 @@ bool tail_fits(const MGLevel* levels, int first, int n, bool coarse64) {
   return first >= 0 && first < n && n - first - tail_dist_levels(levels, first, n) <= TAIL_MAX_LEVELS &&
          tail_smem_bytes(levels, first, n, coarse64) <= TAIL_SMEM_BUDGET;
 }
-// The step's V-cycle keeps its tail single-CTA: measured in CUDA graphs on GB300, a level of >= 32k cells
-// costs less as its 10 full-grid launches (~21 us) than inside the cluster tail (the 8-CTA tail from 32x64x32
-// takes 57 us against 21 + 31 us for that level separately plus the single-CTA tail below it).  The
-// standalone solver's tail (FP64 coarsest solve) still gains from the cluster form and asks for it.
-int tail_first(const MGLevel* levels, int n, bool coarse64, bool allow_cluster) {
+// Where the tail starts, from measurements in CUDA graphs on GB300 (us per V-cycle for the coarse end):
+//   128x256x128: tail from 32x64x32 (cluster) 57.4 | 32x64x32 as 10 launches + tail from 16x32x16 (cluster)
+//   20.6 + 30.8 = 51.4 | two levels as launches + tail from 8x16x8 (single CTA) 20.6 + 20.6 + 16.5 = 57.7;
+//   the same ordering at 64x128x64 and 256x512x256.  A level of more than TAIL_FIRST_CELLS (8192) cells is cheaper
+//   as its own launches than inside the tail, so a simulation's tail starts at the finest level that fits and
+//   is no larger than that.  An ensemble runs its members' tails side by side in one launch, which hides a
+//   larger tail's latency, so it lets the tail start at the finest level that fits.
+int tail_first(const MGLevel* levels, int n, bool coarse64, long max_cells) {
   int first = n;
-  for (int l = n - 1; l >= 0 && tail_fits(levels, l, n, coarse64) && (allow_cluster || tail_dist_levels(levels, l, n) == 0); --l)
+  for (int l = n - 1; l >= 0 && tail_fits(levels, l, n, coarse64) && (long)levels[l].nx * levels[l].ny * levels[l].nz <= max_cells; --l)
     first = l;
   return first;
 }

@@ -1055,7 +1055,7 @@ int fire_poisson_create(const int res[3], float h, int precision, int device, Fi
     ps->coarseIters = (int)std::max(8.0, std::min(64.0, std::ceil(std::log(0.05) / std::log(mu * mu))));
   }
   const int n = (int)ps->mg.size();
-  ps->tailFirst = tail_first(ps->mg.data(), n, ps->ir, true);
+  ps->tailFirst = tail_first(ps->mg.data(), n, ps->ir);
   std::vector<double> cinv;
   const MGLevel& C = ps->mg.back();
   const int ccells = C.nx * C.ny * C.nz;

@@ -9,8 +9,9 @@ import fire_cases as FC
 
 pytestmark = pytest.mark.gpu
 
-# grids chosen to cover every batched path: levels outside the tail (48x96x48: two; 64x128x64: three) and
-# single-CTA tails starting at different levels (24x48x24 from level 0)
+# grids chosen to cover every batched path: levels outside the tail (48x96x48: two; 64x128x64: two), the
+# single-CTA tail (48x96x48 from level 2, 24x48x24 from level 1) and the cluster tail (32x64x32 from level 1,
+# 64x128x64 from level 2)
 MEMBERS = [
     dict(res=(48, 96, 48), size=(0.6, 1.2, 0.6), seed=11, spots=5),
     dict(res=(32, 64, 32), size=(0.4, 0.8, 0.4), seed=12, spots=2),

@@ -154,8 +154,9 @@ def test_rb_sweeps(level, sweeps):
                                  (64, 128, 64)])
 def test_mg_vcycle_tail_shapes(res):
     """V-cycles whose shared-memory tail has only warp-sized levels (8x16x8), only CTA-sized levels (12x400x12:
-    coarsest 6x200x6), an odd coarsest level (20x30x20 -> 10x15x10), and launch-per-phase levels above the
-    tail (16x32x16 up to 64x128x64; 48x32x32 with nx not a power of two)."""
+    coarsest 6x200x6), an odd coarsest level (20x30x20 -> 10x15x10), cluster tails (16x32x16: one distributed
+    level over gathered levels), and launch-per-phase levels above the tail (32x64x32 up to 64x128x64;
+    48x32x32 with nx not a power of two)."""
     cfg = dict(res=res, size=(0.02 * res[0], 0.02 * res[1], 0.02 * res[2]), dt=0.01, vcycles=2)
     sim, orc = FC.make_pair(cfg)
     rng = np.random.default_rng(sum(res))
