@@ -49,8 +49,9 @@ __device__ __forceinline__ float rb_update(const float* p, const float* b, int x
 constexpr int SMZ = FIRE_SMOOTH_Z;
 // omega != 1 over-relaxes the update (p + omega (p_gs - p)); omega == 1 is the reference's Gauss-Seidel
 // update bit for bit.
-__device__ __forceinline__ void smooth_body(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz, float h, int color,
-                                            uint3 blk, float omega = 1.0f) {
+template <bool kRelax>
+__device__ __forceinline__ void smooth_body_t(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz, float h, int color,
+                                              uint3 blk, float omega) {
   pdl_wait();
   pdl_trigger();
   const int gx = blk.x * GX + threadIdx.x, y = blk.y * GY + threadIdx.y;
@@ -64,7 +65,7 @@ __device__ __forceinline__ void smooth_body(float* __restrict__ p, const float* 
     const int x = gx * 2 + ((y + z + color) & 1);
     if (z < nz && x < nx) {
       v[k] = rb_update(p, b, x, y, z, nx, ny, nz, h2);
-      if (omega != 1.0f) {
+      if (kRelax) {
         const float old = p[x + nx * (y + ny * z)];
         v[k] = fmaf(omega, v[k] - old, old);
       }
@@ -76,6 +77,11 @@ __device__ __forceinline__ void smooth_body(float* __restrict__ p, const float* 
     const int x = gx * 2 + ((y + z + color) & 1);
     if (z < nz && x < nx) p[x + nx * (y + ny * z)] = v[k];
   }
+}
+__device__ __forceinline__ void smooth_body(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz, float h, int color,
+                                            uint3 blk, float omega = 1.0f) {
+  if (omega == 1.0f) smooth_body_t<false>(p, b, nx, ny, nz, h, color, blk, omega);
+  else smooth_body_t<true>(p, b, nx, ny, nz, h, color, blk, omega);
 }
 
 // ---------------- fused residual + restriction (src/sim.js:439-466) ----------------
@@ -261,8 +267,8 @@ struct Box3 {
     if (z0 >= tz) z0 = 1 << 30;   // surplus thread: its loops never run (prolongation is read-modify-write)
   }
 };
-template <bool kWarp>
-__device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters, float omega) {
+template <bool kWarp, bool kRelax>
+__device__ void tail_smooth_t(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters, float omega) {
   const int hx = (nx + 1) >> 1;
   const float h2 = h * h;
   const Box3 bx(tm.size, tm.rank, hx, ny, nz);
@@ -274,13 +280,18 @@ __device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int
             const int x = gx * 2 + ((y + z + color) & 1);
             if (x < nx) {
               const int c = x + nx * (y + ny * z);
-              float v = rb_update(p, b, x, y, z, nx, ny, nz, h2);
-              if (omega != 1.0f) v = fmaf(omega, v - p[c], p[c]);
-              p[c] = v;
+              const float v = rb_update(p, b, x, y, z, nx, ny, nz, h2);
+              p[c] = kRelax ? fmaf(omega, v - p[c], p[c]) : v;
             }
           }
       tm.sync();
     }
+}
+// `iters` red-black sweeps of one level (over-relaxed by omega when omega != 1).
+template <bool kWarp>
+__device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters, float omega) {
+  if (omega == 1.0f) tail_smooth_t<kWarp, false>(tm, p, b, nx, ny, nz, h, iters, omega);
+  else tail_smooth_t<kWarp, true>(tm, p, b, nx, ny, nz, h, iters, omega);
 }
 // `iters` red-black sweeps in FP64 on a double copy (dp: p then b) of one level; p is written back in FP32.
 // The update is mgSmooth's (src/sim.js:417-437) with IEEE double division.
@@ -619,7 +630,8 @@ __device__ __forceinline__ float rb_update_planes(const float* pl, const float* 
   if (y < ny - 1) sum += pm[c + nx]; else diag += 1.0f;
   return __fdividef(sum - h2 * bm[c], diag);
 }
-__device__ void ct_smooth(const cg::cluster_group& cl, const DSlab& s, unsigned r, int tid, int iters, float omega) {
+template <bool kRelax>
+__device__ void ct_smooth_t(const cg::cluster_group& cl, const DSlab& s, unsigned r, int tid, int iters, float omega) {
   const int hx = (s.nx + 1) >> 1;
   const float h2 = s.h * s.h;
   const float* b = s.p + s.P * s.plane;
@@ -636,14 +648,17 @@ __device__ void ct_smooth(const cg::cluster_group& cl, const DSlab& s, unsigned 
           for (int gx = bx.x0; gx < hx; gx += bx.tx) {
             const int x = gx * 2 + ((y + z + color) & 1);
             if (x < s.nx) {
-              float v = rb_update_planes(pl, pm, pu, bm, x, y, s.nx, s.ny, h2);
-              if (omega != 1.0f) v = fmaf(omega, v - pm[x + s.nx * y], pm[x + s.nx * y]);
-              pm[x + s.nx * y] = v;
+              const float v = rb_update_planes(pl, pm, pu, bm, x, y, s.nx, s.ny, h2);
+              pm[x + s.nx * y] = kRelax ? fmaf(omega, v - pm[x + s.nx * y], pm[x + s.nx * y]) : v;
             }
           }
       }
       cl.sync();
     }
+}
+__device__ void ct_smooth(const cg::cluster_group& cl, const DSlab& s, unsigned r, int tid, int iters, float omega) {
+  if (omega == 1.0f) ct_smooth_t<false>(cl, s, r, tid, iters, omega);
+  else ct_smooth_t<true>(cl, s, r, tid, iters, omega);
 }
 // Fused residual + 8-child restriction of this CTA's slab into coarse planes z0/2 .. z0/2 + P/2 - 1.
 // cp points at coarse plane z0/2 of p (local, or in CTA 0 for a gathered level); b is cb_off floats after p.
