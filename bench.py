@@ -367,8 +367,10 @@ ADJOINT = dict(name="adjoint-fit-64x128x64", res=(64, 128, 64), size=(0.64, 1.28
 
 
 def run_adjoint(dev: int, steps: int = 0, iterations: int = -1, mg_fixed: int = 0):
-    """Forward and adjoint time per step of the source fit, and a few gradient steps on the fluxes
-    (steps / iterations override the workload's for profiling runs)."""
+    """Adjoint cost per step on the source-fit workload (checkpoints every 10 steps, and with the whole
+    rollout on the tape), then how far the gradient describes the loss: for rollouts of 10, 30 and 120 steps,
+    the loss along -grad against the first-order prediction, and a fit of the fluxes on the horizon where the
+    gradient is predictive (steps / iterations override the workload's for profiling runs)."""
     import torch
     import fire_sim as F
     A = dict(ADJOINT)
@@ -392,7 +394,22 @@ def run_adjoint(dev: int, steps: int = 0, iterations: int = -1, mg_fixed: int = 
             s.set_mg_omega(A["mg_omega"])
         return s
 
-    # the target, and the plain forward's time per step (the step graph, same solve)
+    def target_at(n):
+        s = make(spots_a)
+        s.step(A["dt"], n, stream=st.cuda_stream)
+        out = s.download("S").astype(np.float32)
+        s.close()
+        return out
+
+    def run(adj, sim, flux, target):
+        sim.reset()
+        sp = spots_b.copy()
+        sp[:, 4] = flux
+        sim.set_spots(sp)
+        adj.forward(A["dt"], stream=st.cuda_stream)
+        return adj.loss(target)
+
+    # cost: the plain forward (the step graph, same solve), the taped forward and the backward
     sim = make(spots_a)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
@@ -403,48 +420,59 @@ def run_adjoint(dev: int, steps: int = 0, iterations: int = -1, mg_fixed: int = 
     target = sim.download("S").astype(np.float32)
     sim.close()
     sim = make(spots_b)
-    adj = F.Adjoint(sim, A["steps"], A["checkpoint"])
-    flux = spots_b[:, 4].astype(np.float64)
-    hist, fwd, bwd = [], [], []
-    for it in range(A["iterations"] + 1):
-        sim.reset()
-        sp = spots_b.copy()
-        sp[:, 4] = flux
-        sim.set_spots(sp)
-        adj.forward(A["dt"], stream=st.cuda_stream)
-        loss = adj.loss(target)
-        adj.backward(stream=st.cuda_stream)
-        g = adj.grad_spots(A["spots"])
-        f_ms, b_ms = adj.timing()
+    fwd, bwd = [], []
+    for ck in (A["checkpoint"], A["steps"]):
+        adj = F.Adjoint(sim, A["steps"], ck)
+        for _ in range(2):
+            run(adj, sim, spots_b[:, 4], target)
+            adj.backward(stream=st.cuda_stream)
+            f_ms, b_ms = adj.timing()
         fwd.append(f_ms / A["steps"])
         bwd.append(b_ms / A["steps"])
-        hist.append({"loss": loss, "flux_err_gps": float(np.abs(flux - spots_a[:, 4]).max()), "grad_norm": float(np.linalg.norm(g))})
-        if it == A["iterations"]:
-            break
-        # a projected gradient step on the fluxes along -g, backtracking from 0.2 g/s until the loss drops
-        # (the rollout is chaotic: the gradient describes the loss only over small flux changes)
-        step = 0.2
-        for _ in range(6):
-            trial = np.clip(flux - step * g / max(np.linalg.norm(g), 1e-30), 0.0, 8.0)
-            sim.reset()
-            sp = spots_b.copy()
-            sp[:, 4] = trial
-            sim.set_spots(sp)
-            adj.forward(A["dt"], stream=st.cuda_stream)
-            if adj.loss(target) < loss:
-                flux = trial
-                break
-            step *= 0.25
-    adj.close()
+        adj.close()
+    # how far the gradient describes the loss, per rollout length
+    horizons = []
+    fit = []
+    for n in sorted({10, 30, A["steps"]}):
+        tgt = target_at(n)
+        adj = F.Adjoint(sim, n, min(A["checkpoint"], n))
+        flux0 = spots_b[:, 4].astype(np.float64)
+        L0 = run(adj, sim, flux0, tgt)
+        adj.backward(stream=st.cuda_stream)
+        g = adj.grad_spots(A["spots"])
+        d = -g / max(np.linalg.norm(g), 1e-30)
+        probe = []
+        for s in (1e-4, 1e-3, 1e-2, 1e-1):
+            L = run(adj, sim, np.clip(flux0 + s * d, 0.0, 8.0), tgt)
+            probe.append({"step_gps": s, "loss_change": L - L0, "predicted_change": s * float(g @ d)})
+        horizons.append({"steps": n, "loss": L0, "grad_norm": float(np.linalg.norm(g)), "along_minus_grad": probe})
+        if n == 10 and A["iterations"] > 0:
+            # projected gradient descent on the fluxes with backtracking, on this horizon
+            flux, L = flux0.copy(), L0
+            fit.append({"loss": L, "flux_err_gps": float(np.abs(flux - spots_a[:, 4]).max())})
+            for _ in range(A["iterations"]):
+                run(adj, sim, flux, tgt)
+                adj.backward(stream=st.cuda_stream)
+                g = adj.grad_spots(A["spots"])
+                step = 0.5
+                for _ in range(6):
+                    trial = np.clip(flux - step * g / max(np.linalg.norm(g), 1e-30), 0.0, 8.0)
+                    Lt = run(adj, sim, trial, tgt)
+                    if Lt < L:
+                        flux, L = trial, Lt
+                        break
+                    step *= 0.25
+                fit.append({"loss": L, "flux_err_gps": float(np.abs(flux - spots_a[:, 4]).max())})
+        adj.close()
     sim.close()
-    fwd_ms, bwd_ms = float(np.median(fwd[1:] or fwd)), float(np.median(bwd[1:] or bwd))
     return {"workload": A["name"], "steps": A["steps"], "checkpoint_every": A["checkpoint"],
             "mg": f"{mg_fixed} fixed V(2,2) cycles" if mg_fixed else
                   f"V(2,2), omega {A['mg_omega']}, to {A['mg_tol']} rel. residual, max {A['mg_max_cycles']}",
-            "ms_per_step_forward_plain": ms_plain, "ms_per_step_forward_taped": fwd_ms,
-            "ms_per_step_backward": bwd_ms, "adjoint_over_forward": bwd_ms / ms_plain,
+            "ms_per_step_forward_plain": ms_plain, "ms_per_step_forward_taped": fwd[0],
+            "ms_per_step_backward": bwd[0], "adjoint_over_forward": bwd[0] / ms_plain,
+            "ms_per_step_backward_whole_tape": bwd[1], "adjoint_over_forward_whole_tape": bwd[1] / ms_plain,
             "backward_includes": "recompute of every segment but the last from its checkpoint, then the reverse steps",
-            "fit": hist}
+            "gradient_vs_horizon": horizons, "fit_10_steps": fit}
 
 
 # ------------------------------------------------------------------------------------------ arms

@@ -450,7 +450,8 @@ enum {
   FIRE_ADJ_COUNT = 14
 };
 typedef struct FireAdjoint FireAdjoint;
-/* n_steps >= 1, 1 <= checkpoint_every <= 64.  Device memory: (k + 1) * 3 + k * 7 + 12 float4 fields plus
+/* n_steps >= 1, 1 <= checkpoint_every <= 512 (k >= n_steps keeps the whole rollout on the tape: no
+ * recomputation, 2 CUDA graphs per step captured once).  Device memory: (k + 1) * 3 + k * 7 + 12 float4 fields plus
  * (n_steps / k + 1) * 3 checkpoint fields.  The solve mode (fixed V-cycles or residual-driven) is the
  * simulation's at creation.                                                                             */
 int fire_adjoint_create(FireSim* sim, int n_steps, int checkpoint_every, FireAdjoint** out);

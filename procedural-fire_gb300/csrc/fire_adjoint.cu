@@ -1010,7 +1010,7 @@ float4* adj_buf4(FireAdjoint* A, int which) {
 extern "C" {
 
 int fire_adjoint_create(FireSim* sim, int n_steps, int checkpoint_every, FireAdjoint** out) {
-  if (!sim || !out || n_steps < 1 || checkpoint_every < 1 || checkpoint_every > 64) return FIRE_ERR_BAD_ARG;
+  if (!sim || !out || n_steps < 1 || checkpoint_every < 1 || checkpoint_every > 512) return FIRE_ERR_BAD_ARG;
   *out = nullptr;
   if (cudaSetDevice(sim->device) != cudaSuccess) return FIRE_ERR_CUDA;
   FireAdjoint* A = new FireAdjoint();
