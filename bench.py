@@ -173,18 +173,27 @@ def make_sim(F, device: int, mg_fixed: int = 0):
 
 
 def launches_per_step(sim, cycles_per_step: float) -> float:
-    """Kernels launched per step by the captured graph: 5 stencil kernels, the counter reset, and per
-    V-cycle 6 per level above the shared-memory tail (2 + 2 sweeps, restrict, prolong), the tail kernel,
-    2 residual kernels and the decision."""
+    """Kernels launched per step by the captured graph: 5 stencil kernels and the cycle-counter reset, and per
+    V-cycle 10 per level above the shared-memory tail (2 + 2 red-black sweeps of 2 colour launches each,
+    restriction, prolongation), the tail kernel, the residual norm and the decision kernel.  The tail starts at
+    the finest level that fits in 200 KB of shared memory (one CTA, or 8 CTAs with distributed levels) and has
+    at most 8192 cells."""
     n = len(sim.levels)
-    cells = [l["dims"][0] * l["dims"][1] * l["dims"][2] for l in sim.levels]
     T = n
     for l in range(n - 1, -1, -1):
-        if 8 * sum(cells[l:]) <= 200 * 1024:
+        nx, ny, nz = sim.levels[l]["dims"]
+        cells = nx * ny * nz
+        smem = 0
+        for k in range(l, n):
+            kx, ky, kz = sim.levels[k]["dims"]
+            c = kx * ky * kz
+            dist = k < n - 1 and kz % 16 == 0 and c >= 8 * 512
+            smem += 8 * (c // 8 if dist else c)
+        if cells <= 8192 and smem <= 200 * 1024:
             T = l
         else:
             break
-    per_cycle = 6 * min(T, n - 1) + (1 if T < n else sim.coarse_iters) + 3
+    per_cycle = 10 * T + (1 if T < n else 0) + 2
     return 6 + per_cycle * cycles_per_step
 
 
