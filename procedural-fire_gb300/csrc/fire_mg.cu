@@ -37,8 +37,9 @@ __device__ __forceinline__ float rb_update(const float* p, const float* b, int x
   if (y > 0) sum += p[c - sy]; else diag -= 1.0f;
   if (y < ny - 1) sum += p[c + sy]; else diag += 1.0f;
   // WGSL's `/` is specified to 2.5 ULP; the fast reciprocal-multiply quotient (<= 2 ULP) keeps the
-  // smoother at a handful of instructions per cell instead of an IEEE division sequence
-  return __fdividef(sum - h2 * b[c], diag);
+  // smoother at a handful of instructions per cell instead of an IEEE division sequence.  sum - h2 b is one
+  // explicit FMA in every form of the sweep (launch per colour, shared-memory tails), so they give the same bits.
+  return __fdividef(__fmaf_rn(-h2, b[c], sum), diag);
 }
 // Each thread updates SMZ cells of one colour, SMZ planes apart in z (unrolled and independent, so their
 // loads are in flight together): the sweep is latency-bound on L2 hits, and fewer, longer CTAs also cut the
@@ -628,7 +629,7 @@ __device__ __forceinline__ float rb_update_planes(const float* pl, const float* 
   if (pu) sum += pu[c]; else diag += 1.0f;
   if (y > 0) sum += pm[c - nx]; else diag -= 1.0f;
   if (y < ny - 1) sum += pm[c + nx]; else diag += 1.0f;
-  return __fdividef(sum - h2 * bm[c], diag);
+  return __fdividef(__fmaf_rn(-h2, bm[c], sum), diag);
 }
 template <bool kRelax>
 __device__ void ct_smooth_t(const cg::cluster_group& cl, const DSlab& s, unsigned r, int tid, int iters, float omega) {
