@@ -674,7 +674,11 @@ class Adjoint:
         return out
 
     def put(self, name: str, arr: np.ndarray):
-        a = np.ascontiguousarray(arr, np.float32).reshape(self._shape(name))
+        shape = self._shape(name)
+        a = np.ascontiguousarray(arr, np.float32)
+        if a.size != int(np.prod(shape)):
+            raise FireError(1, f"adjoint put {name}: expected shape {shape}")
+        a = a.reshape(shape)
         self._check(self._lib.fire_adjoint_io(self._h, ADJ_BUFFERS[name], _ptr(a), a.nbytes, 1), f"adjoint put {name}")
 
     def clear(self):

@@ -1,0 +1,55 @@
+"""Error behaviour of the C ABI entry points beyond the step (status codes, no state change on a refused call),
+as the reference's UniformStruct.set throws on an unknown name (src/gpu.js:65)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mg_omega_and_adjoint_misuse():
+    import fire_sim as F
+    sim = F.FireSim(res=(16, 32, 16), size=(0.2, 0.4, 0.2), vcycles=2)
+    for bad in (0.0, -1.0, 2.0, float("nan")):
+        with pytest.raises(F.FireError) as e:
+            sim.set_mg_omega(bad)
+        assert e.value.code == 1
+    sim.set_mg_omega(1.2)
+    sim.step(0.01, 2)
+    sim.sync()
+    adj = F.Adjoint(sim, 4, 2)
+    with pytest.raises(F.FireError) as e:   # a backward needs a forward first
+        adj.backward()
+    assert e.value.code == 6
+    with pytest.raises(F.FireError):
+        adj.put("vel", np.zeros(10, np.float32))   # wrong size
+    with pytest.raises(F.FireError):
+        adj.stage("geo", 0.01)                     # no adjoint of the geometry stage
+    with pytest.raises(F.FireError):
+        F.Adjoint(sim, 0, 1)
+    with pytest.raises(F.FireError):
+        F.Adjoint(sim, 4, 0)
+    adj.forward(0.01)
+    adj.seed(S=np.ones((16, 32, 16, 4), np.float32))
+    adj.backward()
+    sim.sync()
+    assert np.isfinite(adj.get("vel")).all()
+    adj.close()
+    sim.close()
+
+
+def test_ensemble_tile_api_misuse():
+    import fire_sim as F
+    ens = F.Ensemble([dict(res=(16, 32, 16), size=(0.2, 0.4, 0.2))] * 2, vcycles=2)
+    assert ens.tiles() is None                      # no tuning step yet
+    for bad in ([0, 0, 3, 0, 0], [4, 0, 0, 0, 0], [0, 0, 0, 0, -1]):
+        with pytest.raises(F.FireError):
+            ens.set_tiles(bad)
+    with pytest.raises(F.FireError):
+        ens.set_autotune(-2)
+    ens.set_tiles([1, 2, 1, 3, 0])
+    tiles, _ = ens.tiles()
+    assert list(tiles) == [1, 2, 1, 3, 0]
+    ens.step(0.01, 2)
+    ens.sync()
+    assert all(np.isfinite(m.download("vel")).all() for m in ens.members)
+    ens.close()
