@@ -484,6 +484,78 @@ def run_adjoint(dev: int, steps: int = 0, iterations: int = -1, mg_fixed: int = 
             "gradient_vs_horizon": horizons, "fit_10_steps": fit}
 
 
+# Consumers of the step on the throughput workload's state: the sparks update (8192 sparks, the page's count,
+# src/main.js:42), the renderer's fire passes into a headless image at the page's 960x1080 view and the
+# 1080x1920 capture size (src/main.js:53-54, 161) with volume scale 1, and the cinematic's capture-mode driver.
+CONSUMERS = dict(name="consumers-128x256x128", sparks=8192, views=((960, 1080), (1080, 1920)), vol_scale=1.0, reps=20)
+
+
+def run_consumers(dev: int):
+    """Device time per call of the sparks step and the volume render, and capture-mode steps/s."""
+    import torch
+    import fire_sim as F
+    C, W = CONSUMERS, WORKLOAD
+    st = torch.cuda.current_stream(dev)
+    sh = st.cuda_stream
+    sim = make_sim(F, dev)
+    sim.step(W["dt"], W["preroll"], stream=sh)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize(dev)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps
+
+    out = {"workload": C["name"]}
+    sp = F.Sparks(sim, C["sparks"])
+    sp.set(rate=60.0)
+    for _ in range(30):
+        sp.burst(n=120, pos=(0.0, 0.1, 0.0))
+        sp.step(W["dt"], stream=sh)
+    alive = int((sp.download()[:, 14] > 0.5).sum())
+    out["sparks"] = {"count": C["sparks"], "alive": alive, "ms_per_step": timed(lambda: sp.step(W["dt"], stream=sh), 200)}
+    sp.close()
+    views = []
+    for w, h in C["views"]:
+        vol = F.Volume(sim, width=w, height=h, vol_scale=C["vol_scale"])
+        vol.set_camera((0.45, 0.45, 1.1), (0.0, 0.35, 0.0), 40.0)
+        frame = [0]
+
+        def render():
+            frame[0] += 1
+            vol.render(1.0 + frame[0] / 30.0, frame[0], stream=sh)
+
+        ms = timed(render, C["reps"])
+        views.append({"image": [vol.vw, vol.vh], "ms_per_frame": ms, "mrays_per_s": vol.vw * vol.vh / (ms * 1e-3) / 1e6})
+        vol.close()
+    out["volume"] = views
+    sim.close()
+    # capture mode: timeline.capStep (parameters, log offsets, bursts) + the simulation and spark steps
+    sim = make_sim(F, dev)
+    sp = F.Sparks(sim, C["sparks"])
+    tl = F.Timeline(F.build_campfire(7), 8)
+    for j in range(24):
+        tl.step(sim, j, sp, stream=sh)
+    torch.cuda.synchronize(dev)
+    n = 120
+    t0 = time.perf_counter()
+    for j in range(24, 24 + n):
+        tl.step(sim, j, sp, stream=sh)
+    torch.cuda.synchronize(dev)
+    out["timeline_capture"] = {"steps_per_frame": 8, "capture_steps_per_s": n / (time.perf_counter() - t0),
+                               "note": "host clock, timeline cues + simulation + sparks per step"}
+    tl.close()
+    sp.close()
+    sim.close()
+    return out
+
+
 # ------------------------------------------------------------------------------------------ arms
 def run_ours(args):
     import torch
@@ -598,7 +670,8 @@ def run_ours(args):
     }
     out["ensemble"] = None
     out["adjoint"] = None
-    if world == 1 and not (args.no_poisson and args.no_ensemble and args.no_adjoint):
+    out["consumers"] = None
+    if world == 1 and not (args.no_poisson and args.no_ensemble and args.no_adjoint and args.no_consumers):
         sim.close()   # frees the step's arena before the standalone workloads
         if not args.no_poisson:
             out["poisson"] = run_poisson(dev)
@@ -606,6 +679,8 @@ def run_ours(args):
             out["ensemble"] = run_ensemble(dev)
         if not args.no_adjoint:
             out["adjoint"] = run_adjoint(dev)
+        if not args.no_consumers:
+            out["consumers"] = run_consumers(dev)
     return out
 
 
@@ -665,7 +740,8 @@ def main(argv=None):
     ap.add_argument("--no-poisson", action="store_true", help="skip the standalone 256x512x256 pressure-solve timings")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-fire ensemble timings")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint source-fit timings")
-    ap.add_argument("--only", choices=["poisson", "ensemble", "adjoint"],
+    ap.add_argument("--no-consumers", action="store_true", help="skip the sparks / volume / capture-mode timings")
+    ap.add_argument("--only", choices=["poisson", "ensemble", "adjoint", "consumers"],
                     help="run just one of the side workloads and print its block (profiling aid)")
     ap.add_argument("--adjoint-steps", type=int, default=0, help="override the adjoint rollout length")
     ap.add_argument("--adjoint-iters", type=int, default=-1, help="override the number of fit iterations")
@@ -677,7 +753,8 @@ def main(argv=None):
         import torch
         torch.cuda.init()
         fn = {"poisson": lambda: run_poisson(0), "ensemble": lambda: run_ensemble(0),
-              "adjoint": lambda: run_adjoint(0, args.adjoint_steps, args.adjoint_iters, args.mg_fixed)}[args.only]
+              "adjoint": lambda: run_adjoint(0, args.adjoint_steps, args.adjoint_iters, args.mg_fixed),
+              "consumers": lambda: run_consumers(0)}[args.only]
         print(json.dumps({args.only: fn()}), flush=True)
         return
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
