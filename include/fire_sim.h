@@ -120,7 +120,8 @@ typedef struct FireInfo {
 /* new FireSim(device, {res, size, logs, vcycles, noiseTex, curlTex}) (src/sim.js:49-101).  Bakes the noise
  * and curl tables on the device (makeNoiseTexture/makeCurlTexture, src/noise.js:6-90).  `logs` holds
  * n_logs capsules of 8 floats (a.xyz, r, b.xyz, burn) as packLogs writes them (src/scene.js:92-98);
- * the reference passes all 16 packed slots, so n_logs = 16 with zero padding reproduces it.       */
+ * the reference passes all 16 packed slots, so n_logs = 16 with zero padding reproduces it.
+ * FIRE_ERR_BAD_ARG for a resolution below 2 on any axis or of more than 2^31 - 1 cells.           */
 int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSim** out);
 int fire_sim_destroy(FireSim* sim);
 

@@ -157,12 +157,13 @@ int ring_slot(FireSim* sim, float** slot, cudaEvent_t* ev) {
   return FIRE_OK;
 }
 
-int upload_block(FireSim* sim, float dt, cudaStream_t st, bool with_logs) {
+int upload_block(FireSim* sim, float dt, cudaStream_t st, bool with_logs, const float** staged) {
   float* slot;
   cudaEvent_t ev;
   int rc = ring_slot(sim, &slot, &ev);
   if (rc) return rc;
   fill_block(sim, dt, slot);
+  if (staged) *staged = slot;
   CK(cudaMemcpyAsync(sim->dBlock, slot, sizeof(float) * BLOCK_FLOATS, cudaMemcpyHostToDevice, st));
   if (with_logs) {
     std::memcpy(slot + BLOCK_FLOATS, sim->logs, sizeof(float) * MAX_LOGS * 8);
@@ -240,7 +241,19 @@ int record_step(FireSim* sim, cudaStream_t st, bool prof) {
   launch_adv2(P, sim->f, d, st);
   if ((rc = record_ev(sim, 2, st, prof))) return rc;
   if ((rc = record_ev(sim, 3, st, prof))) return rc;    // curl is fused into forces
-  launch_forces(P, sim->f, sim->noise, sim->curl, d, st);
+  {
+    // the block is a kernel parameter here; fire_sim_step sets each step's on the instantiated graph
+    ParamBlock pb;
+    std::memset(&pb, 0, sizeof pb);
+    launch_forces_pb(pb, sim->f, sim->noise, sim->curl, d, st);
+    CK(cudaGetLastError());
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &ndeps));
+    if (cs != cudaStreamCaptureStatusActive || ndeps != 1) return set_err(sim, FIRE_ERR_STATE, "forces node not captured");
+    sim->forcesNode = deps[0];
+  }
   if ((rc = record_ev(sim, 4, st, prof))) return rc;
   launch_div(P, sim->f, sim->levels[0].b, d, st);
   if ((rc = record_ev(sim, 5, st, prof))) return rc;
@@ -257,6 +270,7 @@ void drop_graph(FireSim* s) {
   if (s->graph) cudaGraphDestroy(s->graph);
   s->exec = nullptr;
   s->graph = nullptr;
+  s->forcesNode = nullptr;
 }
 
 int build_graph(FireSim* sim) {
@@ -331,6 +345,8 @@ int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSi
   *out = nullptr;
   for (int i = 0; i < 3; ++i)
     if (cfg->res[i] < 2 || cfg->size[i] <= 0.0f) return FIRE_ERR_BAD_ARG;
+  // the stencil kernels address cells with 32-bit offsets
+  if ((long long)cfg->res[0] * cfg->res[1] * cfg->res[2] > 0x7fffffffLL) return FIRE_ERR_BAD_ARG;
   if (n_logs < 0 || n_logs > MAX_LOGS || (n_logs > 0 && !logs)) return FIRE_ERR_BAD_ARG;
   if (cfg->vcycles < 0 || cfg->mg_max_cycles < 0) return FIRE_ERR_BAD_ARG;
   int ndev = 0;
@@ -473,9 +489,13 @@ int fire_sim_step(FireSim* sim, float dt, int n_steps, void* stream) {
   for (int s = 0; s < n_steps; ++s) {
     advance_events(sim, dt);
     const bool geo = !sim->geoReady || sim->logsDirty;
-    int rc = upload_block(sim, dt, st, geo);
+    const float* staged = nullptr;
+    int rc = upload_block(sim, dt, st, geo, &staged);
     if (rc) return rc;
     if (geo && (rc = ensure_geo(sim, st))) return rc;
+    ParamBlock pb;
+    std::memcpy(pb.v, staged, sizeof pb.v);
+    CK(forces_pb_set(sim->exec, sim->forcesNode, pb, sim->f, sim->noise, sim->curl, sim->d));
     CK(cudaGraphLaunch(sim->exec, st));
     sim->time += dt;                                                          // src/sim.js:646-647
     sim->frame += 1;

@@ -139,7 +139,7 @@ __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 // textureLoad with clamped coordinates (`ld`, src/sim.js:114)
 __device__ __forceinline__ float4 ldc(const float4* __restrict__ f, int x, int y, int z, Dims d) {
   x = min(max(x, 0), d.nx - 1); y = min(max(y, 0), d.ny - 1); z = min(max(z, 0), d.nz - 1);
-  return __ldg(f + cell(x, y, z, d.nx, d.ny));
+  return __ldg(f + (x + d.nx * (y + d.ny * z)));   // 32-bit offset, as in sample()
 }
 
 // ---- hashes (src/shaders/lib.js:3-18) ----
@@ -180,10 +180,12 @@ __device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {
   float s = 1.0f - t;
   return make_float4(a.x * s + b.x * t, a.y * s + b.y * t, a.z * s + b.z * t, a.w * s + b.w * t);
 }
+// Cell offsets of the gathers are 32-bit (a simulation has fewer than 2^31 cells, checked at creation): half the
+// registers of 64-bit offsets, which keeps the MacCormack kernels' eight-texel stencils out of local memory.
 __device__ __forceinline__ float4 sample(const float4* __restrict__ f, const Tap& t, Dims d) {
-  const size_t sy = (size_t)d.nx, sz = (size_t)d.nx * d.ny;
-  const size_t r00 = (size_t)t.y0 * sy + (size_t)t.z0 * sz, r10 = (size_t)t.y1 * sy + (size_t)t.z0 * sz;
-  const size_t r01 = (size_t)t.y0 * sy + (size_t)t.z1 * sz, r11 = (size_t)t.y1 * sy + (size_t)t.z1 * sz;
+  const int sy = d.nx, sz = d.nx * d.ny;
+  const int r00 = t.y0 * sy + t.z0 * sz, r10 = t.y1 * sy + t.z0 * sz;
+  const int r01 = t.y0 * sy + t.z1 * sz, r11 = t.y1 * sy + t.z1 * sz;
   float4 c00 = lerp4(__ldg(f + r00 + t.x0), __ldg(f + r00 + t.x1), t.fx);
   float4 c10 = lerp4(__ldg(f + r10 + t.x0), __ldg(f + r10 + t.x1), t.fx);
   float4 c01 = lerp4(__ldg(f + r01 + t.x0), __ldg(f + r01 + t.x1), t.fx);

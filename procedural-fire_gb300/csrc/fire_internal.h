@@ -104,6 +104,13 @@ void launch_adv1(const float* P, Fields f, Dims d, cudaStream_t st);
 void launch_adv2(const float* P, Fields f, Dims d, cudaStream_t st);
 void launch_curl(Fields f, Dims d, cudaStream_t st);
 void launch_forces(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
+// The parameter block as a kernel parameter (BLOCK_FLOATS floats, 832 bytes): the step graph's forces launch
+// takes it by value, and the host sets it on the instantiated graph before each step (forces_pb_set; `node`
+// is the kernel node that launch_forces_pb captured).
+struct ParamBlock { float v[BLOCK_FLOATS]; };
+void launch_forces_pb(const ParamBlock& pb, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
+cudaError_t forces_pb_set(cudaGraphExec_t exec, cudaGraphNode_t node, const ParamBlock& pb, Fields f, const uint2* noise,
+                          const uint2* curl, Dims d);
 void launch_forces_unfused(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
 void launch_forces_recompute(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
 // Opts the shared-memory kernels of fire_step.cu into their dynamic shared memory on the current device.

@@ -59,6 +59,7 @@ struct FireSim {
   cudaStream_t capStream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t forcesNode = nullptr;   // the step graph's forces launch, which takes the block by value
   bool graphProfiled = false;
   bool profiling = false;
   cudaEvent_t stageEv[FIRE_STAGE_COUNT + 1];
@@ -93,8 +94,9 @@ void advance_events(FireSim* s, float dt);
 int record_mg(FireSim* sim, cudaStream_t st);
 // Rebuilds the emitter geometry when stale (src/sim.js:632).
 int ensure_geo(FireSim* sim, cudaStream_t st);
-// Stages the block for dt (and the log buffer) in the pinned ring and copies it to the device on `st`.
-int upload_block(FireSim* sim, float dt, cudaStream_t st, bool with_logs);
+// Stages the block for dt (and the log buffer) in the pinned ring and copies it to the device on `st`;
+// `staged` (optional) receives the host copy of the block.
+int upload_block(FireSim* sim, float dt, cudaStream_t st, bool with_logs, const float** staged = nullptr);
 // One V(2,2) cycle of the pressure solve (src/sim.js:588-599) on `st`.
 void record_vcycle(FireSim* s, cudaStream_t st);
 cudaStream_t as_stream(void* s);

@@ -126,41 +126,51 @@ __global__ void __launch_bounds__(256) k_curl(Fields f, Dims d) {
 // velY Laplacian (only evaluated when visc > 0).
 // The cell's own SY, S2Y and geometry values are passed in (the z-marching kernel prefetches them a plane
 // ahead).
-template <class Nb>
-__device__ __forceinline__ void forces_cell(const float* __restrict__ P, const Fields& f, const uint2* __restrict__ noiseT,
+// Readers of the per-step parameter block for the forces physics: from global memory (batched, eager and
+// adjoint launches), or from the kernel's own parameter space (the step graph's launch, whose block is set on
+// the instantiated graph before every step), where each read is a constant-bank operand instead of a load.
+struct ParamsGlobal {
+  const float* __restrict__ P;
+  __device__ __forceinline__ float operator[](int i) const { return __ldg(P + i); }
+};
+struct ParamsByValue {
+  const ParamBlock& b;
+  __device__ __forceinline__ float operator[](int i) const { return b.v[i]; }
+};
+template <class PA, class Nb>
+__device__ __forceinline__ void forces_cell(const PA& pa, const Fields& f, const uint2* __restrict__ noiseT,
                                             const uint2* __restrict__ curlT, Dims d, int i, int j, int k, const Nb& nb,
                                             float4 s, float4 s2, const float4 geo) {
   const size_t ci = cell(i, j, k, d.nx, d.ny);
-  const float dt = __ldg(P + P_dt), dx = __ldg(P + P_dx), I = __ldg(P + P_intensity);
-  const float seed = __ldg(P + P_seed), time = __ldg(P + P_time);
-  const float* E = P + P_STRIDE;
-  f3 p = mk3(__ldg(P + P_ox), __ldg(P + P_oy), __ldg(P + P_oz)) + mk3((float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f) * dx;
+  const float dt = pa[P_dt], dx = pa[P_dx], I = pa[P_intensity];
+  const float seed = pa[P_seed], time = pa[P_time];
+  f3 p = mk3(pa[P_ox], pa[P_oy], pa[P_oz]) + mk3((float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f) * dx;
   float4 v4 = nb.vel_center();
   f3 v = xyz(v4);
 
   // ---- sources: pyrolysis on the hot log surfaces + the coal bed (src/sim.js:246-284)
   float src = 0.0f, anchor = 0.0f;
   if (geo.x > 0.001f) {
-    f3 qa = p * __ldg(P + P_anchorFreq) + mk3(seed * 0.37f, 0.0f, 0.11f);
+    f3 qa = p * pa[P_anchorFreq] + mk3(seed * 0.37f, 0.0f, 0.11f);
     anchor = sstep(-0.05f, 0.25f, noise4(noiseT, qa).z);
-    f3 qn = p * (__ldg(P + P_srcFreq) * 0.06f) + mk3(seed * 0.131f, 0.0f, time * __ldg(P + P_srcSpeed));
-    const float th = __ldg(P + P_srcThresh);
+    f3 qn = p * (pa[P_srcFreq] * 0.06f) + mk3(seed * 0.131f, 0.0f, time * pa[P_srcSpeed]);
+    const float th = pa[P_srcThresh];
     float pulse = sstep(th - 0.25f, th + 0.25f, noise4(noiseT, qn).x);
-    src = clampf(geo.x * __ldg(P + P_logSrc) * (__ldg(P + P_srcFloor) + __ldg(P + P_anchorGain) * anchor) * mixf(0.55f, 1.0f, pulse) * 1.2f,
+    src = clampf(geo.x * pa[P_logSrc] * (pa[P_srcFloor] + pa[P_anchorGain] * anchor) * mixf(0.55f, 1.0f, pulse) * 1.2f,
                  0.0f, 1.0f) * I;
     src *= 1.0f - geo.z;
   }
   // Gaussian pyrolysis spots (build-defined extension; none by default)
-  const int nSpots = (int)__ldg(E + E_nSpots);
-  if (nSpots > 0 && p.y < __ldg(E + E_spotTop)) {   // above every spot's 4-sigma reach the sum is exactly 0
-    const float spotRef = __ldg(E + E_spotRef);
+  const int nSpots = (int)pa[P_STRIDE + E_nSpots];
+  if (nSpots > 0 && p.y < pa[P_STRIDE + E_spotTop]) {   // above every spot's 4-sigma reach the sum is exactly 0
+    const float spotRef = pa[P_STRIDE + E_spotRef];
     float acc = 0.0f;
     for (int q = 0; q < nSpots; ++q) {
-      const float* sp = E + E_SPOTS + SPOT_STRIDE * q;
-      f3 dd = p - mk3(__ldg(sp + 0), __ldg(sp + 1), __ldg(sp + 2));
-      float sg = __ldg(sp + 3);
+      const int sp = P_STRIDE + E_SPOTS + SPOT_STRIDE * q;
+      f3 dd = p - mk3(pa[sp + 0], pa[sp + 1], pa[sp + 2]);
+      float sg = pa[sp + 3];
       float d2 = dot3(dd, dd);
-      if (d2 < 16.0f * sg * sg) acc += (__ldg(sp + 4) / spotRef) * expf(-d2 / (2.0f * sg * sg));
+      if (d2 < 16.0f * sg * sg) acc += (pa[sp + 4] / spotRef) * expf(-d2 / (2.0f * sg * sg));
     }
     src = fmaxf(src, clampf(acc, 0.0f, 1.0f) * I);
   }
@@ -171,10 +181,10 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
     f3 qb = p * 2.4f + mk3(0.17f, -time * 0.12f, time * 0.05f);
     bed *= sstep(0.0f, 0.3f, noise4(noiseT, qb).y);
   }
-  s.y = fmaxf(s.y, src * __ldg(P + P_fuelSrc));
-  s.y = fmaxf(s.y, bed * __ldg(P + P_bedFuel));
-  s.x = fmaxf(s.x, src * __ldg(P + P_srcTemp));
-  s.x = fmaxf(s.x, bedHot * __ldg(P + P_bedTemp));
+  s.y = fmaxf(s.y, src * pa[P_fuelSrc]);
+  s.y = fmaxf(s.y, bed * pa[P_bedFuel]);
+  s.x = fmaxf(s.x, src * pa[P_srcTemp]);
+  s.x = fmaxf(s.x, bedHot * pa[P_bedTemp]);
   const float srcAll = fmaxf(srcW, bed);
   s2.w = mixf(s2.w, 1.0f, bed * (1.0f - srcW));
   s2.w = mixf(s2.w, 0.0f, srcW);
@@ -184,13 +194,13 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   // pow(1, y) = 1 exactly, so cells without a source skip the pow (here and for the sponge/top factors below)
   const float wsa = clampf(srcW + bed * 0.4f, 0.0f, 1.0f);
   float wsrc = wsa > 0.0f ? 1.0f - powf(1.0f - wsa * 0.5f, dt * 90.0f) : 0.0f;
-  v.y = mixf(v.y, fmaxf(v.y, __ldg(P + P_srcVel)), wsrc);
-  s2.z += geo.x * (1.0f - anchor) * __ldg(P + P_smolder) * dt * I;
+  v.y = mixf(v.y, fmaxf(v.y, pa[P_srcVel]), wsrc);
+  s2.z += geo.x * (1.0f - anchor) * pa[P_smolder] * dt * I;
 
   // ---- burst (src/sim.js:288-296)
-  const float burstAmt = __ldg(P + P_burstAmt);
+  const float burstAmt = pa[P_burstAmt];
   if (burstAmt > 0.0f) {
-    float bd = len3(p - mk3(__ldg(P + P_burstX), __ldg(P + P_burstY), __ldg(P + P_burstZ)));
+    float bd = len3(p - mk3(pa[P_burstX], pa[P_burstY], pa[P_burstZ]));
     float bw = clampf(expf(-bd * bd / 0.006f) * burstAmt, 0.0f, 1.0f);
     s.y = fmaxf(s.y, 0.17f * bw);
     s.x = fmaxf(s.x, 0.9f * bw);
@@ -203,48 +213,48 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   // ---- mixing-limited combustion (src/sim.js:299-309)
   const float T0 = 293.0f + 1000.0f * s.x;
   const float o = clampf(1.0f - s.y - s2.x, 0.0f, 1.0f);
-  const float ignT = __ldg(P + P_ignT), rs = __ldg(P + P_rs);
+  const float ignT = pa[P_ignT], rs = pa[P_rs];
   const float ign = sstep(ignT - 50.0f, ignT + 50.0f, T0);
-  const float b = fminf(s.y, o / rs) * (1.0f - expf(-__ldg(P + P_kMix) * ign * dt));
+  const float b = fminf(s.y, o / rs) * (1.0f - expf(-pa[P_kMix] * ign * dt));
   s.y -= b;
   s2.x = fminf(s2.x + (1.0f + rs) * b, 1.0f);
-  const float dT = fminf(__ldg(P + P_heatOut) * b, fmaxf(2100.0f - T0, 0.0f));
+  const float dT = fminf(pa[P_heatOut] * b, fmaxf(2100.0f - T0, 0.0f));
   float T = T0 + dT;
   const float q = dT / dt;
-  const float phi = geo.z > 0.5f ? 0.0f : fminf(__ldg(P + P_expansion) * q / T, 60.0f);
+  const float phi = geo.z > 0.5f ? 0.0f : fminf(pa[P_expansion] * q / T, 60.0f);
 
   // ---- soot (src/sim.js:312-318); the age gate bounds come from the extension block
-  const float sootOx = __ldg(P + P_sootOx);
+  const float sootOx = pa[P_sootOx];
   ageF = fminf(ageF + dt, 4.0f);
-  s.z += __ldg(P + P_sootForm) * b * sstep(__ldg(E + E_sootAge0), __ldg(E + E_sootAge1), ageF) * sstep(1000.0f, 1400.0f, T) * (1.0f - s2.w);
+  s.z += pa[P_sootForm] * b * sstep(pa[P_STRIDE + E_sootAge0], pa[P_STRIDE + E_sootAge1], ageF) * sstep(1000.0f, 1400.0f, T) * (1.0f - s2.w);
   s.z *= expf(-sootOx * (0.25f + o) * sstep(1100.0f, 1400.0f, T) * dt);
   s.z *= expf(-sootOx * 0.5f * o * sstep(850.0f, 1100.0f, T) * (1.0f - sstep(1100.0f, 1300.0f, T)) * dt);
-  s.z *= __ldg(E + E_decaySoot);   // exp(-sootDissip dt), the same for every cell (host-evaluated)
+  s.z *= pa[P_STRIDE + E_decaySoot];   // exp(-sootDissip dt), the same for every cell (host-evaluated)
 
   // ---- cooling (src/sim.js:321-330)
   const float th = T * 0.001f;
-  T -= fminf(__ldg(P + P_radCool) * 970.0f * s.z * th * th * (th * th * th * th - 0.00737f), 6000.0f) * dt;
+  T -= fminf(pa[P_radCool] * 970.0f * s.z * th * th * (th * th * th * th - 0.00737f), 6000.0f) * dt;
   const float notBurning = 1.0f - sstep(500.0f, 5000.0f, q);
-  T = 293.0f + fmaxf(T - 293.0f, 0.0f) * expf(-__ldg(P + P_coolRate) * notBurning * dt);
+  T = 293.0f + fmaxf(T - 293.0f, 0.0f) * expf(-pa[P_coolRate] * notBurning * dt);
   s.x = (T - 293.0f) * 0.001f;
   s.w = q * 1e-4f;
-  s.y *= __ldg(E + E_decayFuel);    // exp(-fuelDissip dt)
-  s2.x *= __ldg(E + E_decayVit);    // exp(-vitDecay dt)
-  s2.z *= __ldg(E + E_decaySmoke);  // exp(-smokeDissip dt)
+  s.y *= pa[P_STRIDE + E_decayFuel];    // exp(-fuelDissip dt)
+  s2.x *= pa[P_STRIDE + E_decayVit];    // exp(-vitDecay dt)
+  s2.z *= pa[P_STRIDE + E_decaySmoke];  // exp(-smokeDissip dt)
   s2.y = ageF * clampf(s.y + s2.x, 0.0f, 1.0f);
 
   // ---- buoyancy (src/sim.js:333)
-  v.y += __ldg(P + P_buoyancy) * s.x * dt;
+  v.y += pa[P_buoyancy] * s.x * dt;
 
   // ---- hot-gas viscosity (src/sim.js:339-346)
-  const float visc = __ldg(P + P_visc);
+  const float visc = pa[P_visc];
   if (visc > 0.0f) {
     f3 lapV = nb.lap_v();
     float nu = visc * 1.5e-5f * powf(fmaxf(T, 293.0f) / 293.0f, 1.7f);
     v = v + lapV * fminf(nu * dt / (dx * dx), 0.15f);
   }
   // ---- laminar flame base (src/sim.js:350)
-  const float lamAge = __ldg(P + P_lamAge);
+  const float lamAge = pa[P_lamAge];
   const float lam = lamAge > 0.0f ? sstep(0.5f * lamAge, fmaxf(lamAge, 1e-3f), ageF) : 1.0f;
 
   // ---- vorticity confinement (src/sim.js:353-361)
@@ -253,28 +263,28 @@ __device__ __forceinline__ void forces_cell(const float* __restrict__ P, const F
   const float gl = len3(g);
   if (gl > 1e-6f) {
     float gate = sstep(450.0f, 900.0f, T) * (1.0f - srcAll) * sstep(0.02f, 0.08f, p.y) * lam;
-    v = v + cross3(g / gl, xyz(wc)) * (__ldg(P + P_vortEps) * gate) * dt;
+    v = v + cross3(g / gl, xyz(wc)) * (pa[P_vortEps] * gate) * dt;
   }
 
   // ---- sub-grid turbulence: rising, evolving curl noise (src/sim.js:364-368)
-  f3 tq = (p - mk3(0.0f, time * __ldg(P + P_turbRise), 0.0f)) * __ldg(P + P_turbFreq) + mk3(0.0f, 0.0f, time * __ldg(P + P_turbEvolve));
+  f3 tq = (p - mk3(0.0f, time * pa[P_turbRise], 0.0f)) * pa[P_turbFreq] + mk3(0.0f, 0.0f, time * pa[P_turbEvolve]);
   f3 cn = xyz(sample_table(curlT, tq));
   float tgate = fmaxf(sstep(500.0f, 1100.0f, T), sstep(0.0f, 3.0f, s.w)) * (1.0f - srcAll) *
                 mixf(0.6f, 1.8f, sstep(0.2f, 0.75f, p.y)) * lam;
-  v = v + cn * (__ldg(P + P_turbAmp) / 12.0f) * tgate * dt * 10.0f;
+  v = v + cn * (pa[P_turbAmp] / 12.0f) * tgate * dt * 10.0f;
 
   // ---- wind above the logs (src/sim.js:372-375)
-  const float windX = __ldg(P + P_windX), windZ = __ldg(P + P_windZ);
-  const float windK = sstep(0.05f, 0.5f, p.y) * (1.0f + __ldg(P + P_gust));
+  const float windX = pa[P_windX], windZ = pa[P_windZ];
+  const float windK = sstep(0.05f, 0.5f, p.y) * (1.0f + pa[P_gust]);
   v.x += (windX * windK - v.x) * dt * 0.35f * windK;
   v.z += (windZ * windK - v.z) * dt * 0.35f * windK;
-  v = v * __ldg(E + E_decayVel);    // exp(-velDissip dt)
+  v = v * pa[P_STRIDE + E_decayVel];    // exp(-velDissip dt)
 
   // ---- solids & sponge layers (src/sim.js:378-388)
   if (geo.z > 0.5f) { v = mk3(0.0f, 0.0f, 0.0f); s.y = 0.0f; s2.y = 0.0f; }
   f3 fp = mk3((float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f);
   float side = fminf(fminf(fp.x, (float)d.nx - fp.x), fminf(fp.z, (float)d.nz - fp.z));
-  float sp = (1.0f - sstep(0.0f, 5.0f, side)) * __ldg(P + P_sponge);
+  float sp = (1.0f - sstep(0.0f, 5.0f, side)) * pa[P_sponge];
   float wsy = sstep(0.03f, 0.4f, p.y);
   float wSx = windX * wsy, wSz = windZ * wsy;
   const float spc = clampf(sp, 0.0f, 1.0f);
@@ -336,7 +346,7 @@ __global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fie
   if (!id.ok) return;
   GlobalNb<kFusedCurl> nb{f, d, id.i, id.j, id.k};
   const size_t ci = cell(id.i, id.j, id.k, d.nx, d.ny);
-  forces_cell(P, f, noiseT, curlT, d, id.i, id.j, id.k, nb, __ldg(f.SY + ci), __ldg(f.S2Y + ci), __ldg(f.geo + ci));
+  forces_cell(ParamsGlobal{P}, f, noiseT, curlT, d, id.i, id.j, id.k, nb, __ldg(f.SY + ci), __ldg(f.S2Y + ci), __ldg(f.geo + ci));
 }
 
 // ---- z-marching shared-memory variant of curl + forces ----
@@ -402,15 +412,13 @@ __device__ __forceinline__ void curl_plane(float4* dst, float4* vbuf, int zlog, 
     dst[t] = make_float4(w.x, w.y, w.z, len3(w));
   }
 }
-template <int ZD = FZ>   // planes one CTA marches through
-__device__ __forceinline__ void forces_tiled_body(const float* __restrict__ P, const Fields& f, const uint2* __restrict__ noiseT,
-                                                  const uint2* __restrict__ curlT, Dims d, uint3 blk, float4* fsm) {
-  pdl_wait();
-  pdl_trigger();
+// Marches the column tile at (x0, y0) through planes [z0, z1), z1 > z0.
+template <class PA>
+__device__ __forceinline__ void forces_march(const PA& pa, const Fields& f, const uint2* __restrict__ noiseT,
+                                             const uint2* __restrict__ curlT, Dims d, int x0, int y0, int z0, int z1,
+                                             float4* fsm) {
   float4* vbuf = fsm;                    // 5 * VX * VY
   float4* wbuf = fsm + 5 * VX * VY;      // 3 * WX * WY
-  const int x0 = blk.x * FT_X, y0 = blk.y * FT_Y, z0 = blk.z * ZD;
-  const int z1 = min(z0 + ZD, d.nz);
   for (int z = z0 - 2; z <= z0 + 2; ++z) load_vplane(vslot(vbuf, z), f.velY, x0, y0, z, d);
   __syncthreads();
   for (int z = z0 - 1; z <= z0 + 1; ++z) curl_plane(wslot(wbuf, z), vbuf, z, x0, y0, d);
@@ -435,7 +443,7 @@ __device__ __forceinline__ void forces_tiled_body(const float* __restrict__ P, c
       nb.wm = wslot(wbuf, z - 1); nb.w0 = wslot(wbuf, z); nb.wp = wslot(wbuf, z + 1);
       nb.tx = threadIdx.x;
       nb.ty = threadIdx.y;
-      forces_cell(P, f, noiseT, curlT, d, i, j, z, nb, s, s2, g);
+      forces_cell(pa, f, noiseT, curlT, d, i, j, z, nb, s, s2, g);
     }
     if (z + 1 < z1) {
       __syncthreads();                                   // everyone is done with vorticity plane z - 1
@@ -445,6 +453,15 @@ __device__ __forceinline__ void forces_tiled_body(const float* __restrict__ P, c
       __syncthreads();
     }
   }
+}
+// The batched kernel's CTA: column tile (blk.x, blk.y), planes [blk.z * ZD, blk.z * ZD + ZD).
+template <int ZD = FZ>   // planes one CTA marches through
+__device__ __forceinline__ void forces_tiled_body(const float* __restrict__ P, const Fields& f, const uint2* __restrict__ noiseT,
+                                                  const uint2* __restrict__ curlT, Dims d, uint3 blk, float4* fsm) {
+  pdl_wait();
+  pdl_trigger();
+  const int z0 = blk.z * ZD;
+  forces_march(ParamsGlobal{P}, f, noiseT, curlT, d, blk.x * FT_X, blk.y * FT_Y, z0, min(z0 + ZD, d.nz), fsm);
 }
 constexpr size_t FORCES_TILED_SMEM = sizeof(float4) * (5 * VX * VY + 3 * WX * WY);
 
@@ -494,11 +511,37 @@ __device__ __forceinline__ void project_body(const float* __restrict__ P, const 
 // ---------------- per-simulation kernels ----------------
 __global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv1(const float* __restrict__ P, Fields f, Dims d) { adv1_body(P, f, d, blockIdx); }
 __global__ void __launch_bounds__(256, FIRE_ADV_MIN_CTAS) k_adv2(const float* __restrict__ P, Fields f, Dims d) { adv2_body(P, f, d, blockIdx); }
+// One wave of resident CTAs.  The (column tile, plane) units, planes fastest, are split into gridDim.x equal
+// contiguous ranges, so every SM marches the same number of planes (a grid of fixed-depth chunks leaves its
+// last wave partly idle); a range that runs into the next column restarts the march there.
+template <class PA>
+__device__ __forceinline__ void forces_persistent(const PA& pa, const Fields& f, const uint2* __restrict__ noiseT,
+                                                  const uint2* __restrict__ curlT, Dims d, float4* fsm) {
+  pdl_wait();
+  pdl_trigger();
+  const int gx = (d.nx + FT_X - 1) / FT_X, gy = (d.ny + FT_Y - 1) / FT_Y;
+  const long long units = (long long)gx * gy * d.nz;
+  long long u = units * blockIdx.x / gridDim.x;
+  const long long end = units * (blockIdx.x + 1) / gridDim.x;
+  while (u < end) {
+    const int col = (int)(u / d.nz), z0 = (int)(u % d.nz);
+    const int z1 = (int)min((long long)d.nz, z0 + (end - u));
+    forces_march(pa, f, noiseT, curlT, d, (col % gx) * FT_X, (col / gx) * FT_Y, z0, z1, fsm);
+    u += z1 - z0;
+    if (u < end) __syncthreads();   // the next march refills the rings
+  }
+}
 __global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_tiled(const float* __restrict__ P, Fields f,
                                                                                      const uint2* __restrict__ noiseT,
                                                                                      const uint2* __restrict__ curlT, Dims d) {
   extern __shared__ float4 fsm[];
-  forces_tiled_body(P, f, noiseT, curlT, d, blockIdx, fsm);
+  forces_persistent(ParamsGlobal{P}, f, noiseT, curlT, d, fsm);
+}
+__global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_tiled_pb(const __grid_constant__ ParamBlock pb, Fields f,
+                                                                                        const uint2* __restrict__ noiseT,
+                                                                                        const uint2* __restrict__ curlT, Dims d) {
+  extern __shared__ float4 fsm[];
+  forces_persistent(ParamsByValue{pb}, f, noiseT, curlT, d, fsm);
 }
 __global__ void __launch_bounds__(256) k_div(const float* __restrict__ P, const float4* __restrict__ velX, float* __restrict__ b0, Dims d) {
   div_body(P, velX, b0, d, blockIdx);
@@ -569,15 +612,44 @@ template <class F> void with_forces_depth(int v, F&& f) {
 void launch_adv1(const float* P, Fields f, Dims d, cudaStream_t st) { launch_pdl(k_adv1, grid_for(d), block_shape(), 0, st, P, f, d); }
 void launch_adv2(const float* P, Fields f, Dims d, cudaStream_t st) { launch_pdl(k_adv2, grid_for(d), block_shape(), 0, st, P, f, d); }
 void launch_curl(Fields f, Dims d, cudaStream_t st) { launch_pdl(k_curl, grid_for(d), block_shape(), 0, st, f, d); }
+// Resident k_forces_tiled CTAs of each device (CTAs per SM x SMs), set by step_configure.
+constexpr int kMaxDevices = 64;
+static int g_forces_wave[kMaxDevices];
+static dim3 forces_wave_grid(Dims d) {
+  const long long units = (long long)((d.nx + FT_X - 1) / FT_X) * ((d.ny + FT_Y - 1) / FT_Y) * d.nz;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int wave = dev >= 0 && dev < kMaxDevices && g_forces_wave[dev] > 0 ? g_forces_wave[dev] : 4 * 152;
+  return dim3((unsigned)(units < wave ? units : wave));
+}
 void launch_forces(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
-  dim3 g((d.nx + FT_X - 1) / FT_X, (d.ny + FT_Y - 1) / FT_Y, (d.nz + FZ - 1) / FZ);
-  launch_pdl(k_forces_tiled, g, dim3(FT_X, FT_Y), FORCES_TILED_SMEM, st, P, f, noise, curl, d);
+  launch_pdl(k_forces_tiled, forces_wave_grid(d), dim3(FT_X, FT_Y), FORCES_TILED_SMEM, st, P, f, noise, curl, d);
+}
+void launch_forces_pb(const ParamBlock& pb, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
+  launch_pdl(k_forces_tiled_pb, forces_wave_grid(d), dim3(FT_X, FT_Y), FORCES_TILED_SMEM, st, pb, f, noise, curl, d);
+}
+cudaError_t forces_pb_set(cudaGraphExec_t exec, cudaGraphNode_t node, const ParamBlock& pb, Fields f, const uint2* noise,
+                          const uint2* curl, Dims d) {
+  void* args[] = {(void*)&pb, (void*)&f, (void*)&noise, (void*)&curl, (void*)&d};
+  cudaKernelNodeParams kp = {};
+  kp.func = (void*)k_forces_tiled_pb;
+  kp.gridDim = forces_wave_grid(d);
+  kp.blockDim = dim3(FT_X, FT_Y);
+  kp.sharedMemBytes = (unsigned)FORCES_TILED_SMEM;
+  kp.kernelParams = args;
+  return cudaGraphExecKernelNodeSetParams(exec, node, &kp);
 }
 void launch_forces_recompute(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
   launch_pdl(k_forces<true>, grid_for(d), block_shape(), 0, st, P, f, noise, curl, d);
 }
 cudaError_t step_configure() {
   cudaError_t e = cudaFuncSetAttribute(k_forces_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_forces_tiled_pb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
+  int dev = 0, sms = 0, per_sm = 0;
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces_tiled, FT_X * FT_Y, FORCES_TILED_SMEM);
+  if (e == cudaSuccess && dev >= 0 && dev < kMaxDevices) g_forces_wave[dev] = (per_sm > 0 ? per_sm : 1) * sms;
   for (int v = 0; v < FORCES_TILES && e == cudaSuccess; ++v)
     with_forces_depth(v, [&](auto z) {
       e = cudaFuncSetAttribute(k_forces_b<decltype(z)::value>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCES_TILED_SMEM);
