@@ -118,6 +118,14 @@ void fill_block(FireSim* s, float dt, float* out) {
   E[E_decayVit] = std::exp(-P[P_vitDecay] * dt);
   E[E_decaySmoke] = std::exp(-P[P_smokeDissip] * dt);
   E[E_decayVel] = std::exp(-P[P_velDissip] * dt);
+  E[E_turbK] = P[P_turbAmp] / 12.0f;                                        // src/sim.js:368
+  {
+    const float ign0 = P[P_ignT] - 50.0f, ign1 = P[P_ignT] + 50.0f;         // src/sim.js:302
+    const float th0 = P[P_srcThresh] - 0.25f, th1 = P[P_srcThresh] + 0.25f;   // src/sim.js:252
+    E[E_invIgn] = 1.0f / (ign1 - ign0);
+    E[E_invPulse] = 1.0f / (th1 - th0);
+    E[E_invSootAge] = 1.0f / (E[E_sootAge1] - E[E_sootAge0]);
+  }
   float top = -1e30f;
   for (int i = 0; i < (int)E[E_nSpots]; ++i) {
     const float* sp = E + E_SPOTS + SPOT_STRIDE * i;
@@ -872,8 +880,7 @@ int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream) {
   if (!sim || !pinned_out17) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
-  launch_stats(sim->f.S, sim->d, sim->dPartials, sim->dSmall + 2, st);
-  launch_hrr(sim->f.S, sim->d, (float)sim->dx, sim->dPartials, sim->dSmall + 18, st);   // reuses the partials after stats
+  launch_diag(sim->f.S, sim->d, (float)sim->dx, sim->dPartials, sim->dSmall + 2, st);   // dSmall[2..18]
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(pinned_out17, sim->dSmall + 2, 17 * sizeof(double), cudaMemcpyDeviceToHost, st));
   return FIRE_OK;

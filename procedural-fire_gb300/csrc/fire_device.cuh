@@ -17,11 +17,13 @@ __device__ __forceinline__ float mixf(float a, float b, float t) { return a * (1
 // smoothstep with t = (x - e0) * (1 / (e1 - e0)): the reciprocal folds to a constant for literal edges, so
 // the ~15 smoothsteps per cell cost no division (well inside WGSL's smoothstep accuracy; the oracle uses
 // the same formula).
-__device__ __forceinline__ float sstep(float e0, float e1, float x) {
-  const float inv = 1.0f / (e1 - e0);
+// sstep_inv takes the reciprocal precomputed: for edges that are per-step parameters the host evaluates
+// 1 / (e1 - e0) once, in the same FP32 operations, so the result is the same bit for bit.
+__device__ __forceinline__ float sstep_inv(float e0, float inv, float x) {
   float t = clampf((x - e0) * inv, 0.0f, 1.0f);
   return t * t * (3.0f - 2.0f * t);
 }
+__device__ __forceinline__ float sstep(float e0, float e1, float x) { return sstep_inv(e0, 1.0f / (e1 - e0), x); }
 
 // ---- double-float ("df64") accumulation: value = hi + lo with |lo| <= ulp(hi)/2 ----
 // GB300 executes FP64 on a slow path, so every cross-thread reduction accumulates in pairs of FP32 with

@@ -22,12 +22,16 @@ constexpr int P_STRIDE = 64;
 // Extension block appended after the 64-float parameter block (no counterpart in the reference): the soot
 // age gate, coal-bed gain and spots, plus per-step constants the host derives from the uniforms: the five
 // decay factors exp(-k dt) that are the same for every cell (src/sim.js:318, 327-329, 375; computed with the
-// same expf the oracle uses) and the height above which no spot contributes (max spot y + 4 sigma).
+// same expf the oracle uses), the height above which no spot contributes (max spot y + 4 sigma), and the
+// uniform divisions of the forces physics (turbAmp / 12 and the reciprocals 1 / (e1 - e0) of the smoothsteps
+// whose edges are parameters: ignition, source pulse, soot age), in the FP32 operations the kernel would use.
 enum ExtIndex {
   E_sootAge0 = 0, E_sootAge1, E_bedGain, E_nSpots, E_spotRef, E_spotTop,
   E_decaySoot, E_decayFuel, E_decayVit, E_decaySmoke, E_decayVel,
+  E_turbK, E_invIgn, E_invPulse, E_invSootAge,
   E_SPOTS = 16
 };
+static_assert(E_invSootAge < E_SPOTS, "per-step constants fit before the spot table");
 constexpr int MAX_SPOTS = 16;
 constexpr int SPOT_STRIDE = 8;
 constexpr int E_COUNT = E_SPOTS + MAX_SPOTS * SPOT_STRIDE;   // 144
@@ -173,5 +177,7 @@ void launch_residual(const MGLevel& L, double* partials, double* out2, cudaStrea
 int stats_partials_count(Dims d);
 void launch_stats(const float4* f, Dims d, double* partials, double* out16, cudaStream_t st);
 void launch_hrr(const float4* S, Dims d, float dx, double* partials, double* out1, cudaStream_t st);
+// launch_stats of S and launch_hrr in one pass over S (same results); out17 = the 16 stats, then the heat release.
+void launch_diag(const float4* S, Dims d, float dx, double* partials, double* out17, cudaStream_t st);
 
 }  // namespace fire

@@ -116,6 +116,78 @@ __global__ void __launch_bounds__(SB) k_hrr_final(const df64* __restrict__ parti
   }
 }
 
+// fire_sim_stats_async's diagnostics in one pass over S: the stats of S (as k_stats) and the heat release
+// (as k_hrr) from the same loads.  Per thread, per CTA and in the final merge every sum runs in the order of
+// k_stats / k_stats_final and k_hrr / k_hrr_final, so the results are those kernels' bit for bit.
+__global__ void __launch_bounds__(SB) k_diag(const float4* __restrict__ S, long long n, ChanPart* __restrict__ cparts,
+                                             df64* __restrict__ hparts) {
+  __shared__ ChanPart sh[SB / 32];
+  __shared__ df64 shh[SB / 32];
+  ChanPart c[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { c[k].mn = INFINITY; c[k].mx = -INFINITY; c[k].sum = df_make(0.0f); c[k].bad = 0; }
+  float sm[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  float acc = 0.0f;
+  for (long long t = (long long)blockIdx.x * SB + threadIdx.x; t < n; t += (long long)gridDim.x * SB) {
+    const float4 v = __ldg(S + t);
+    const float a[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (!isfinite(a[k])) { c[k].bad += 1; continue; }
+      c[k].mn = fminf(c[k].mn, a[k]);
+      c[k].mx = fmaxf(c[k].mx, a[k]);
+      sm[k] += a[k];
+    }
+    const float q = v.w * 1e4f;
+    if (q > 0.0f) acc += q / (293.0f + 1000.0f * v.x);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    c[k].sum = df_make(sm[k]);
+    ChanPart r = cp_block(c[k], sh);
+    if (threadIdx.x == 0) cparts[4 * (size_t)blockIdx.x + k] = r;
+  }
+  df64 h = df_warp_sum(df_make(acc));
+  if ((threadIdx.x & 31) == 0) shh[threadIdx.x >> 5] = h;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    h = df_warp_sum(threadIdx.x < SB / 32 ? shh[threadIdx.x] : df_make(0.0f));
+    if (threadIdx.x == 0) hparts[blockIdx.x] = h;
+  }
+}
+// out17 = 4 x (min, max, mean, bad) of S, then the heat release (kW).
+__global__ void __launch_bounds__(SB) k_diag_final(const ChanPart* __restrict__ cparts, const df64* __restrict__ hparts, int count,
+                                                   long long n, double scale, double* __restrict__ out17) {
+  __shared__ ChanPart sh[SB / 32];
+  __shared__ df64 shh[SB / 32];
+  ChanPart v[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { v[k].mn = INFINITY; v[k].mx = -INFINITY; v[k].sum = df_make(0.0f); v[k].bad = 0; }
+  df64 h = df_make(0.0f);
+  for (int i = threadIdx.x; i < count; i += SB) {   // each channel's merge runs in k_stats_final's order
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = cp_merge(v[k], cparts[4 * (size_t)i + k]);
+    h = df_add(h, hparts[i]);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const ChanPart r = cp_block(v[k], sh);
+    if (threadIdx.x == 0) {
+      out17[4 * k + 0] = r.mn;
+      out17[4 * k + 1] = r.mx;
+      out17[4 * k + 2] = df_to_double(r.sum) / (double)n;
+      out17[4 * k + 3] = (double)r.bad;
+    }
+  }
+  h = df_warp_sum(h);
+  if ((threadIdx.x & 31) == 0) shh[threadIdx.x >> 5] = h;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    h = df_warp_sum(threadIdx.x < SB / 32 ? shh[threadIdx.x] : df_make(0.0f));
+    if (threadIdx.x == 0) out17[16] = df_to_double(h) * scale;
+  }
+}
+
 int stats_partials_count(Dims d) {
   long long n = (long long)d.nx * d.ny * d.nz;
   long long b = (n + SB - 1) / SB;
@@ -129,6 +201,18 @@ void launch_stats(const float4* f, Dims d, double* partials, double* out16, cuda
   ChanPart* part = reinterpret_cast<ChanPart*>(partials);
   k_stats<<<nb, SB, 0, st>>>(f, n, part);
   k_stats_final<<<1, SB, 0, st>>>(part, nb, n, out16);
+}
+// `partials`: the stats partials (80 bytes per CTA) followed by the heat-release partials (8 bytes per CTA).
+void launch_diag(const float4* S, Dims d, float dx, double* partials, double* out17, cudaStream_t st) {
+  long long n = (long long)d.nx * d.ny * d.nz;
+  int nb = stats_partials_count(d);
+  double vol = (double)dx * (double)dx * (double)dx;
+  ChanPart* cpart = reinterpret_cast<ChanPart*>(partials);
+  df64* hpart = reinterpret_cast<df64*>(cpart + 4 * (size_t)nb);
+  static_assert(sizeof(ChanPart) * 4 + sizeof(df64) <= 128 && sizeof(ChanPart) * 4 % alignof(df64) == 0,
+                "diagnostics partials fit the scratch stride");
+  k_diag<<<nb, SB, 0, st>>>(S, n, cpart, hpart);
+  k_diag_final<<<1, SB, 0, st>>>(cpart, hpart, nb, n, 354800.0 * vol * 1e-3, out17);   // W -> kW
 }
 void launch_hrr(const float4* S, Dims d, float dx, double* partials, double* out1, cudaStream_t st) {
   long long n = (long long)d.nx * d.ny * d.nz;

@@ -155,7 +155,7 @@ __device__ __forceinline__ void forces_cell(const PA& pa, const Fields& f, const
     anchor = sstep(-0.05f, 0.25f, noise4(noiseT, qa).z);
     f3 qn = p * (pa[P_srcFreq] * 0.06f) + mk3(seed * 0.131f, 0.0f, time * pa[P_srcSpeed]);
     const float th = pa[P_srcThresh];
-    float pulse = sstep(th - 0.25f, th + 0.25f, noise4(noiseT, qn).x);
+    float pulse = sstep_inv(th - 0.25f, pa[P_STRIDE + E_invPulse], noise4(noiseT, qn).x);
     src = clampf(geo.x * pa[P_logSrc] * (pa[P_srcFloor] + pa[P_anchorGain] * anchor) * mixf(0.55f, 1.0f, pulse) * 1.2f,
                  0.0f, 1.0f) * I;
     src *= 1.0f - geo.z;
@@ -214,7 +214,7 @@ __device__ __forceinline__ void forces_cell(const PA& pa, const Fields& f, const
   const float T0 = 293.0f + 1000.0f * s.x;
   const float o = clampf(1.0f - s.y - s2.x, 0.0f, 1.0f);
   const float ignT = pa[P_ignT], rs = pa[P_rs];
-  const float ign = sstep(ignT - 50.0f, ignT + 50.0f, T0);
+  const float ign = sstep_inv(ignT - 50.0f, pa[P_STRIDE + E_invIgn], T0);
   const float b = fminf(s.y, o / rs) * (1.0f - expf(-pa[P_kMix] * ign * dt));
   s.y -= b;
   s2.x = fminf(s2.x + (1.0f + rs) * b, 1.0f);
@@ -226,7 +226,7 @@ __device__ __forceinline__ void forces_cell(const PA& pa, const Fields& f, const
   // ---- soot (src/sim.js:312-318); the age gate bounds come from the extension block
   const float sootOx = pa[P_sootOx];
   ageF = fminf(ageF + dt, 4.0f);
-  s.z += pa[P_sootForm] * b * sstep(pa[P_STRIDE + E_sootAge0], pa[P_STRIDE + E_sootAge1], ageF) * sstep(1000.0f, 1400.0f, T) * (1.0f - s2.w);
+  s.z += pa[P_sootForm] * b * sstep_inv(pa[P_STRIDE + E_sootAge0], pa[P_STRIDE + E_invSootAge], ageF) * sstep(1000.0f, 1400.0f, T) * (1.0f - s2.w);
   s.z *= expf(-sootOx * (0.25f + o) * sstep(1100.0f, 1400.0f, T) * dt);
   s.z *= expf(-sootOx * 0.5f * o * sstep(850.0f, 1100.0f, T) * (1.0f - sstep(1100.0f, 1300.0f, T)) * dt);
   s.z *= pa[P_STRIDE + E_decaySoot];   // exp(-sootDissip dt), the same for every cell (host-evaluated)
@@ -271,7 +271,7 @@ __device__ __forceinline__ void forces_cell(const PA& pa, const Fields& f, const
   f3 cn = xyz(sample_table(curlT, tq));
   float tgate = fmaxf(sstep(500.0f, 1100.0f, T), sstep(0.0f, 3.0f, s.w)) * (1.0f - srcAll) *
                 mixf(0.6f, 1.8f, sstep(0.2f, 0.75f, p.y)) * lam;
-  v = v + cn * (pa[P_turbAmp] / 12.0f) * tgate * dt * 10.0f;
+  v = v + cn * pa[P_STRIDE + E_turbK] * tgate * dt * 10.0f;   // E_turbK = turbAmp / 12
 
   // ---- wind above the logs (src/sim.js:372-375)
   const float windX = pa[P_windX], windZ = pa[P_windZ];

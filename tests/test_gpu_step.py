@@ -170,6 +170,14 @@ def test_stats_and_hrr_match_numpy(campfire):
     assert sim.hrr() == pytest.approx(want, rel=1e-5)
     # deterministic: the same reduction twice gives identical bits
     assert sim.stats("S") == st and sim.hrr() == sim.hrr()
+    # the one-pass form behind fire_sim_stats_async gives the same bits as the two reductions
+    import torch
+    pinned = torch.zeros(17, dtype=torch.float64, pin_memory=True)
+    sim.stats_async(pinned.data_ptr())
+    sim.sync()
+    got = pinned.numpy().copy()
+    want17 = [v for c in st for v in (c["min"], c["max"], c["mean"], float(c["bad"]))] + [sim.hrr()]
+    assert got.tolist() == want17
 
 
 def test_residual_driven_solve(campfire):
