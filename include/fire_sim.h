@@ -223,6 +223,14 @@ int fire_sim_hrr(FireSim* sim, double* q_kw, void* stream);
  * out[0..15] = S stats as in fire_sim_stats, out[16] = heat release (kW).  The values are valid once
  * `stream` has reached this point (fire_sim_sync or a stream/event wait).                          */
 int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream);
+/* FIRE.profile's height profile (src/main.js:322-340): for rows j = 0, 4, 8, ... of y, over the x-z plane
+ * of S, with T = 293 + 1000 S.x: h = (j + 0.5) dx, the mean T of the centreline cells (|i - nx/2| < 3 and
+ * |k - nz/2| < 3), the maximum T (from 0), the maximum soot S.z and fuel S.y (from 0) and the count of
+ * cells above 1000 K.  rows6 receives n = ceil(ny / 4) rows of 6 doubles (h, Tc, Tmax, soot, fuel, hot);
+ * FIRE_ERR_BAD_ARG if max_rows < n.  T, Tc and the comparisons are FP64 like the reference's JS; the
+ * reference rounds the values for display (Tc, Tmax to integers, h, soot, fuel to 0.01), this does not.
+ * Synchronous.                                                                                      */
+int fire_sim_height_profile(FireSim* sim, double* rows6, int max_rows, int* n_rows, void* stream);
 
 /* ---- scene helpers (src/scene.js) ------------------------------------------------------------- */
 /* buildCampfire(seed) + packLogs (src/scene.js:13-42, 92-98): writes max_logs*8 floats (8 real logs,

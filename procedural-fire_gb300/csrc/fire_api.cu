@@ -876,6 +876,23 @@ int fire_sim_hrr(FireSim* sim, double* q_kw, void* stream) {
   *q_kw = sim->hSmall[18];
   return FIRE_OK;
 }
+int fire_sim_height_profile(FireSim* sim, double* rows6, int max_rows, int* n_rows, void* stream) {
+  if (!sim || !rows6 || !n_rows) return FIRE_ERR_BAD_ARG;
+  const int n = height_profile_rows(sim->d);
+  *n_rows = n;
+  if (max_rows < n) return set_err(sim, FIRE_ERR_BAD_ARG, "height profile needs %d rows", n);
+  CK(cudaSetDevice(sim->device));
+  cudaStream_t st = as_stream(stream);
+  double* d = nullptr;
+  CK(cudaMallocAsync(&d, sizeof(double) * 6 * (size_t)n, st));
+  launch_height_profile(sim->f.S, sim->d, sim->dx, d, st);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rows6, d, sizeof(double) * 6 * (size_t)n, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(d, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return set_err(sim, FIRE_ERR_CUDA, "height profile: %s", cudaGetErrorString(e));
+  return FIRE_OK;
+}
 int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream) {
   if (!sim || !pinned_out17) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));

@@ -177,6 +177,9 @@ void launch_residual(const MGLevel& L, double* partials, double* out2, cudaStrea
 int stats_partials_count(Dims d);
 void launch_stats(const float4* f, Dims d, double* partials, double* out16, cudaStream_t st);
 void launch_hrr(const float4* S, Dims d, float dx, double* partials, double* out1, cudaStream_t st);
+// FIRE.profile's height profile rows (6 doubles each, height_profile_rows of them) into device memory.
+int height_profile_rows(Dims d);
+void launch_height_profile(const float4* S, Dims d, double dx, double* rows6, cudaStream_t st);
 // launch_stats of S and launch_hrr in one pass over S (same results); out17 = the 16 stats, then the heat release.
 void launch_diag(const float4* S, Dims d, float dx, double* partials, double* out17, cudaStream_t st);
 

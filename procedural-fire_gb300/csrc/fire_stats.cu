@@ -188,6 +188,56 @@ __global__ void __launch_bounds__(SB) k_diag_final(const ChanPart* __restrict__ 
   }
 }
 
+// FIRE.profile's rows (src/main.js:322-340): one CTA per profile row j = 4 * blockIdx.x.  Threads stride over
+// the x-z plane of that row (x fastest, coalesced); T in FP64 as the reference's JS computes it; maxima are
+// exact; the centreline sum runs per thread in cell order and then through a fixed warp/block tree.
+__global__ void __launch_bounds__(SB) k_height_profile(const float4* __restrict__ S, int nx, int ny, int nz, double dx,
+                                                       double* __restrict__ rows6) {
+  __shared__ double s_tmax[SB / 32], s_tc[SB / 32];
+  __shared__ float s_soot[SB / 32], s_fuel[SB / 32];
+  __shared__ int s_hot[SB / 32], s_nc[SB / 32];
+  const int j = 4 * blockIdx.x;
+  double tmax = 0.0, tc = 0.0;
+  float soot = 0.0f, fuel = 0.0f;
+  int hot = 0, nc = 0;
+  const double cx = nx / 2.0, cz = nz / 2.0;
+  const long long plane = (long long)nx * nz;
+  for (long long t = threadIdx.x; t < plane; t += SB) {
+    const int i = (int)(t % nx), k = (int)(t / nx);
+    const float4 s = __ldg(S + i + (size_t)nx * ((size_t)j + (size_t)ny * k));
+    const double T = 293.0 + 1000.0 * (double)s.x;
+    tmax = fmax(tmax, T);
+    soot = fmaxf(soot, s.z);
+    fuel = fmaxf(fuel, s.y);
+    if (T > 1000.0) hot += 1;
+    if (fabs(i - cx) < 3.0 && fabs(k - cz) < 3.0) { tc += T; nc += 1; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    tmax = fmax(tmax, __shfl_down_sync(0xffffffffu, tmax, o));
+    tc += __shfl_down_sync(0xffffffffu, tc, o);
+    soot = fmaxf(soot, __shfl_down_sync(0xffffffffu, soot, o));
+    fuel = fmaxf(fuel, __shfl_down_sync(0xffffffffu, fuel, o));
+    hot += __shfl_down_sync(0xffffffffu, hot, o);
+    nc += __shfl_down_sync(0xffffffffu, nc, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { s_tmax[w] = tmax; s_tc[w] = tc; s_soot[w] = soot; s_fuel[w] = fuel; s_hot[w] = hot; s_nc[w] = nc; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < SB / 32; ++q) {
+      tmax = fmax(tmax, s_tmax[q]); tc += s_tc[q]; soot = fmaxf(soot, s_soot[q]); fuel = fmaxf(fuel, s_fuel[q]);
+      hot += s_hot[q]; nc += s_nc[q];
+    }
+    double* r = rows6 + 6 * (size_t)blockIdx.x;
+    r[0] = (j + 0.5) * dx;
+    r[1] = tc / nc;   // nc > 0: the centreline window always holds a cell
+    r[2] = tmax;
+    r[3] = soot;
+    r[4] = fuel;
+    r[5] = hot;
+  }
+}
+
 int stats_partials_count(Dims d) {
   long long n = (long long)d.nx * d.ny * d.nz;
   long long b = (n + SB - 1) / SB;
@@ -201,6 +251,10 @@ void launch_stats(const float4* f, Dims d, double* partials, double* out16, cuda
   ChanPart* part = reinterpret_cast<ChanPart*>(partials);
   k_stats<<<nb, SB, 0, st>>>(f, n, part);
   k_stats_final<<<1, SB, 0, st>>>(part, nb, n, out16);
+}
+int height_profile_rows(Dims d) { return (d.ny + 3) / 4; }
+void launch_height_profile(const float4* S, Dims d, double dx, double* rows6, cudaStream_t st) {
+  k_height_profile<<<height_profile_rows(d), SB, 0, st>>>(S, d.nx, d.ny, d.nz, dx, rows6);
 }
 // `partials`: the stats partials (80 bytes per CTA) followed by the heat-release partials (8 bytes per CTA).
 void launch_diag(const float4* S, Dims d, float dx, double* partials, double* out17, cudaStream_t st) {

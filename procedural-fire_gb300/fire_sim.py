@@ -102,6 +102,7 @@ _SIGS = {
     "fire_sim_stats": (_ip, [_vp, _ip, _vp, _vp]),
     "fire_sim_hrr": (_ip, [_vp, ctypes.POINTER(_dp), _vp]),
     "fire_sim_stats_async": (_ip, [_vp, _vp, _vp]),
+    "fire_sim_height_profile": (_ip, [_vp, ctypes.POINTER(_dp), _ip, ctypes.POINTER(_ip), _vp]),
     "fire_build_campfire": (_ip, [ctypes.c_uint32, _vp, _ip]),
     "fire_make_spots": (_ip, [ctypes.c_uint32, _ip, _fp, _fp, _fp, _fp, _vp]),
     "fire_poisson_vcycles_noalloc": (_ip, [_vp, _vp, _ip, _ip, _ip, _fp, _ip, _vp]),
@@ -464,6 +465,30 @@ class FireSim:
     def stats_async(self, out_ptr: int, stream=None):
         """Queues S stats + heat release into a pinned host buffer of 17 doubles (no wait)."""
         self._check(self._lib.fire_sim_stats_async(self._h, ctypes.c_void_p(out_ptr), _stream_handle(stream)), "stats_async")
+
+    def height_profile(self, stream=None) -> np.ndarray:
+        """Rows (h, Tc, Tmax, soot, fuel, hot) for y rows 0, 4, 8, ... (src/main.js:322-340), unrounded."""
+        n = (self.res[1] + 3) // 4
+        out = np.zeros((n, 6), np.float64)
+        got = ctypes.c_int()
+        self._check(self._lib.fire_sim_height_profile(self._h, _ptr(out), n, ctypes.byref(got), _stream_handle(stream)),
+                    "height_profile")
+        return out[:got.value]
+
+    def profile(self, stream=None) -> dict:
+        """FIRE.profile (src/main.js:320-353): heat release and the height profile, rounded for display as the
+        reference does (toFixed / Math.round on the exact binary values, ties rounded up)."""
+        from decimal import Decimal, ROUND_HALF_UP
+
+        def fixed(x: float, places: str) -> float:
+            return float(Decimal(x).quantize(Decimal(places), rounding=ROUND_HALF_UP))
+
+        def js_round(x: float) -> int:
+            return int(np.floor(x + 0.5))
+
+        rows = [{"h": fixed(r[0], "0.01"), "Tc": js_round(r[1]), "Tmax": js_round(r[2]), "soot": fixed(r[3], "0.01"),
+                 "fuel": fixed(r[4], "0.01"), "hotCells": int(r[5])} for r in self.height_profile(stream)]
+        return {"Q_kW": fixed(self.hrr(stream), "0.1"), "rows": rows}
 
 
 # ---------------------------------------------------------------------------------------------------

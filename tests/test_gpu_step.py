@@ -180,6 +180,30 @@ def test_stats_and_hrr_match_numpy(campfire):
     assert got.tolist() == want17
 
 
+def test_height_profile_matches_numpy(campfire):
+    """FIRE.profile's rows (src/main.js:322-340) restated in numpy on the downloaded S field."""
+    sim = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=2)
+    sim.step(FC.C1["dt"], 30)
+    nx, ny, nz = sim.res
+    S = sim.download("S").astype(np.float64).reshape(nz, ny, nx, 4)
+    rows = sim.height_profile()
+    assert rows.shape == ((ny + 3) // 4, 6)
+    i = np.arange(nx)[None, :]
+    k = np.arange(nz)[:, None]
+    centre = (np.abs(i - nx / 2) < 3) & (np.abs(k - nz / 2) < 3)
+    for r, j in zip(rows, range(0, ny, 4)):
+        T = 293.0 + 1000.0 * S[:, j, :, 0]
+        assert r[0] == pytest.approx((j + 0.5) * sim.dx, rel=1e-6)   # FP64 dx in the kernel, FP32 in FireInfo
+        assert r[1] == pytest.approx(T[centre].mean(), rel=1e-13)
+        assert r[2] == max(0.0, T.max())
+        assert r[3] == max(0.0, S[:, j, :, 2].max()) and r[4] == max(0.0, S[:, j, :, 1].max())
+        assert r[5] == int((T > 1000.0).sum())
+    assert rows[:, 2].max() > 1000.0   # a burning fire has hot rows
+    prof = sim.profile()
+    assert len(prof["rows"]) == len(rows) and prof["Q_kW"] == pytest.approx(sim.hrr(), abs=0.051)
+    assert prof["rows"][0]["Tmax"] == int(np.floor(rows[0, 2] + 0.5))
+
+
 def test_residual_driven_solve(campfire):
     sim = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=4, mg_max_cycles=12, mg_tol=1e-4)
     # step by step: the first cycles of a step may skip the convergence test (predicted from the previous
