@@ -102,7 +102,7 @@ _SIGS = {
     "fire_sim_stats": (_ip, [_vp, _ip, _vp, _vp]),
     "fire_sim_hrr": (_ip, [_vp, ctypes.POINTER(_dp), _vp]),
     "fire_sim_stats_async": (_ip, [_vp, _vp, _vp]),
-    "fire_sim_height_profile": (_ip, [_vp, ctypes.POINTER(_dp), _ip, ctypes.POINTER(_ip), _vp]),
+    "fire_sim_height_profile": (_ip, [_vp, _vp, _ip, ctypes.POINTER(_ip), _vp]),
     "fire_build_campfire": (_ip, [ctypes.c_uint32, _vp, _ip]),
     "fire_make_spots": (_ip, [ctypes.c_uint32, _ip, _fp, _fp, _fp, _fp, _vp]),
     "fire_poisson_vcycles_noalloc": (_ip, [_vp, _vp, _ip, _ip, _ip, _fp, _ip, _vp]),
