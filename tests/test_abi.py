@@ -74,6 +74,9 @@ def test_argument_checks_without_device():
     cfg.size[:] = [1, 1, 1]
     h = ctypes.c_void_p()
     assert lib.fire_sim_create(ctypes.byref(cfg), None, 0, ctypes.byref(h)) == 1
+    cfg.res[:] = [2048, 1024, 1024]  # 2^31 cells: beyond the kernels' 32-bit cell offsets
+    assert lib.fire_sim_create(ctypes.byref(cfg), None, 0, ctypes.byref(h)) == 1
+    cfg.res[:] = [1, 8, 8]
     assert lib.fire_sim_create(None, None, 0, ctypes.byref(h)) == 1
     for fn in ("fire_sim_step", "fire_sim_reset", "fire_sim_sync"):
         args = {"fire_sim_step": (None, 0.01, 1, None)}.get(fn, (None,))
