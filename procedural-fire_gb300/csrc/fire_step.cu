@@ -257,21 +257,25 @@ __device__ __forceinline__ void forces_cell(const PA& pa, const Fields& f, const
   const float lamAge = pa[P_lamAge];
   const float lam = lamAge > 0.0f ? sstep(0.5f * lamAge, fmaxf(lamAge, 1e-3f), ageF) : 1.0f;
 
-  // ---- vorticity confinement (src/sim.js:353-361)
-  const float4 wc = nb.vort_center();
-  const f3 g = nb.grad_w();
-  const float gl = len3(g);
-  if (gl > 1e-6f) {
-    float gate = sstep(450.0f, 900.0f, T) * (1.0f - srcAll) * sstep(0.02f, 0.08f, p.y) * lam;
-    v = v + cross3(g / gl, xyz(wc)) * (pa[P_vortEps] * gate) * dt;
+  // ---- vorticity confinement (src/sim.js:353-361).  Where the gate is exactly 0 (gas below 450 K, the
+  // sources, the floor layer) the increment is a signed zero, so it is skipped; only the sign of a zero
+  // velocity component can differ.
+  const float gate = sstep(450.0f, 900.0f, T) * (1.0f - srcAll) * sstep(0.02f, 0.08f, p.y) * lam;
+  if (gate != 0.0f) {
+    const f3 g = nb.grad_w();
+    const float gl = len3(g);
+    if (gl > 1e-6f) v = v + cross3(g / gl, xyz(nb.vort_center())) * (pa[P_vortEps] * gate) * dt;
   }
 
-  // ---- sub-grid turbulence: rising, evolving curl noise (src/sim.js:364-368)
-  f3 tq = (p - mk3(0.0f, time * pa[P_turbRise], 0.0f)) * pa[P_turbFreq] + mk3(0.0f, 0.0f, time * pa[P_turbEvolve]);
-  f3 cn = xyz(sample_table(curlT, tq));
-  float tgate = fmaxf(sstep(500.0f, 1100.0f, T), sstep(0.0f, 3.0f, s.w)) * (1.0f - srcAll) *
-                mixf(0.6f, 1.8f, sstep(0.2f, 0.75f, p.y)) * lam;
-  v = v + cn * pa[P_STRIDE + E_turbK] * tgate * dt * 10.0f;   // E_turbK = turbAmp / 12
+  // ---- sub-grid turbulence: rising, evolving curl noise (src/sim.js:364-368); skipped the same way where
+  // its gate is exactly 0 (below 500 K with no heat release: most of the domain), which saves the table sample
+  const float tgate = fmaxf(sstep(500.0f, 1100.0f, T), sstep(0.0f, 3.0f, s.w)) * (1.0f - srcAll) *
+                      mixf(0.6f, 1.8f, sstep(0.2f, 0.75f, p.y)) * lam;
+  if (tgate != 0.0f) {
+    f3 tq = (p - mk3(0.0f, time * pa[P_turbRise], 0.0f)) * pa[P_turbFreq] + mk3(0.0f, 0.0f, time * pa[P_turbEvolve]);
+    f3 cn = xyz(sample_table(curlT, tq));
+    v = v + cn * pa[P_STRIDE + E_turbK] * tgate * dt * 10.0f;   // E_turbK = turbAmp / 12
+  }
 
   // ---- wind above the logs (src/sim.js:372-375)
   const float windX = pa[P_windX], windZ = pa[P_windZ];

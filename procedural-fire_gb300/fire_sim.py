@@ -475,7 +475,7 @@ class FireSim:
                     "height_profile")
         return out[:got.value]
 
-    def profile(self, stream=None) -> dict:
+    def fire_profile(self, stream=None) -> dict:
         """FIRE.profile (src/main.js:320-353): heat release and the height profile, rounded for display as the
         reference does (toFixed / Math.round on the exact binary values, ties rounded up)."""
         from decimal import Decimal, ROUND_HALF_UP

@@ -67,6 +67,18 @@ def test_make_spots_deterministic_and_in_disc():
         F.make_spots(5, 17)
 
 
+def test_host_classes_define_each_method_once():
+    """A second definition of a method name silently replaces the first (a FIRE.profile mirror named `profile`
+    would hide the per-stage timing switch `profile(enable)` that bench.py uses)."""
+    import ast
+    import collections
+    src = (Path(F.__file__)).read_text()
+    for node in ast.walk(ast.parse(src)):
+        if isinstance(node, ast.ClassDef):
+            names = collections.Counter(n.name for n in node.body if isinstance(n, ast.FunctionDef))
+            assert not [k for k, v in names.items() if v > 1], (node.name, names)
+
+
 def test_argument_checks_without_device():
     lib = F.load_library()
     cfg = F.FireConfig()

@@ -199,9 +199,25 @@ def test_height_profile_matches_numpy(campfire):
         assert r[3] == max(0.0, S[:, j, :, 2].max()) and r[4] == max(0.0, S[:, j, :, 1].max())
         assert r[5] == int((T > 1000.0).sum())
     assert rows[:, 2].max() > 1000.0   # a burning fire has hot rows
-    prof = sim.profile()
+    prof = sim.fire_profile()
     assert len(prof["rows"]) == len(rows) and prof["Q_kW"] == pytest.approx(sim.hrr(), abs=0.051)
     assert prof["rows"][0]["Tmax"] == int(np.floor(rows[0, 2] + 0.5))
+
+
+def test_stage_times_profiled_graph(campfire):
+    """Profiler / profileStages (src/gpu.js:128-171): per-stage times from event nodes in the step graph; the
+    profiled graph computes the same step as the plain one."""
+    a = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=2)
+    b = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=2)
+    a.step(FC.C1["dt"], 3)
+    b.profile(True)
+    b.step(FC.C1["dt"], 3)
+    st = b.stage_times()
+    b.profile(False)
+    assert {"adv1", "adv2", "forces", "div", "vcycle", "project"} <= set(st)
+    assert all(st[k] > 0 for k in ("adv1", "adv2", "forces", "div", "vcycle", "project"))
+    a.sync(); b.sync()
+    np.testing.assert_array_equal(a.download("S"), b.download("S"))
 
 
 def test_residual_driven_solve(campfire):
