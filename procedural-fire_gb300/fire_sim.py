@@ -477,18 +477,23 @@ class FireSim:
 
     def fire_profile(self, stream=None) -> dict:
         """FIRE.profile (src/main.js:320-353): heat release and the height profile, rounded for display as the
-        reference does (toFixed / Math.round on the exact binary values, ties rounded up)."""
-        from decimal import Decimal, ROUND_HALF_UP
+        reference does (`+x.toFixed(n)` and `Math.round`)."""
+        rows = [{"h": js_to_fixed(r[0], 2), "Tc": js_round(r[1]), "Tmax": js_round(r[2]), "soot": js_to_fixed(r[3], 2),
+                 "fuel": js_to_fixed(r[4], 2), "hotCells": int(r[5])} for r in self.height_profile(stream)]
+        return {"Q_kW": js_to_fixed(self.hrr(stream), 1), "rows": rows}
 
-        def fixed(x: float, places: str) -> float:
-            return float(Decimal(x).quantize(Decimal(places), rounding=ROUND_HALF_UP))
 
-        def js_round(x: float) -> int:
-            return int(np.floor(x + 0.5))
+def js_to_fixed(x: float, digits: int) -> float:
+    """JavaScript's `+x.toFixed(digits)`: the decimal nearest the exact binary value of x, a tie going to the
+    larger magnitude (Number.prototype.toFixed, ECMA-262), read back as a double."""
+    from decimal import Decimal, ROUND_HALF_UP
+    return float(Decimal(x).quantize(Decimal(1).scaleb(-digits), rounding=ROUND_HALF_UP))
 
-        rows = [{"h": fixed(r[0], "0.01"), "Tc": js_round(r[1]), "Tmax": js_round(r[2]), "soot": fixed(r[3], "0.01"),
-                 "fuel": fixed(r[4], "0.01"), "hotCells": int(r[5])} for r in self.height_profile(stream)]
-        return {"Q_kW": fixed(self.hrr(stream), "0.1"), "rows": rows}
+
+def js_round(x: float) -> int:
+    """JavaScript's `Math.round`: the nearest integer, a tie going toward +infinity (no x + 0.5 rounding step)."""
+    r = float(np.floor(x))
+    return int(r + 1.0 if x - r >= 0.5 else r)
 
 
 # ---------------------------------------------------------------------------------------------------

@@ -67,6 +67,16 @@ def test_make_spots_deterministic_and_in_disc():
         F.make_spots(5, 17)
 
 
+def test_js_rounding_helpers():
+    """FIRE.profile's display rounding: toFixed works on the exact binary value, Math.round ties go up."""
+    assert F.js_to_fixed(1.005, 2) == 1.0          # 1.005 is 1.00499999999999989... in binary
+    assert F.js_to_fixed(0.125, 2) == 0.13         # an exact tie: the larger n
+    assert F.js_to_fixed(-0.125, 2) == -0.13       # toFixed rounds |x| and keeps the sign
+    assert F.js_to_fixed(1234.56789, 1) == 1234.6
+    assert F.js_round(2.5) == 3 and F.js_round(-2.5) == -2 and F.js_round(1672.49) == 1672
+    assert F.js_round(0.49999999999999994) == 0     # floor(x + 0.5) would give 1
+
+
 def test_host_classes_define_each_method_once():
     """A second definition of a method name silently replaces the first (a FIRE.profile mirror named `profile`
     would hide the per-stage timing switch `profile(enable)` that bench.py uses)."""

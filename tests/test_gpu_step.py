@@ -201,7 +201,7 @@ def test_height_profile_matches_numpy(campfire):
     assert rows[:, 2].max() > 1000.0   # a burning fire has hot rows
     prof = sim.fire_profile()
     assert len(prof["rows"]) == len(rows) and prof["Q_kW"] == pytest.approx(sim.hrr(), abs=0.051)
-    assert prof["rows"][0]["Tmax"] == int(np.floor(rows[0, 2] + 0.5))
+    assert prof["rows"][0]["Tmax"] == F.js_round(rows[0, 2]) and prof["rows"][0]["h"] == F.js_to_fixed(rows[0, 0], 2)
 
 
 def test_stage_times_profiled_graph(campfire):
