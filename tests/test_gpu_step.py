@@ -62,6 +62,35 @@ def _derived(f):
             "soot": S[..., 2], "age": S2[..., 1] / np.maximum(S[..., 1] + S2[..., 0], 1e-4), "p": f["p"]}
 
 
+def test_nan_cells_are_counted_and_scrubbed(campfire):
+    """NaN planted in the state: fire_sim_stats reports them as bad values, and one step scrubs them as the
+    reference does (NaN-ignoring limiter min/max in adv2, the forces and project NaN checks, src/sim.js:392,
+    547) — the GPU step stays finite and matches the oracle fed the same NaNs."""
+    sim, orc = FC.make_pair(FC.C1, logs=campfire)
+    dt = FC.C1["dt"]
+    st = FC.random_state(FC.C1["res"], 33)
+    rng = np.random.default_rng(4)
+    nz, ny, nx = st["S"].shape[:3]
+    planted = {("S", 0): 5, ("S2", 2): 3, ("vel", 1): 2}
+    for (name, c), n in planted.items():
+        idx = rng.choice(nz * ny * nx, n, replace=False)
+        st[name].reshape(-1, 4)[idx, c] = np.nan
+    FC.put_state(sim, orc, st)
+    s = sim.stats("S")
+    assert [c["bad"] for c in s] == [5, 0, 0, 0]
+    assert sim.stats("S2")[2]["bad"] == 3 and sim.stats("vel")[1]["bad"] == 2
+    FC.sync_block(sim, orc, dt)
+    sim.step(dt, 1)
+    sim.sync()
+    orc.step_raw(True, FC.C1["vcycles"])
+    g, o = _fields(sim, True), _fields(orc, False)
+    for k in ("vel", "S", "S2"):
+        assert np.isfinite(g[k]).all() and np.isfinite(o[k]).all(), k
+        assert all(c["bad"] == 0 for c in sim.stats(k)), k
+        for c in range(4):
+            FC.compare(g[k][..., c], o[k][..., c], 1e-3, 1e-4, 5e-3, what=f"nan-step:{k}[{c}]")
+
+
 @pytest.mark.parametrize("emitter", ["campfire", "spots"])
 def test_sixty_steps_vs_oracles(campfire, emitter):
     """60 steps from rest.  Against the FP32 oracle: rel L2 <= 1e-2 per field (2e-2 for soot and age, which
