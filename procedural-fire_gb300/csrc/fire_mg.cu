@@ -504,13 +504,21 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
-// Waits for phase 0 of the barrier with an iteration limit; returns false if the limit was reached.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for phase 0 of the barrier for at most about a second (and at most 2^22 polls); returns false if the
+// limit was reached.
 __device__ __forceinline__ bool mbar_wait0(uint64_t* bar) {
+  const unsigned long long t0 = global_ns();
   for (int it = 0; it < (1 << 22); ++it) {
     unsigned done;
     asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
                  : "=r"(done) : "r"(smem_addr(bar)), "r"(0u) : "memory");
     if (done) return true;
+    if ((it & 63) == 63 && global_ns() - t0 > 1000000000ull) return false;
   }
   return false;
 }
@@ -548,6 +556,9 @@ __device__ __forceinline__ void tail_body(const TailLevels& T, int pre, int post
       __syncthreads();                        // the barrier is initialised before anyone polls it
       if (!mbar_wait0(&bar)) {                // bounded wait: report and leave instead of hanging
         if (tid == 0) atomicExch(err, 1);
+        // copies may still be landing in this CTA's shared memory: a second bounded wait for them before the
+        // CTA exits and its shared memory can be handed to another CTA
+        mbar_wait0(&bar);
         return;
       }
     } else {
