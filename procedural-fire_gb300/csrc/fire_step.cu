@@ -1,8 +1,9 @@
 // Per-step stencil kernels of the fire simulation: MacCormack advection, curl + forces (fused),
 // divergence and projection.  Each kernel restates one WGSL compute shader of src/sim.js; the line
 // ranges are given per kernel.  One thread per cell; CTAs cover 32 x 4 x 2 bricks so the gathers of
-// the semi-Lagrangian back-trace and the 7-point stencils hit L1.  Fields are dense float4 arrays,
-// x fastest, so every warp reads and writes 512 contiguous bytes per field.
+// the semi-Lagrangian back-trace and the 7-point stencils hit L1 (the forces stage instead marches 32 x 8
+// column tiles up z, one wave of resident CTAs).  Fields are dense float4 arrays, x fastest, so every warp
+// reads and writes 512 contiguous bytes per field.
 #include <type_traits>
 #include "fire_device.cuh"
 #include "fire_launch.cuh"
@@ -354,7 +355,8 @@ __global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fie
 }
 
 // ---- z-marching shared-memory variant of curl + forces ----
-// A CTA of 32 x 8 threads owns a 32 x 8 column tile and marches through FZ planes.  Shared memory holds a
+// A CTA of 32 x 8 threads owns a 32 x 8 column tile and marches through a run of planes (FZ planes per CTA
+// in the batched kernel; an equal share of all (column, plane) units in the one-wave kernel).  Shared memory holds a
 // ring of 5 velY planes (tile + 2-cell halo, clamped to the domain like `ld`) and a ring of 3 vorticity
 // planes (tile + 1-cell halo).  Vorticity at a halo position outside the domain is the vorticity of the
 // clamped position, which is what `ld(vortT, c +- e)` returns.  Each velY value is loaded ~2x per cell
