@@ -97,3 +97,118 @@ def test_level_hierarchy(oracle_mod):
     O2 = oracle_mod.OracleSim((128, 256, 128), 0.005)
     assert [l[0] for l in O2.levels][-1] == (4, 8, 4) and len(O2.levels) == 6
     assert O2.levels[2][1] == pytest.approx(0.02, rel=1e-6)
+
+
+def _trilinear(f, c):
+    """textureSampleLevel with a linear, clamp-to-edge sampler at positions c (..., 3) in cell units (texel i's
+    centre at i + 0.5), as a weighted sum of the 8 texels."""
+    nz, ny, nx = f.shape[:3]
+    u = c - 0.5
+    i0 = np.floor(u).astype(np.int64)
+    fr = u - i0
+    out = np.zeros(c.shape[:-1] + (f.shape[-1],))
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                w = ((fr[..., 0] if dx else 1 - fr[..., 0]) * (fr[..., 1] if dy else 1 - fr[..., 1]) *
+                     (fr[..., 2] if dz else 1 - fr[..., 2]))
+                ix = np.clip(i0[..., 0] + dx, 0, nx - 1)
+                iy = np.clip(i0[..., 1] + dy, 0, ny - 1)
+                iz = np.clip(i0[..., 2] + dz, 0, nz - 1)
+                out += w[..., None] * f[iz, iy, ix]
+    return out
+
+
+def test_adv1_matches_numpy_restatement(oracle_mod):
+    """The oracle's first MacCormack pass (src/sim.js:123-157: RK2 midpoint back-trace, trilinear samples,
+    outside fade, wind carried in from the open sides) against a numpy restatement, both in FP64."""
+    import fire_sim as F
+    res, dx, dt = (10, 14, 8), 0.0125, 1.0 / 120.0
+    nx, ny, nz = res
+    rng = np.random.default_rng(11)
+    vel = np.zeros((nz, ny, nx, 4))
+    vel[..., :3] = rng.uniform(-2.5, 2.5, (nz, ny, nx, 3))   # back-traces of up to ~2 cells, some leave the box
+    S = rng.uniform(0.0, 1.0, (nz, ny, nx, 4))
+    S2 = rng.uniform(0.0, 1.0, (nz, ny, nx, 4))
+    p = F.param_defaults().copy()
+    idx = {n: i for i, n in enumerate(F.SIM_FIELDS)}
+    for k, v in (("nx", nx), ("ny", ny), ("nz", nz), ("dx", dx), ("dt", dt), ("windX", 0.7), ("windZ", -0.4)):
+        p[idx[k]] = v
+    orc = oracle_mod.OracleSim(res, float(np.float32(dx)), dbl=True)
+    orc.set_params(p)
+    for k, a in (("vel", vel), ("S", S), ("S2", S2)):
+        orc.put(k, a)
+    orc.stage("adv1")
+    dt64, dx64 = float(p[idx["dt"]]), float(p[idx["dx"]])
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    c = np.stack([i, j, k], -1) + 0.5
+    v0 = _trilinear(vel, c)[..., :3]
+    mid = c - 0.5 * dt64 * v0 / dx64
+    b = c - dt64 * _trilinear(vel, mid)[..., :3] / dx64
+    lo = np.minimum(b[..., 0], b[..., 2])
+    hi = np.maximum(b[..., 0] - nx, np.maximum(b[..., 1] - ny, b[..., 2] - nz))
+    fade = np.clip(1.0 - np.maximum(-lo, hi), 0.0, 1.0)
+    t = np.clip((b[..., 1] * dx64 - 0.03) / (0.4 - 0.03), 0.0, 1.0)
+    ws = t * t * (3.0 - 2.0 * t)
+    wind = np.stack([float(p[idx["windX"]]) * ws, 0.0 * ws, float(p[idx["windZ"]]) * ws], -1)
+    sv = _trilinear(vel, b)[..., :3]
+    want_v = wind * (1.0 - fade[..., None]) + sv * fade[..., None]
+    assert (fade < 1.0).any() and (fade > 0.0).any()   # the case reaches the open sides
+    np.testing.assert_allclose(orc.get("velX", np.float64)[..., :3], want_v, rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(orc.get("SX", np.float64), _trilinear(S, b) * fade[..., None], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(orc.get("S2X", np.float64), _trilinear(S2, b) * fade[..., None], rtol=1e-9, atol=1e-12)
+
+
+def test_adv2_matches_numpy_restatement(oracle_mod):
+    """The oracle's MacCormack correction and limiter (src/sim.js:159-197: reverse sample of the hats at the
+    forward-traced point, min/max of the 8 clamped texels around the back-traced point, revert where that
+    point's stencil leaves the domain, non-negative scalars) against a numpy restatement, both in FP64."""
+    import fire_sim as F
+    res, dx, dt = (9, 12, 7), 0.0125, 1.0 / 120.0
+    nx, ny, nz = res
+    rng = np.random.default_rng(12)
+    sh = (nz, ny, nx, 4)
+    vel = np.zeros(sh)
+    vel[..., :3] = rng.uniform(-2.5, 2.5, sh[:3] + (3,))
+    fields = {"vel": vel, "S": rng.uniform(0, 1, sh), "S2": rng.uniform(0, 1, sh)}
+    hats = {"velX": vel + rng.normal(0, 0.3, sh), "SX": fields["S"] + rng.normal(0, 0.2, sh),
+            "S2X": fields["S2"] + rng.normal(0, 0.2, sh)}
+    hats["velX"][..., 3] = 0.0
+    p = F.param_defaults().copy()
+    idx = {n: i for i, n in enumerate(F.SIM_FIELDS)}
+    for k, v in (("nx", nx), ("ny", ny), ("nz", nz), ("dx", dx), ("dt", dt)):
+        p[idx[k]] = v
+    orc = oracle_mod.OracleSim(res, float(np.float32(dx)), dbl=True)
+    orc.set_params(p)
+    for k, a in list(fields.items()) + list(hats.items()):
+        orc.put(k, a)
+    orc.stage("adv2")
+    dt64, dx64 = float(p[idx["dt"]]), float(p[idx["dx"]])
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    c = np.stack([i, j, k], -1) + 0.5
+    v = vel[..., :3]
+    fw = c + dt64 * v / dx64
+    mid = c - 0.5 * dt64 * _trilinear(vel, c)[..., :3] / dx64
+    b = c - dt64 * _trilinear(vel, mid)[..., :3] / dx64 - 0.5
+    b0 = np.floor(b).astype(np.int64)
+    lo_b = np.minimum(b[..., 0] + 0.5, b[..., 2] + 0.5)
+    hi_b = np.maximum(b[..., 0] + 0.5 - nx, np.maximum(b[..., 1] + 0.5 - ny, b[..., 2] + 0.5 - nz))
+    revert = np.clip(1.0 - np.maximum(-lo_b, hi_b), 0.0, 1.0) < 1.0
+    assert revert.any() and (~revert).any()
+    for name, hat, out, ch in (("vel", "velX", "velY", 3), ("S", "SX", "SY", 4), ("S2", "S2X", "S2Y", 4)):
+        f, h = fields[name], hats[hat]
+        N = h + 0.5 * (f - _trilinear(h, fw))
+        N[revert] = h[revert]
+        mn = np.full(f.shape, 1e9)
+        mx = np.full(f.shape, -1e9)
+        for q in range(8):
+            qx = np.clip(b0[..., 0] + (q & 1), 0, nx - 1)
+            qy = np.clip(b0[..., 1] + ((q >> 1) & 1), 0, ny - 1)
+            qz = np.clip(b0[..., 2] + ((q >> 2) & 1), 0, nz - 1)
+            t = f[qz, qy, qx]
+            mn, mx = np.minimum(mn, t), np.maximum(mx, t)
+        want = np.minimum(np.maximum(N, np.minimum(mn, h)), np.maximum(mx, h))
+        if name != "vel":
+            want = np.maximum(want, 0.0)
+        got = orc.get(out, np.float64)
+        np.testing.assert_allclose(got[..., :ch], want[..., :ch], rtol=1e-9, atol=1e-12, err_msg=out)
