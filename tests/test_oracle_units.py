@@ -212,3 +212,70 @@ def test_adv2_matches_numpy_restatement(oracle_mod):
             want = np.maximum(want, 0.0)
         got = orc.get(out, np.float64)
         np.testing.assert_allclose(got[..., :ch], want[..., :ch], rtol=1e-9, atol=1e-12, err_msg=out)
+
+
+def _setup_small(oracle_mod, res, seed):
+    import fire_sim as F
+    nx, ny, nz = res
+    p = F.param_defaults().copy()
+    idx = {n: i for i, n in enumerate(F.SIM_FIELDS)}
+    for k, v in (("nx", nx), ("ny", ny), ("nz", nz), ("dx", 0.0125), ("dt", 1.0 / 120.0)):
+        p[idx[k]] = v
+    orc = oracle_mod.OracleSim(res, float(np.float32(0.0125)), dbl=True)
+    orc.set_params(p)
+    return orc, float(p[idx["dx"]]), np.random.default_rng(seed)
+
+
+def test_div_matches_numpy_restatement(oracle_mod):
+    """Divergence minus the expansion target (src/sim.js:399-413): clamped central differences of velX,
+    the floor's mirrored normal velocity, minus phi (velX.w)."""
+    res = (9, 11, 8)
+    nx, ny, nz = res
+    orc, dx, rng = _setup_small(oracle_mod, res, 13)
+    vx = rng.uniform(-2, 2, (nz, ny, nx, 4))
+    orc.put("velX", vx)
+    orc.stage("div")
+    pad = lambda a: np.pad(a, 1, mode="edge")
+    u, v, w = (pad(vx[..., c]) for c in range(3))
+    R, L = u[1:-1, 1:-1, 2:], u[1:-1, 1:-1, :-2]
+    T, B = v[1:-1, 2:, 1:-1], v[1:-1, :-2, 1:-1].copy()
+    F_, K = w[2:, 1:-1, 1:-1], w[:-2, 1:-1, 1:-1]
+    B[:, 0, :] = -vx[:, 0, :, 1]
+    want = ((R - L) + (T - B) + (F_ - K)) / (2.0 * dx) - vx[..., 3]
+    np.testing.assert_allclose(orc.get_level(0, "b", np.float64), want, rtol=1e-12, atol=1e-12)
+
+
+def test_project_matches_numpy_restatement(oracle_mod):
+    """Projection (src/sim.js:526-550): minus the central pressure gradient with the open-side (-p) and floor
+    (+p) ghosts, zero in solids, no flow into the floor, speed capped at 20."""
+    res = (9, 11, 8)
+    nx, ny, nz = res
+    orc, dx, rng = _setup_small(oracle_mod, res, 14)
+    vx = np.zeros((nz, ny, nx, 4))
+    vx[..., :3] = rng.uniform(-3, 3, (nz, ny, nx, 3))
+    p = rng.uniform(-0.02, 0.02, (nz, ny, nx))
+    p[2, 5, 4] = 3.0                                    # a gradient that pushes the speed past the cap
+    geo = np.zeros((nz, ny, nx, 4))
+    geo[3:5, 2:4, 3:6, 2] = 1.0                         # a solid block (geo.b > 0.5)
+    orc.put("velX", vx)
+    orc.put("geo", geo)
+    orc.put_level(0, "p", p)
+    orc.stage("project")
+    pp = np.pad(p, 1)
+    # ghosts: -me beyond the open sides and the top, +me below the floor (y < 0)
+    me = p
+    xm = np.where(np.arange(nx)[None, None, :] > 0, pp[1:-1, 1:-1, :-2], -me)
+    xp = np.where(np.arange(nx)[None, None, :] < nx - 1, pp[1:-1, 1:-1, 2:], -me)
+    ym = np.where(np.arange(ny)[None, :, None] > 0, pp[1:-1, :-2, 1:-1], me)
+    yp = np.where(np.arange(ny)[None, :, None] < ny - 1, pp[1:-1, 2:, 1:-1], -me)
+    zm = np.where(np.arange(nz)[:, None, None] > 0, pp[:-2, 1:-1, 1:-1], -me)
+    zp = np.where(np.arange(nz)[:, None, None] < nz - 1, pp[2:, 1:-1, 1:-1], -me)
+    g = np.stack([xp - xm, yp - ym, zp - zm], -1) / (2.0 * dx)
+    v = vx[..., :3] - g
+    v[geo[..., 2] > 0.5] = 0.0
+    v[:, 0, :, 1] = np.maximum(v[:, 0, :, 1], 0.0)
+    vl = np.linalg.norm(v, axis=-1)
+    cap = vl > 20.0
+    assert cap.any()
+    v[cap] *= (20.0 / vl[cap])[:, None]
+    np.testing.assert_allclose(orc.get("vel", np.float64)[..., :3], v, rtol=1e-12, atol=1e-12)
