@@ -230,3 +230,52 @@ def test_forces_matches_numpy_restatement(oracle_mod, tables):
     for name, want in (("velX", want_v), ("S", want_s), ("S2", want_s2)):
         got = orc.get(name, np.float64)
         np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-10, err_msg=name)
+
+
+def test_geo_matches_numpy_restatement(oracle_mod):
+    """Emitter geometry (src/sim.js:498-523, sdCapsule src/shaders/lib.js:57-62) for the packed campfire
+    (8 logs + 8 zero slots, as packLogs leaves them), against a numpy restatement in FP64.  The zero slots are
+    degenerate capsules (dot(ba, ba) = 0); clamp ignores the NaN, so h = 0 there."""
+    res, dx = (24, 20, 22), 0.02
+    nx, ny, nz = res
+    logs = oracle_mod.build_campfire(7).astype(np.float64).reshape(16, 8)
+    P = F.param_defaults().copy()
+    for k, v in (("nx", nx), ("ny", ny), ("nz", nz), ("dx", dx), ("ox", -nx * dx / 2), ("oy", 0.0),
+                 ("oz", -nz * dx / 2), ("nLogs", 16.0)):
+        P[IDX[k]] = v
+    E = np.zeros(144, np.float32)
+    E[2] = 1.0                       # coal-bed gain 1: the reference's bed
+    E[5] = -1e30
+    orc = oracle_mod.OracleSim(res, float(np.float32(dx)), dbl=True)
+    orc.set_params(P)
+    orc.set_ext(E)
+    orc.set_logs(logs.astype(np.float32).ravel())
+    orc.stage("geo")
+    got = orc.get("geo", np.float64)
+
+    g = lambda n: float(P[IDX[n]])
+    dxd = g("dx")
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    p = np.array([g("ox"), g("oy"), g("oz")]) + (np.stack([i, j, k], -1) + 0.5) * dxd
+    rxz = np.linalg.norm(p[..., [0, 2]], axis=-1)
+    lg = logs.astype(np.float32).astype(np.float64)
+    dmin = np.full(p.shape[:-1], 1e9)
+    band = np.zeros(p.shape[:-1])
+    for n in range(int(g("nLogs"))):
+        a, r, bb, burn = lg[n, 0:3], lg[n, 3], lg[n, 4:7], lg[n, 7]
+        pa, ba = p - a, bb - a
+        with np.errstate(invalid="ignore", divide="ignore"):
+            h = np.fmin(np.fmax((pa @ ba) / (ba @ ba), 0.0), 1.0)      # NaN-ignoring clamp
+        dd = np.linalg.norm(pa - h[..., None] * ba, axis=-1) - r
+        dd = dd + r * 0.3 * (1.0 - smoothstep(0.0, 0.16, rxz)) * burn
+        dmin = np.minimum(dmin, dd)
+        bnd = 1.0 - smoothstep(0.0, 1.6 * dxd, np.abs(dd - 0.6 * dxd))
+        hot = burn * (1.0 - smoothstep(g("hotR0"), g("hotR1"), rxz)) * (1.0 - smoothstep(0.08, g("hotY1"), p[..., 1]))
+        band = np.maximum(band, bnd * hot)
+    bedH = 0.05 * (1.0 - smoothstep(0.0, g("bedRadius"), rxz)) + 0.02
+    bed = ((1.0 - smoothstep(0.0, 2.0 * dxd, p[..., 1] - bedH)) *
+           (1.0 - smoothstep(g("bedRadius") * 0.6, g("bedRadius") * 1.15, rxz)))
+    solid = np.where(dmin < -0.5 * dxd, 1.0, 0.0)
+    want = np.stack([band, bed, solid, dmin], -1)
+    assert band.max() > 0.5 and bed.max() > 0.5 and solid.sum() > 10
+    np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-12)
