@@ -279,3 +279,68 @@ def test_project_matches_numpy_restatement(oracle_mod):
     assert cap.any()
     v[cap] *= (20.0 / vl[cap])[:, None]
     np.testing.assert_allclose(orc.get("vel", np.float64)[..., :3], v, rtol=1e-12, atol=1e-12)
+
+
+def _neighbours(p):
+    """The six neighbour values of every cell with the ghost rules applied (ghosts use the cell's own value)."""
+    nz, ny, nx = p.shape
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    get = lambda a, b, c: p[np.clip(a, 0, nz - 1), np.clip(b, 0, ny - 1), np.clip(c, 0, nx - 1)]
+    xm = np.where(i > 0, get(k, j, i - 1), -p)
+    xp = np.where(i < nx - 1, get(k, j, i + 1), -p)
+    zm = np.where(k > 0, get(k - 1, j, i), -p)
+    zp = np.where(k < nz - 1, get(k + 1, j, i), -p)
+    ym = np.where(j > 0, get(k, j - 1, i), p)
+    yp = np.where(j < ny - 1, get(k, j + 1, i), -p)
+    return xm, xp, ym, yp, zm, zp
+
+
+def test_multigrid_operators_match_numpy_restatement(oracle_mod):
+    """One red-black colour sweep, the fused residual + restriction and the mirror-ghost prolongation
+    (src/sim.js:417-495) of the oracle's FP64 mode against numpy restatements."""
+    res = (12, 16, 10)
+    orc = oracle_mod.OracleSim(res, 0.0125, dbl=True)
+    (nx, ny, nz), h = orc.levels[0]
+    (cx, cy, cz), _ = orc.levels[1]
+    rng = np.random.default_rng(31)
+    p = rng.normal(0, 1, (nz, ny, nx))
+    b = rng.normal(0, 50, (nz, ny, nx))
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    # smooth, colour 1: the cells with (x + y + z + 1) even, i.e. x + y + z odd
+    orc.put_level(0, "p", p)
+    orc.put_level(0, "b", b)
+    orc.mg_smooth(0, 1)
+    nb = _neighbours(p)
+    inside = [i > 0, i < nx - 1, j > 0, j < ny - 1, k > 0, k < nz - 1]
+    ssum = sum(np.where(m, v, 0.0) for m, v in zip(inside, nb))
+    diag = 6.0 + (i == 0) + (i == nx - 1) + (k == 0) + (k == nz - 1) + (j == ny - 1) - (j == 0)
+    gs = (ssum - h * h * b) / diag
+    want = np.where((i + j + k) % 2 == 1, gs, p)
+    np.testing.assert_allclose(orc.get_level(0, "p", np.float64), want, rtol=1e-12, atol=1e-12)
+    # restriction of the residual of `want`
+    orc.mg_restrict(0)
+    xm, xp, ym, yp, zm, zp = _neighbours(want)
+    r = b - (xm + xp + ym + yp + zm + zp - 6.0 * want) / (h * h)
+    bc = r[:2 * cz, :2 * cy, :2 * cx].reshape(cz, 2, cy, 2, cx, 2).mean(axis=(1, 3, 5))
+    np.testing.assert_allclose(orc.get_level(1, "b", np.float64), bc, rtol=1e-11, atol=1e-9)
+    assert not orc.get_level(1, "p", np.float64).any()
+    # prolongation of a random coarse correction
+    pc = rng.normal(0, 1, (cz, cy, cx))
+    orc.put_level(1, "p", pc)
+    orc.mg_prolong(0)
+    acc = np.zeros((nz, ny, nx))
+    g = (np.stack([i, j, k], -1) + 0.5) * 0.5 - 0.5
+    g0 = np.floor(g).astype(np.int64)
+    f = g - g0
+    nc = np.array([cx, cy, cz])
+    for q8 in range(8):
+        o = np.array([q8 & 1, (q8 >> 1) & 1, (q8 >> 2) & 1])
+        q = g0 + o
+        qc = np.clip(q, 0, nc - 1)
+        val = pc[qc[..., 2], qc[..., 1], qc[..., 0]]
+        val = np.where((q[..., 0] < 0) | (q[..., 0] >= cx), -val, val)
+        val = np.where((q[..., 2] < 0) | (q[..., 2] >= cz), -val, val)
+        val = np.where(q[..., 1] >= cy, -val, val)
+        w = np.where(o == 1, f, 1.0 - f)
+        acc += val * w[..., 0] * w[..., 1] * w[..., 2]
+    np.testing.assert_allclose(orc.get_level(0, "p", np.float64), want + acc, rtol=1e-12, atol=1e-12)
