@@ -297,7 +297,7 @@ def _neighbours(p):
 
 def test_multigrid_operators_match_numpy_restatement(oracle_mod):
     """One red-black colour sweep, the fused residual + restriction and the mirror-ghost prolongation
-    (src/sim.js:417-495) of the oracle's FP64 mode against numpy restatements."""
+    (src/sim.js:417-495) of the oracle's FP64 mode against numpy restatements (the helpers below)."""
     res = (12, 16, 10)
     orc = oracle_mod.OracleSim(res, 0.0125, dbl=True)
     (nx, ny, nz), h = orc.levels[0]
@@ -305,34 +305,48 @@ def test_multigrid_operators_match_numpy_restatement(oracle_mod):
     rng = np.random.default_rng(31)
     p = rng.normal(0, 1, (nz, ny, nx))
     b = rng.normal(0, 50, (nz, ny, nx))
-    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
-    # smooth, colour 1: the cells with (x + y + z + 1) even, i.e. x + y + z odd
     orc.put_level(0, "p", p)
     orc.put_level(0, "b", b)
     orc.mg_smooth(0, 1)
+    want = _smooth_colour(p, b, h, 1)
+    assert not np.array_equal(want, p)
+    np.testing.assert_allclose(orc.get_level(0, "p", np.float64), want, rtol=1e-12, atol=1e-12)
+    orc.mg_restrict(0)
+    np.testing.assert_allclose(orc.get_level(1, "b", np.float64), _restrict(want, b, h, (cx, cy, cz)), rtol=1e-11, atol=1e-9)
+    assert not orc.get_level(1, "p", np.float64).any()
+    pc = rng.normal(0, 1, (cz, cy, cx))
+    orc.put_level(1, "p", pc)
+    orc.mg_prolong(0)
+    np.testing.assert_allclose(orc.get_level(0, "p", np.float64), _prolong_add(want, pc), rtol=1e-12, atol=1e-12)
+
+
+def _smooth_colour(p, b, h, colour):
+    """One red-black colour sweep (src/sim.js:417-437): the cells with (x + y + z + colour) even."""
+    nz, ny, nx = p.shape
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
     nb = _neighbours(p)
     inside = [i > 0, i < nx - 1, j > 0, j < ny - 1, k > 0, k < nz - 1]
     ssum = sum(np.where(m, v, 0.0) for m, v in zip(inside, nb))
     diag = 6.0 + (i == 0) + (i == nx - 1) + (k == 0) + (k == nz - 1) + (j == ny - 1) - (j == 0)
-    gs = (ssum - h * h * b) / diag
-    want = np.where((i + j + k) % 2 == 1, gs, p)
-    np.testing.assert_allclose(orc.get_level(0, "p", np.float64), want, rtol=1e-12, atol=1e-12)
-    # restriction of the residual of `want`
-    orc.mg_restrict(0)
-    xm, xp, ym, yp, zm, zp = _neighbours(want)
-    r = b - (xm + xp + ym + yp + zm + zp - 6.0 * want) / (h * h)
-    bc = r[:2 * cz, :2 * cy, :2 * cx].reshape(cz, 2, cy, 2, cx, 2).mean(axis=(1, 3, 5))
-    np.testing.assert_allclose(orc.get_level(1, "b", np.float64), bc, rtol=1e-11, atol=1e-9)
-    assert not orc.get_level(1, "p", np.float64).any()
-    # prolongation of a random coarse correction
-    pc = rng.normal(0, 1, (cz, cy, cx))
-    orc.put_level(1, "p", pc)
-    orc.mg_prolong(0)
-    acc = np.zeros((nz, ny, nx))
+    return np.where((i + j + k + colour) % 2 == 0, (ssum - h * h * b) / diag, p)
+
+
+def _restrict(p, b, h, cdims):
+    cx, cy, cz = cdims
+    xm, xp, ym, yp, zm, zp = _neighbours(p)
+    r = b - (xm + xp + ym + yp + zm + zp - 6.0 * p) / (h * h)
+    return r[:2 * cz, :2 * cy, :2 * cx].reshape(cz, 2, cy, 2, cx, 2).mean(axis=(1, 3, 5))
+
+
+def _prolong_add(p, pc):
+    nz, ny, nx = p.shape
+    cz, cy, cx = pc.shape
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
     g = (np.stack([i, j, k], -1) + 0.5) * 0.5 - 0.5
     g0 = np.floor(g).astype(np.int64)
     f = g - g0
     nc = np.array([cx, cy, cz])
+    acc = np.zeros(p.shape)
     for q8 in range(8):
         o = np.array([q8 & 1, (q8 >> 1) & 1, (q8 >> 2) & 1])
         q = g0 + o
@@ -343,4 +357,37 @@ def test_multigrid_operators_match_numpy_restatement(oracle_mod):
         val = np.where(q[..., 1] >= cy, -val, val)
         w = np.where(o == 1, f, 1.0 - f)
         acc += val * w[..., 0] * w[..., 1] * w[..., 2]
-    np.testing.assert_allclose(orc.get_level(0, "p", np.float64), want + acc, rtol=1e-12, atol=1e-12)
+    return p + acc
+
+
+def test_vcycle_matches_numpy_restatement(oracle_mod):
+    """The step's V(2,2) cycle (src/sim.js:576-599): pre-sweeps and residual restriction down the hierarchy,
+    coarseIters sweeps on the coarsest level (src/sim.js:88-92), prolongation and post-sweeps back up — the
+    oracle's FP64 cycle against one composed from the numpy operators."""
+    res = (16, 24, 16)
+    orc = oracle_mod.OracleSim(res, 0.0125, dbl=True)
+    levels = orc.levels
+    assert len(levels) >= 3
+    rng = np.random.default_rng(41)
+    (nx, ny, nz), _ = levels[0]
+    p0 = rng.normal(0, 1, (nz, ny, nx))
+    b0 = rng.normal(0, 30, (nz, ny, nx))
+    orc.put_level(0, "p", p0)
+    orc.put_level(0, "b", b0)
+    orc.vcycle(2, 2)
+    P, B = [p0], [b0]
+    n = len(levels)
+    for l in range(n - 1):
+        h = levels[l][1]
+        for _ in range(2):
+            P[l] = _smooth_colour(_smooth_colour(P[l], B[l], h, 0), B[l], h, 1)
+        B.append(_restrict(P[l], B[l], h, levels[l + 1][0]))
+        cx, cy, cz = levels[l + 1][0]
+        P.append(np.zeros((cz, cy, cx)))
+    for _ in range(orc.coarse_iters):
+        P[n - 1] = _smooth_colour(_smooth_colour(P[n - 1], B[n - 1], levels[n - 1][1], 0), B[n - 1], levels[n - 1][1], 1)
+    for l in range(n - 2, -1, -1):
+        P[l] = _prolong_add(P[l], P[l + 1])
+        for _ in range(2):
+            P[l] = _smooth_colour(_smooth_colour(P[l], B[l], levels[l][1], 0), B[l], levels[l][1], 1)
+    np.testing.assert_allclose(orc.get_level(0, "p", np.float64), P[0], rtol=1e-9, atol=1e-9 * np.abs(P[0]).max())
