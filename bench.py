@@ -200,48 +200,95 @@ def launches_per_step(sim, cycles_per_step: float) -> float:
     return 6 + per_cycle * cycles_per_step
 
 
-def cpu_baseline(O, sim_tables, cycles: int, steps: int = 2):
-    """The oracle (FP32, OpenMP on all cores) on `steps` steps of the same workload from rest."""
-    import fire_sim as F
+def workload_config(preroll: int) -> dict:
+    """The workload description both arms print (identical, so the two lines describe the same work)."""
     W = WORKLOAD
-    threads = os.cpu_count() or 1
-    O.set_threads(threads)
-    dx = np.float32(np.float64(np.float32(W["size"][0])) / W["res"][0])
-    orc = O.OracleSim(W["res"], float(dx))
-    noise, curl = sim_tables
-    orc.set_tables(noise, curl)
-    orc.set_logs(np.zeros(0, np.float32))
-    blk = _block(F)
-    orc.set_params(blk[:64])
-    orc.set_ext(blk[64:])
-    t0 = time.perf_counter()
-    for s in range(steps):
-        orc.step_raw(s == 0, cycles)
-    dt = time.perf_counter() - t0
-    return steps / dt, threads, f"{steps} steps of {W['res'][0]}x{W['res'][1]}x{W['res'][2]} from rest, {cycles} V-cycles each"
+    return {"workload": W["name"], "grid": list(W["res"]), "cell_m": 0.005, "dt": W["dt"], "spots": W["spots"],
+            "emitter": "6 seeded floor spots, flux U(1, 4) g/s, no logs, no coal bed",
+            "mg": f"V(2,2), every sweep over-relaxed (omega {W['mg_omega']}), to {W['mg_tol']} rel. residual, "
+                  f"max {W['mg_max_cycles']} cycles",
+            "state": f"timed steps follow {preroll} preroll steps from rest",
+            "l2": "inputs larger than L2 (fields ~740 MB vs 129 MB L2)"}
 
 
-def _block(F):
-    """The 208-float block for the workload (uniforms and extension; the oracle ignores the derived slots)."""
+class OracleStepper:
+    """The workload on the CPU oracle (FP32, OpenMP): the same seeded tables, spots, parameters, solver and
+    per-step simulated time as the GPU arm.  Built from the oracle alone (no product library is loaded)."""
+
+    def __init__(self, O, threads: int):
+        W = WORKLOAD
+        O.build()
+        O.set_threads(threads)
+        noise = O.noise_table(128, 1)
+        self.O = O
+        self.dx = np.float32(np.float64(np.float32(W["size"][0])) / W["res"][0])
+        self.orc = O.OracleSim(W["res"], float(self.dx))
+        self.orc.set_tables(noise, O.curl_table(noise))
+        self.orc.set_logs(np.zeros(0, np.float32))
+        self.orc.set_modes(omega=W["mg_omega"])
+        self.blk = oracle_block(O)
+        self.time, self.frame, self.geo = 0.0, 0, True
+        self.cycles = []
+
+    def step(self):
+        W = WORKLOAD
+        dt = np.float32(W["dt"])
+        self.blk[5] = np.float32(self.time)      # time and frame as FireSim.uploadUniforms writes them (src/sim.js:620-624)
+        self.blk[6] = np.float32(self.frame)
+        self.orc.set_params(self.blk[:64])
+        self.orc.set_ext(self.blk[64:])
+        self.cycles.append(self.orc.step_raw(self.geo, -W["mg_max_cycles"], W["mg_tol"]))
+        self.geo = False
+        self.time += float(dt)
+        self.frame += 1
+
+    def load_state(self, sim):
+        """Continues from a GPU simulation's state (fields, level-0 pressure, time and frame)."""
+        for name in ("vel", "S", "S2", "geo"):
+            self.orc.put(name, sim.download(name).astype(np.float32))
+        self.orc.put_level(0, "p", sim.download("p").astype(np.float32).reshape(self.orc.levels[0][0][::-1]))
+        info = sim.info()
+        self.time, self.frame, self.geo = float(info.time), int(info.frame), False
+
+
+def oracle_block(O):
+    """The workload's 208-float block (SIM_FIELDS uniforms + extension) from the oracle's restatements of
+    SIM_DEFAULTS and the seeded spots; the oracle recomputes the derived extension slots itself."""
     W = WORKLOAD
+    names = ["nx", "ny", "nz", "dx", "dt", "time", "frame", "seed", "ox", "oy", "oz", "nLogs"]
     blk = np.zeros(208, np.float32)
-    blk[:64] = F.param_defaults()
+    blk[:64] = O.sim_defaults()
     for i, v in enumerate(W["res"]):
         blk[i] = v
     size0 = np.float32(W["size"][0])
-    blk[3] = np.float32(np.float64(size0) / W["res"][0])
-    blk[4] = np.float32(W["dt"])
-    blk[8] = np.float32(-size0 / np.float32(2))
-    blk[10] = np.float32(-np.float32(W["size"][2]) / np.float32(2))
-    blk[F.SIM_FIELDS.index("vortEps")] = W["vortEps"]
-    blk[F.SIM_FIELDS.index("turbAmp")] = W["turbAmp"]
+    blk[names.index("dx")] = np.float32(np.float64(size0) / W["res"][0])
+    blk[names.index("dt")] = np.float32(W["dt"])
+    blk[names.index("ox")] = np.float32(-size0 / np.float32(2))
+    blk[names.index("oz")] = np.float32(-np.float32(W["size"][2]) / np.float32(2))
+    blk[34] = W["vortEps"]     # SIM_FIELDS index of vortEps (src/sim.js:19)
+    blk[35] = W["turbAmp"]     # turbAmp
     e = blk[64:]
     e[0], e[1], e[2], e[4] = W["soot_age"][0], W["soot_age"][1], 0.0, 4.0
-    spots = F.make_spots(W["spot_seed"], W["spots"], W["flux"][0], W["flux"][1], W["sigma"], W["radius"])
+    spots = O.make_spots(W["spot_seed"], W["spots"], W["flux"][0], W["flux"][1], W["sigma"], W["radius"])
     e[3] = len(spots)
-    for i, s in enumerate(spots):
-        e[16 + 8 * i: 16 + 8 * i + 5] = s
+    for i, sp in enumerate(spots):
+        e[16 + 8 * i: 16 + 8 * i + 5] = sp
     return blk
+
+
+def cpu_baseline(sim, steps: int = 2):
+    """The oracle (FP32, OpenMP on all host threads) continuing the GPU simulation's developed state for
+    `steps` steps of the same workload and solver."""
+    import oracle as O
+    threads = os.cpu_count() or 1
+    ref = OracleStepper(O, threads)
+    ref.load_state(sim)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ref.step()
+    el = time.perf_counter() - t0
+    return steps / el, threads, (f"{steps} steps of {WORKLOAD['res'][0]}x{WORKLOAD['res'][1]}x{WORKLOAD['res'][2]} continuing "
+                                 f"the GPU run's developed state (after its timed steps), {np.mean(ref.cycles):.2f} V-cycles each")
 
 
 # Standalone pressure solve: 256x512x256 cells at 5 mm, seeded zero-mean RHS of 32 Gaussian sources
@@ -643,9 +690,7 @@ def run_ours(args):
     # ---- CPU baseline: oracle on a bounded sample
     cpu = None
     if world == 1 and not args.no_cpu:
-        import oracle as O
-        tabs = (sim.download("noise").astype(np.float32), sim.download("curl").astype(np.float32))
-        v, cores, sample = cpu_baseline(O, tabs, max(1, int(round(cycles))), steps=2)
+        v, cores, sample = cpu_baseline(sim, steps=2)
         cpu = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
 
     clocks = sampler.summary() if sampler else None
@@ -653,10 +698,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": W["name"], "grid": list(W["res"]), "cell_m": 0.005, "dt": W["dt"],
-                   "spots": W["spots"], "mg": f"V(2,2), fine-level smoothing over-relaxed (omega {W['mg_omega']}), to {W['mg_tol']} rel. residual, max {W['mg_max_cycles']}",
-                   "mean_vcycles_per_step": cycles, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (fields ~740 MB vs 129 MB L2)"},
+        "config": workload_config(args.preroll),
+        "parallelism": f"replicas x{world}", "mean_vcycles_per_step": cycles,
         "gcell_updates_per_s": value * cells / 1e9,
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 208 * 4, "d2h_bytes_per_step": 17 * 8},
         "gpu_launches": int(round(args.steps * launches_per_step(sim, cycles))),
@@ -688,46 +731,40 @@ def run_ours(args):
 
 
 def run_reference(args):
-    """CPU implementation of the step (oracle port, all host threads) on the same workload."""
+    """The CPU implementation of the step (the oracle port of the reference's WGSL, FP32, all host threads) on
+    the same workload: the same preroll from rest, solver and per-step time; then `steps` timed steps (fewer
+    if a step is slow, within a fixed budget).  Loads no product library."""
     rank, world, _ = dist_env()
     if rank != 0:
         return None
-    import fire_sim as F
     import oracle as O
-    O.build()
-    W = WORKLOAD
     threads = os.cpu_count() or 1
-    O.set_threads(threads)
-    noise = O.noise_table(128, 1)
-    curl = O.curl_table(noise)
-    dx = np.float32(np.float64(np.float32(W["size"][0])) / W["res"][0])
-    orc = O.OracleSim(W["res"], float(dx))
-    orc.set_tables(noise, curl)
-    orc.set_logs(np.zeros(0, np.float32))
-    blk = _block(F)
-    orc.set_params(blk[:64])
-    orc.set_ext(blk[64:])
+    ref = OracleStepper(O, threads)
+    for _ in range(args.preroll + args.warmup):
+        ref.step()
     t_step = None
-    for s in range(max(args.warmup, 1)):
-        t0 = time.perf_counter()
-        orc.step_raw(s == 0, -W["mg_max_cycles"], W["mg_tol"])
-        t_step = time.perf_counter() - t0
-    budget = 150.0
-    k = max(2, min(args.steps, int(budget / max(t_step, 1e-3))))
     t0 = time.perf_counter()
-    for s in range(k):
-        orc.step_raw(False, -W["mg_max_cycles"], W["mg_tol"])
+    ref.step()
+    t_step = time.perf_counter() - t0
+    budget = 120.0
+    k = max(2, min(args.steps, int(budget / max(t_step, 1e-3))))
+    n0 = len(ref.cycles)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        ref.step()
     el = time.perf_counter() - t0
     v = k / el
+    cycles = float(np.mean(ref.cycles[n0:]))
     return {
         "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world, "steps": k, "warmup": args.warmup,
         "ms_per_step": 1e3 * el / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": {"workload": W["name"], "grid": list(W["res"]), "cell_m": 0.005, "dt": W["dt"],
-                   "spots": W["spots"], "mg": f"the reference's Gauss-Seidel V(2,2) to {W['mg_tol']} rel. residual, max {W['mg_max_cycles']}"},
+        "dtype": "f32", "data": "synthetic", "impl": "reference", "config": workload_config(args.preroll),
+        "parallelism": "CPU, one process", "mean_vcycles_per_step": cycles,
+        "gcell_updates_per_s": v * np.prod(WORKLOAD["res"]) / 1e9,
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{k} timed steps after {max(args.warmup, 1)} warm-up steps from rest "
-                                   f"(the reference's WebGPU step needs a browser GPU stack, unavailable on this box)"},
+                         "sample": f"{k} timed steps after {args.preroll} preroll + {args.warmup + 1} warm-up steps from rest, "
+                                   f"{cycles:.2f} V-cycles each (the reference's WebGPU step needs a browser GPU stack, "
+                                   f"unavailable on this box; this is the oracle's C++ restatement of its WGSL)"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

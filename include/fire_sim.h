@@ -164,6 +164,13 @@ int fire_sim_set_spots(FireSim* sim, const float* spots, int n);
  * Gauss-Seidel (src/sim.js:417-437) bit for bit; a larger value can cut the cycles a residual-driven solve
  * needs (no counterpart in the reference).                                                            */
 int fire_sim_set_mg_omega(FireSim* sim, float omega);
+/* Fault-injection hook for the device-side bounded wait (no counterpart in the reference, which logs
+ * WebGPU device loss, src/gpu.js:25-26): the multigrid's single-CTA tail waits for the TMA bulk copies that
+ * stage its first level into shared memory for at most `polls` polls (default 4194304, and about a second)
+ * before it records a timeout, waits again at the full bound for the copies in flight and returns without
+ * running the cycle; fire_sim_sync then reports FIRE_ERR_CUDA ("a device-side wait timed out") and clears
+ * the flag.  0 makes the first wait give up at once, so a test can exercise that path on a healthy GPU.   */
+int fire_sim_set_tail_wait_limit(FireSim* sim, int polls);
 
 /* ---- events (src/main.js:401-407, 456-461; src/timeline.js:126-157) ---------------------------- */
 /* inject: a burst puff (burstX/Y/Z, burstAmt; forces at src/sim.js:288-296) of `amount` lasting
@@ -249,9 +256,10 @@ int fire_make_spots(uint32_t seed, int n, float flux_lo, float flux_hi, float si
  *
  * Runs `cycles` V(2,2) cycles of the step's multigrid on caller-owned level-0 device arrays: `p` (pressure,
  * updated in place) and `b` (right-hand side, read only), both nx*ny*nz floats, x fastest; `h` is the cell
- * size in metres.  The level rules, coarse sweep count and kernels are those of fire_sim_step.  Every coarser
- * level lives in one file-scope device array of FIRE_NOALLOC_SCRATCH_BYTES that the library holds on every
- * GPU that loads it until the process exits; nothing is allocated and nothing is freed.
+ * size in metres.  The level rules, coarse sweep count and kernels are those of fire_sim_step; the sweeps
+ * are the reference's plain Gauss-Seidel (omega 1, fire_sim_step's default; fire_sim_set_mg_omega does not
+ * apply here).  Every coarser level lives in one file-scope device array of FIRE_NOALLOC_SCRATCH_BYTES that
+ * the library holds on every GPU that loads it until the process exits; nothing is allocated or freed.
  *   - The first call on a device (the one current when it is called) sets that device up: it resolves the
  *     array's device address and opts the coarse-level kernel into its shared memory.  Make that first call
  *     before any stream capture.
@@ -260,9 +268,16 @@ int fire_make_spots(uint32_t seed, int n, float flux_lo, float flux_hi, float si
  *   - All calls share the array and it keeps the last call's contents; each cycle rewrites the coarse
  *     levels before reading them, so nothing needs clearing between calls.  Calls whose work overlaps on the
  *     GPU (concurrent streams, or several host threads) race on the array: serialise them.
- * Asynchronous on `stream` (a cudaStream_t, or NULL).                                                   */
+ * Asynchronous on `stream` (a cudaStream_t, or NULL).
+ * Returns FIRE_ERR_CUDA if a launch failed (an error left by the caller's earlier work is not blamed on it).
+ * If the coarse-level kernel's bounded wait for its staging copies ever runs out, that cycle skips its coarse
+ * correction and the kernel records it in a flag at the end of the array: fire_poisson_noalloc_status reports
+ * it (FIRE_ERR_CUDA) after waiting for `stream`, and clears it.                                            */
 #define FIRE_NOALLOC_SCRATCH_BYTES (8u * 1024u * 1024u)
 int fire_poisson_vcycles_noalloc(float* p, const float* b, int nx, int ny, int nz, float h, int cycles, void* stream);
+/* Waits for `stream` and reports (FIRE_ERR_CUDA) and clears a bulk-copy wait timeout recorded by the calls
+ * above on the current device; FIRE_OK if none.  Allocates nothing; synchronous.                         */
+int fire_poisson_noalloc_status(void* stream);
 
 /* ---- ensembles of independent simulations ------------------------------------------------------
  * n (<= 64) simulations of possibly different grids advanced together: each stage of a step is one
@@ -431,6 +446,14 @@ int fire_poisson_make_rhs(FirePoisson* ps, float* b, unsigned seed, int n_source
 /* The sources of fire_poisson_make_rhs as 5 floats each (centre x, y, z in cells, sigma in cells,
  * amplitude); host only.                                                                                */
 int fire_poisson_sources(unsigned seed, int n_sources, const int res[3], float* out);
+/* FIRE_POISSON_FP32 form only: runs the V-cycle variant of the reference's multigrid convergence studies
+ * instead of the simulation's (research/webgpu-bench/poisson.mjs:28-75 rbgs / prolongAdd / vcycle and
+ * research/webgpu-bench/wgsl/mg.wgsl:20-35 smoothRB, 97-105 prolongAdd): the red-black update takes ghost
+ * values from the cell's old value, p <- mix(p, (sum_nb - h^2 b) / 6, omega), prolongation is clamp-to-edge
+ * trilinear without sign flips, and the coarsest level gets `coarse_sweeps` sweeps (poisson.mjs: 30,
+ * bench.js benchMG: 16).  Restriction and the level hierarchy are unchanged.  With h = 1 the levels have
+ * h^2 = 4^l as in the studies.  Lets the GPU reproduce the studies' recorded residual histories.           */
+int fire_poisson_set_study(FirePoisson* ps, int coarse_sweeps);
 
 /* ---- discrete adjoint of the step and checkpointed rollouts -----------------------------------------
  * Reverse-mode derivatives of FireSim.step (src/sim.js:627-648) over a rollout of n steps: the adjoint of

@@ -216,12 +216,21 @@ inline void store4(std::vector<R>& f, int x, int y, int z, int nx, int ny, const
 }
 
 // One axis of the clamp-to-edge linear filter: u is the continuous cell coordinate (texel centre at i+.5)
+// Texture-unit filter weights: the reference samples its fields through the GPU's linear filter, whose
+// interpolation weights are fixed point with about 8 fractional bits, i.e. 1/256 steps (research/webgpu.md,
+// "Filter weight precision").  fbits > 0 rounds each axis fraction to the nearest multiple of 2^-fbits;
+// fbits = 0 keeps exact weights (the semantics of the CUDA kernels).
+template <class R> inline R quant_frac(R f, int fbits) {
+  if (fbits <= 0) return f;
+  const R sc = R(1 << fbits);
+  return std::floor(f * sc + R(0.5)) / sc;
+}
 template <class R>
-inline void axis_clamp(R c, int n, int& i0, int& i1, R& f) {
+inline void axis_clamp(R c, int n, int& i0, int& i1, R& f, int fbits = 0) {
   R u = clampf(c - R(0.5), R(-1), R(n));       // clamping u to [-1, n] does not change a clamp-to-edge sample
   R fl = std::floor(u);
   int i = (int)fl;
-  f = u - fl;
+  f = quant_frac(u - fl, fbits);
   i0 = std::min(std::max(i, 0), n - 1);
   i1 = std::min(std::max(i + 1, 0), n - 1);
 }
@@ -231,9 +240,9 @@ inline V4<R> lerp4(const V4<R>& a, const V4<R>& b, R t) {
   return V4<R>(a.x * s + b.x * t, a.y * s + b.y * t, a.z * s + b.z * t, a.w * s + b.w * t);
 }
 template <class R>
-V4<R> sample_clamp(const std::vector<R>& f, int nx, int ny, int nz, const V3<R>& c) {
+V4<R> sample_clamp(const std::vector<R>& f, int nx, int ny, int nz, const V3<R>& c, int fbits = 0) {
   int x0, x1, y0, y1, z0, z1; R fx, fy, fz;
-  axis_clamp(c.x, nx, x0, x1, fx); axis_clamp(c.y, ny, y0, y1, fy); axis_clamp(c.z, nz, z0, z1, fz);
+  axis_clamp(c.x, nx, x0, x1, fx, fbits); axis_clamp(c.y, ny, y0, y1, fy, fbits); axis_clamp(c.z, nz, z0, z1, fz, fbits);
   V4<R> c00 = lerp4(load4(f, x0, y0, z0, nx, ny), load4(f, x1, y0, z0, nx, ny), fx);
   V4<R> c10 = lerp4(load4(f, x0, y1, z0, nx, ny), load4(f, x1, y1, z0, nx, ny), fx);
   V4<R> c01 = lerp4(load4(f, x0, y0, z1, nx, ny), load4(f, x1, y0, z1, nx, ny), fx);
@@ -242,10 +251,10 @@ V4<R> sample_clamp(const std::vector<R>& f, int nx, int ny, int nz, const V3<R>&
 }
 // Repeat-addressed sample of a 128^3 table given in normalised coordinates (sim.js:69, 228, 365)
 template <class R>
-V4<R> sample_repeat(const float* tab, int N, const V3<R>& q) {
+V4<R> sample_repeat(const float* tab, int N, const V3<R>& q, int fbits = 0) {
   R ux = q.x * R(N) - R(0.5), uy = q.y * R(N) - R(0.5), uz = q.z * R(N) - R(0.5);
   R flx = std::floor(ux), fly = std::floor(uy), flz = std::floor(uz);
-  R fx = ux - flx, fy = uy - fly, fz = uz - flz;
+  R fx = quant_frac(ux - flx, fbits), fy = quant_frac(uy - fly, fbits), fz = quant_frac(uz - flz, fbits);
   // wrap in 64-bit to stay defined for any finite coordinate
   long long ix = (long long)flx, iy = (long long)fly, iz = (long long)flz;
   auto wr = [N](long long i) { long long m = i % N; return (int)(m < 0 ? m + N : m); };
@@ -296,7 +305,20 @@ template <class R> struct Sim {
   std::vector<float> logs;          // nLogs * 8
   std::vector<float> noise, curl;   // 128^3 * 4 each (half-rounded values)
   int tabN = 128;
+  // Solver and storage modes.  omega: over-relaxation of every multigrid sweep (1 = the reference's
+  // Gauss-Seidel update).  store_half: every float4 field (vel, S, S2, their advected copies, vort, geo) is
+  // rounded to IEEE half after the stage that writes it, as the reference's rgba16float textures store it
+  // (src/sim.js:71-76, 143-145, 163-165, 202); p and b stay FP32 (r32float, src/sim.js:84).  filter_bits:
+  // fractional bits of the trilinear weights of every texture sample (0 = exact).
+  float omega = 1.0f;
+  int store_half = 0;
+  int filter_bits = 0;
 };
+// rgba16float store: rounds every component of a float4 field to the nearest IEEE half.
+template <class R> void round_field_half(std::vector<R>& f) {
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)f.size(); ++i) f[(size_t)i] = (R)round_half((float)f[(size_t)i]);
+}
 
 template <class R> void sim_alloc(Sim<R>& s, int nx, int ny, int nz, double dx) {   // sim.js:71-92
   s.nx = nx; s.ny = ny; s.nz = nz; s.N = (size_t)nx * ny * nz;
@@ -360,7 +382,7 @@ template <class R> void k_geo(Sim<R>& s) {
 // ---------------- advection (src/sim.js:123-197) ----------------
 template <class R> struct AdvCtx {
   const Sim<R>* s; R dt, dx; R nxf, nyf, nzf;
-  V3<R> sampleVel(const V3<R>& c) const { return sample_clamp(s->vel, s->nx, s->ny, s->nz, c).xyz(); }
+  V3<R> sampleVel(const V3<R>& c) const { return sample_clamp(s->vel, s->nx, s->ny, s->nz, c, s->filter_bits).xyz(); }
   V3<R> backtrace(const V3<R>& c) const {                            // sim.js:130-135
     V3<R> v0 = sampleVel(c);
     V3<R> mid = c - v0 * (R(0.5) * dt) / dx;
@@ -386,11 +408,11 @@ template <class R> void k_adv1(Sim<R>& s) {                           // sim.js:
         R f = A.outsideFade(b);
         R ws = smoothstep(R(0.03), R(0.4), b.y * A.dx);
         V3<R> wind(windX * ws, R(0) * ws, windZ * ws);
-        V3<R> sv = sample_clamp(s.vel, s.nx, s.ny, s.nz, b).xyz();
+        V3<R> sv = sample_clamp(s.vel, s.nx, s.ny, s.nz, b, s.filter_bits).xyz();
         V3<R> vo(mixf(wind.x, sv.x, f), mixf(wind.y, sv.y, f), mixf(wind.z, sv.z, f));
         store4(s.velX, i, j, k, s.nx, s.ny, V4<R>(vo.x, vo.y, vo.z, R(0)));
-        store4(s.SX, i, j, k, s.nx, s.ny, sample_clamp(s.S, s.nx, s.ny, s.nz, b) * f);
-        store4(s.S2X, i, j, k, s.nx, s.ny, sample_clamp(s.S2, s.nx, s.ny, s.nz, b) * f);
+        store4(s.SX, i, j, k, s.nx, s.ny, sample_clamp(s.S, s.nx, s.ny, s.nz, b, s.filter_bits) * f);
+        store4(s.S2X, i, j, k, s.nx, s.ny, sample_clamp(s.S2, s.nx, s.ny, s.nz, b, s.filter_bits) * f);
       }
 }
 template <class R> void k_adv2(Sim<R>& s) {                           // sim.js:159-197
@@ -406,9 +428,9 @@ template <class R> void k_adv2(Sim<R>& s) {                           // sim.js:
         V3<R> vH = load4(s.velX, i, j, k, nx, ny).xyz();
         V4<R> sH = load4(s.SX, i, j, k, nx, ny);
         V4<R> s2H = load4(s.S2X, i, j, k, nx, ny);
-        V3<R> vN = vH + (v - sample_clamp(s.velX, nx, ny, nz, fw).xyz()) * R(0.5);
-        V4<R> sN = sH + (load4(s.S, i, j, k, nx, ny) - sample_clamp(s.SX, nx, ny, nz, fw)) * R(0.5);
-        V4<R> s2N = s2H + (load4(s.S2, i, j, k, nx, ny) - sample_clamp(s.S2X, nx, ny, nz, fw)) * R(0.5);
+        V3<R> vN = vH + (v - sample_clamp(s.velX, nx, ny, nz, fw, s.filter_bits).xyz()) * R(0.5);
+        V4<R> sN = sH + (load4(s.S, i, j, k, nx, ny) - sample_clamp(s.SX, nx, ny, nz, fw, s.filter_bits)) * R(0.5);
+        V4<R> s2N = s2H + (load4(s.S2, i, j, k, nx, ny) - sample_clamp(s.S2X, nx, ny, nz, fw, s.filter_bits)) * R(0.5);
         V3<R> bt = A.backtrace(c);
         V3<R> b(bt.x - R(0.5), bt.y - R(0.5), bt.z - R(0.5));
         V3<R> bc(clampf(b.x, R(-2), R(nx + 1)), clampf(b.y, R(-2), R(ny + 1)), clampf(b.z, R(-2), R(nz + 1)));
@@ -452,7 +474,7 @@ template <class R> void k_curl(Sim<R>& s) {
 
 // ---------------- forces (src/sim.js:214-396) ----------------
 template <class R> inline V4<R> noise4(const Sim<R>& s, const V3<R>& q) {     // sim.js:228
-  V4<R> t = sample_repeat(s.noise.data(), s.tabN, q);
+  V4<R> t = sample_repeat(s.noise.data(), s.tabN, q, s.filter_bits);
   return V4<R>(t.x * R(2) - R(1), t.y * R(2) - R(1), t.z * R(2) - R(1), t.w * R(2) - R(1));
 }
 template <class R> void k_forces(Sim<R>& s) {
@@ -588,7 +610,7 @@ template <class R> void k_forces(Sim<R>& s) {
 
         // ---- curl-noise turbulence (sim.js:364-368)
         V3<R> tq = (p - V3<R>(R(0), time * (R)P[P_turbRise], R(0))) * (R)P[P_turbFreq] + V3<R>(R(0), R(0), time * (R)P[P_turbEvolve]);
-        V3<R> cn = sample_repeat(s.curl.data(), s.tabN, tq).xyz();
+        V3<R> cn = sample_repeat(s.curl.data(), s.tabN, tq, s.filter_bits).xyz();
         R tgate = fmx(smoothstep(R(500), R(1100), T), smoothstep(R(0), R(3), sv.w)) * (R(1) - srcAll) *
                   mixf(R(0.6), R(1.8), smoothstep(R(0.2), R(0.75), p.y)) * lam;
         v = v + cn * ((R)P[P_turbAmp] / R(12)) * tgate * dt * R(10);
@@ -644,7 +666,9 @@ template <class R> void k_div(Sim<R>& s) {
 }
 
 // ---------------- multigrid (src/sim.js:415-495, 576-599) ----------------
-template <class R> void k_smooth(Level<R>& L, int color) {            // sim.js:417-437
+// omega != 1 over-relaxes the update, p <- fma(omega, p_gs - p, p) (one rounding, as the CUDA sweep computes
+// it); omega == 1 is mgSmooth's Gauss-Seidel update.
+template <class R> void k_smooth(Level<R>& L, int color, R omega = R(1)) {            // sim.js:417-437
   const int nx = L.nx, ny = L.ny, nz = L.nz;
   const R h2 = L.h * L.h;
 #pragma omp parallel for schedule(static)
@@ -658,7 +682,9 @@ template <class R> void k_smooth(Level<R>& L, int color) {            // sim.js:
         if (z < nz - 1) sum += L.p[cidx(x, y, z + 1, nx, ny)]; else diag += R(1);
         if (y > 0) sum += L.p[cidx(x, y - 1, z, nx, ny)]; else diag -= R(1);
         if (y < ny - 1) sum += L.p[cidx(x, y + 1, z, nx, ny)]; else diag += R(1);
-        L.p[cidx(x, y, z, nx, ny)] = (sum - h2 * L.b[cidx(x, y, z, nx, ny)]) / diag;
+        const R gs = (sum - h2 * L.b[cidx(x, y, z, nx, ny)]) / diag;
+        R& pc = L.p[cidx(x, y, z, nx, ny)];
+        pc = omega == R(1) ? gs : std::fma(omega, gs - pc, pc);
       }
 }
 template <class R> inline R pghost(const Level<R>& L, int x, int y, int z, R me) {   // sim.js:446-450
@@ -709,7 +735,8 @@ template <class R> void k_prolong(Level<R>& F, const Level<R>& C) {   // sim.js:
       }
 }
 template <class R> void smooth_iters(Sim<R>& s, int i, int iters) {   // sim.js:576-586
-  for (int k = 0; k < iters; ++k) { k_smooth(s.levels[i], 0); k_smooth(s.levels[i], 1); }
+  const R w = (R)s.omega;
+  for (int k = 0; k < iters; ++k) { k_smooth(s.levels[i], 0, w); k_smooth(s.levels[i], 1, w); }
 }
 template <class R> void vcycle(Sim<R>& s, int pre = 2, int post = 2) {   // sim.js:588-599
   const int n = (int)s.levels.size();
@@ -764,6 +791,19 @@ template <class R> void k_project(Sim<R>& s) {
 // ---------------- full step (src/sim.js:627-648) ----------------
 enum { ST_GEO = 0, ST_ADV1, ST_ADV2, ST_CURL, ST_FORCES, ST_DIV, ST_VCYCLE, ST_PROJECT };
 
+// In the rgba16float storage mode, the float4 fields a stage wrote are rounded to half after it.
+template <class R> void store_stage_outputs(Sim<R>& s, int st) {
+  if (!s.store_half) return;
+  switch (st) {
+    case ST_GEO: round_field_half(s.geo); break;
+    case ST_ADV1: round_field_half(s.velX); round_field_half(s.SX); round_field_half(s.S2X); break;
+    case ST_ADV2: round_field_half(s.velY); round_field_half(s.SY); round_field_half(s.S2Y); break;
+    case ST_CURL: round_field_half(s.vort); break;
+    case ST_FORCES: round_field_half(s.velX); round_field_half(s.S); round_field_half(s.S2); break;
+    case ST_PROJECT: round_field_half(s.vel); break;
+    default: break;
+  }
+}
 template <class R> void run_stage(Sim<R>& s, int st) {
   switch (st) {
     case ST_GEO: k_geo(s); break;
@@ -775,6 +815,7 @@ template <class R> void run_stage(Sim<R>& s, int st) {
     case ST_VCYCLE: vcycle(s); break;
     case ST_PROJECT: k_project(s); break;
   }
+  store_stage_outputs(s, st);
 }
 
 // ---------------- Poisson known-answer study (research/webgpu-bench/poisson.mjs) ----------------
@@ -1003,6 +1044,45 @@ void orc_build_campfire(uint32_t seed, float* out128) {
     for (int c = 0; c < 8; ++c) out128[i * 8 + c] = (float)logs[i][c];
 }
 
+// SIM_DEFAULTS (src/sim.js:25-44) as the 64-float uniform block in SIM_FIELDS order (src/sim.js:14-23).
+// The entries the simulation fills itself (dims, dx, dt, time, frame, seed, origin, nLogs) and the padding
+// to 64 floats are 0.
+void orc_sim_defaults(float* out64) {
+  for (int i = 0; i < 64; ++i) out64[i] = 0.0f;
+  const struct { int k; float v; } d[] = {
+    {P_fuelSrc, 0.13f}, {P_bedFuel, 0.16f}, {P_srcTemp, 0.75f}, {P_bedTemp, 0.82f}, {P_srcVel, 0.25f},
+    {P_srcFreq, 35.0f}, {P_srcSpeed, 0.06f}, {P_srcThresh, 0.0f},
+    {P_ignT, 550.0f}, {P_kMix, 30.0f}, {P_rs, 4.7f}, {P_heatOut, 7700.0f}, {P_expansion, 0.7f},
+    {P_sootForm, 25.0f}, {P_sootOx, 30.0f}, {P_radCool, 0.25f},
+    {P_coolRate, 3.0f}, {P_sootDissip, 0.4f}, {P_smokeDissip, 0.3f}, {P_vitDecay, 1.5f}, {P_fuelDissip, 0.3f},
+    {P_buoyancy, 26.8f},
+    {P_vortEps, 8.0f}, {P_turbAmp, 0.8f}, {P_turbFreq, 1.5f}, {P_turbRise, 1.5f}, {P_turbEvolve, 0.6f},
+    {P_windX, 0.0f}, {P_windZ, 0.0f}, {P_gust, 0.0f}, {P_intensity, 1.0f}, {P_velDissip, 0.05f},
+    {P_bedRadius, 0.22f}, {P_hotR0, 0.12f}, {P_hotR1, 0.45f}, {P_hotY1, 0.5f}, {P_logSrc, 1.0f},
+    {P_burstX, 0.0f}, {P_burstY, 0.0f}, {P_burstZ, 0.0f}, {P_burstAmt, 0.0f}, {P_smolder, 0.02f}, {P_sponge, 1.0f},
+    {P_visc, 0.0f}, {P_lamAge, 0.0f}, {P_anchorFreq, 1.6f}, {P_srcFloor, 0.25f}, {P_anchorGain, 0.95f},
+  };
+  for (const auto& e : d) out64[e.k] = e.v;
+}
+// Seeded pyrolysis spots of the synthetic workloads (a build-defined emitter; the reference has none):
+// spot i sits at radius r sqrt(u), angle 2 pi v on the floor, with u = rand2(seed, 2i), v = rand2(seed, 2i+1)
+// and flux lo + (hi - lo) rand2(seed ^ 0x9e3779b9, i), where rand2(n, m) = pcg(n ^ pcg(m)) / (2^32 - 1) is the
+// hash of src/shaders/lib.js:18 divided in double on the host; 5 floats per spot (x, y, z, sigma, flux g/s),
+// evaluated in double and stored as float.
+void orc_make_spots(uint32_t seed, int n, float lo, float hi, float sigma, float radius, float* out) {
+  const double PI = 3.141592653589793;
+  auto r2 = [](uint32_t a, uint32_t b) { return (double)pcg1(a ^ pcg1(b)) / 4294967295.0; };
+  for (int i = 0; i < n; ++i) {
+    const double u = r2(seed, 2u * (uint32_t)i), v = r2(seed, 2u * (uint32_t)i + 1u), w = r2(seed ^ 0x9e3779b9u, (uint32_t)i);
+    const double r = (double)radius * std::sqrt(u), th = 2.0 * PI * v;
+    out[5 * i + 0] = (float)(r * std::cos(th));
+    out[5 * i + 1] = 0.0f;
+    out[5 * i + 2] = (float)(r * std::sin(th));
+    out[5 * i + 3] = sigma;
+    out[5 * i + 4] = (float)((double)lo + ((double)hi - (double)lo) * w);
+  }
+}
+
 void* orc_create(int nx, int ny, int nz, double dx, int dbl) {
   OracleSim* o = new OracleSim();
   o->dbl = dbl;
@@ -1061,7 +1141,10 @@ int orc_set_level(void* h, int l, int which, const void* in, int as_double) {
 }
 void orc_stage(void* h, int st) { OracleSim* o = (OracleSim*)h; if (o->dbl) run_stage(o->d, st); else run_stage(o->f, st); }
 // MG pieces on explicit levels, for kernel-level parity.
-void orc_mg_smooth(void* h, int l, int color) { OracleSim* o = (OracleSim*)h; if (o->dbl) k_smooth(o->d.levels[l], color); else k_smooth(o->f.levels[l], color); }
+void orc_mg_smooth(void* h, int l, int color) {
+  OracleSim* o = (OracleSim*)h;
+  if (o->dbl) k_smooth(o->d.levels[l], color, (double)o->d.omega); else k_smooth(o->f.levels[l], color, o->f.omega);
+}
 void orc_mg_restrict(void* h, int l) { OracleSim* o = (OracleSim*)h; if (o->dbl) k_restrict(o->d.levels[l], o->d.levels[l + 1]); else k_restrict(o->f.levels[l], o->f.levels[l + 1]); }
 void orc_mg_prolong(void* h, int l) { OracleSim* o = (OracleSim*)h; if (o->dbl) k_prolong(o->d.levels[l], o->d.levels[l + 1]); else k_prolong(o->f.levels[l], o->f.levels[l + 1]); }
 void orc_mg_vcycle(void* h, int pre, int post) { OracleSim* o = (OracleSim*)h; if (o->dbl) vcycle(o->d, pre, post); else vcycle(o->f, pre, post); }
@@ -1074,8 +1157,8 @@ void orc_residual(void* h, double* rr, double* bb) { OracleSim* o = (OracleSim*)
 int orc_step(void* h, int rebuild_geo, int vcycles, double tol) {
   OracleSim* o = (OracleSim*)h;
   auto go = [&](auto& s) {
-    if (rebuild_geo) k_geo(s);
-    k_adv1(s); k_adv2(s); k_curl(s); k_forces(s); k_div(s);
+    if (rebuild_geo) run_stage(s, ST_GEO);
+    for (int st : {ST_ADV1, ST_ADV2, ST_CURL, ST_FORCES, ST_DIV}) run_stage(s, st);
     int done = 0;
     if (vcycles >= 0) { for (int i = 0; i < vcycles; ++i) vcycle(s); done = vcycles; }
     else {
@@ -1085,11 +1168,20 @@ int orc_step(void* h, int rebuild_geo, int vcycles, double tol) {
         if (std::sqrt(rr) <= tol * std::sqrt(bb)) break;
       }
     }
-    k_project(s);
+    run_stage(s, ST_PROJECT);
     return done;
   };
   return o->dbl ? go(o->d) : go(o->f);
 }
+// Solver / storage modes (see Sim): omega, rgba16float storage of the float4 fields, filter weight bits.
+void orc_set_modes(void* h, double omega, int store_half, int filter_bits) {
+  OracleSim* o = (OracleSim*)h;
+  o->f.omega = o->d.omega = (float)omega;
+  o->f.store_half = o->d.store_half = store_half;
+  o->f.filter_bits = o->d.filter_bits = filter_bits;
+}
+// Sweeps on the coarsest level (the constructor's coarseIters rule, src/sim.js:88-92, unless set here).
+void orc_set_coarse_iters(void* h, int iters) { OracleSim* o = (OracleSim*)h; o->f.coarseIters = o->d.coarseIters = iters; }
 // Reset (sim.js:606-618): zero every velocity / scalar / vorticity field and every pressure level.
 void orc_reset(void* h) {
   OracleSim* o = (OracleSim*)h;

@@ -65,6 +65,9 @@ def lib():
             "orc_sparks_step": (None, [vp, ip, vp, vp, ip, ip, ip, vp, ip]),
             "orc_volume_lights": (None, [vp, vp, ip, ip, ip, vp, vp, vp]),
             "orc_volume_render": (None, [vp, vp, vp, ip, ip, ip, vp, ip, vp, vp, vp, vp]),
+            "orc_set_modes": (None, [vp, dp, ip, ip]), "orc_set_coarse_iters": (None, [vp, ip]),
+            "orc_sim_defaults": (None, [vp]),
+            "orc_make_spots": (None, [ctypes.c_uint32, ip, fp, fp, fp, fp, vp]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -100,6 +103,28 @@ def build_campfire(seed: int = 7) -> np.ndarray:
     out = np.zeros(128, np.float32)
     lib().orc_build_campfire(seed, _ptr(out))
     return out
+
+
+def poisson_rhs(N: int) -> np.ndarray:
+    """The convergence study's right-hand side (research/webgpu-bench/poisson.mjs:78-92), (N, N, N) float32."""
+    out = np.zeros(N * N * N, np.float32)
+    lib().orc_poisson_rhs(int(N), _ptr(out))
+    return out.reshape(N, N, N)
+
+
+def sim_defaults() -> np.ndarray:
+    """SIM_DEFAULTS (src/sim.js:25-44) as the 64-float block in SIM_FIELDS order (simulation-owned slots 0)."""
+    out = np.zeros(64, np.float32)
+    lib().orc_sim_defaults(_ptr(out))
+    return out
+
+
+def make_spots(seed: int, n: int, flux_lo: float = 1.0, flux_hi: float = 4.0, sigma: float = 0.02,
+               radius: float = 0.15) -> np.ndarray:
+    """The synthetic workloads' seeded floor spots, (n, 5) = (x, y, z, sigma, flux g/s)."""
+    out = np.zeros((max(n, 1), 5), np.float32)
+    lib().orc_make_spots(int(seed) & 0xFFFFFFFF, int(n), float(flux_lo), float(flux_hi), float(sigma), float(radius), _ptr(out))
+    return out[:n]
 
 
 def poisson_study(N: int, face: bool, mode: int, omega: float = 1.0, pre: int = 2, post: int = 2,
@@ -270,7 +295,18 @@ class OracleSim:
         return float(rr[0]), float(bb[0])
 
     def step_raw(self, rebuild_geo: bool, vcycles: int, tol: float = 0.0) -> int:
+        """One step; vcycles < 0 solves to `tol` relative residual in at most -vcycles cycles (returns cycles run)."""
         return lib().orc_step(self.h, int(rebuild_geo), int(vcycles), float(tol))
+
+    def set_modes(self, omega: float = 1.0, store_half: bool = False, filter_bits: int = 0):
+        """omega: over-relaxation of every multigrid sweep (1 = Gauss-Seidel); store_half: round every float4
+        field to IEEE half after the stage that writes it (the reference's rgba16float textures); filter_bits:
+        fractional bits of the trilinear texture weights (0 = exact)."""
+        lib().orc_set_modes(self.h, float(omega), int(bool(store_half)), int(filter_bits))
+
+    def set_coarse_iters(self, iters: int):
+        lib().orc_set_coarse_iters(self.h, int(iters))
+        self.coarse_iters = int(iters)
 
     def reset(self):
         lib().orc_reset(self.h)

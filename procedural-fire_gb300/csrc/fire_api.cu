@@ -191,7 +191,7 @@ void record_vcycle(FireSim* s, cudaStream_t st) {
   const int T = s->tailFirst;
   const int top = std::min(T, n - 1);
   for (int i = 0; i < top; ++i) { record_smooth(s, i, 2, st); launch_restrict(s->levels[i], s->levels[i + 1], st); }
-  if (T < n) launch_tail(s->levels.data(), T, n, 2, 2, s->coarseIters, s->dCounter + 2, st);
+  if (T < n) launch_tail(s->levels.data(), T, n, 2, 2, s->coarseIters, s->dCounter + 2, st, false, nullptr, s->tailWaitPolls);
   else record_smooth(s, n - 1, s->coarseIters, st);
   for (int i = top - 1; i >= 0; --i) { launch_prolong(s->levels[i], s->levels[i + 1], st); record_smooth(s, i, 2, st); }
 }
@@ -600,6 +600,13 @@ int fire_sim_set_mg_omega(FireSim* sim, float omega) {
   return FIRE_OK;
 }
 
+int fire_sim_set_tail_wait_limit(FireSim* sim, int polls) {
+  if (!sim || polls < 0) return FIRE_ERR_BAD_ARG;
+  sim->tailWaitPolls = polls;
+  drop_graph(sim);   // the tail launch carries the limit in its descriptor
+  return FIRE_OK;
+}
+
 int fire_sim_set_spots(FireSim* sim, const float* spots, int n) {
   if (!sim || n < 0 || n > MAX_SPOTS || (n > 0 && !spots)) return FIRE_ERR_BAD_ARG;
   for (int i = 0; i < n; ++i)
@@ -787,7 +794,7 @@ int fire_sim_run_mg(FireSim* sim, int op, int level, int arg, void* stream) {
       break;
     case 4:   // the shared-memory V-cycle from `level` down, if it fits
       if (!tail_fits(sim->levels.data(), level, n)) return FIRE_ERR_BAD_ARG;
-      launch_tail(sim->levels.data(), level, n, 2, 2, sim->coarseIters, sim->dCounter + 2, st);
+      launch_tail(sim->levels.data(), level, n, 2, 2, sim->coarseIters, sim->dCounter + 2, st, false, nullptr, sim->tailWaitPolls);
       break;
     default: return FIRE_ERR_BAD_ARG;
   }

@@ -59,6 +59,11 @@ struct MGLevel {
   float* p;
   float* b;
   float omega = 1.0f;   // over-relaxation of the launch-per-sweep smoother (1: Gauss-Seidel, the reference's)
+  // 0: the simulation's multigrid (mgSmooth / mgProlong, src/sim.js:417-437, 468-495).  1: the variant of the
+  // reference's convergence studies (research/webgpu-bench/poisson.mjs:28-65, wgsl/mg.wgsl smoothRB /
+  // prolongAdd): ghost values from the cell's old value, p <- mix(p, (sum_nb - h^2 b) / 6, omega), and
+  // clamp-to-edge trilinear prolongation without sign flips.  Only the standalone solver's FP32 form sets it.
+  int study = 0;
 };
 
 // ---- batched launches over many independent simulations ----
@@ -135,9 +140,9 @@ void launch_div_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStrea
 void launch_project_batch(const BatchMap& m, const StepBatch& I, int tile, cudaStream_t st);
 
 // ---- kernel launchers (fire_mg.cu) ----
-void launch_smooth(const MGLevel& L, int color, cudaStream_t st);
-void launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st);
-void launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st);
+cudaError_t launch_smooth(const MGLevel& L, int color, cudaStream_t st);
+cudaError_t launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st);
+cudaError_t launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st);
 // One launch runs the V-cycle over levels [first, n) out of shared memory: a single CTA when every level
 // fits in its shared memory, or a thread-block cluster whose CTAs each hold a z-slab of the finer tail
 // levels (distributed shared memory for the slab edges) with the coarsest levels gathered on CTA 0.
@@ -150,9 +155,12 @@ constexpr long TAIL_FIRST_CELLS = 8192;
 int tail_first(const MGLevel* levels, int n, bool coarse64 = false, long max_cells = TAIL_FIRST_CELLS);
 // Shared memory per CTA of the tail launch for [first, n).
 size_t tail_smem_bytes(const MGLevel* levels, int first, int n, bool coarse64 = false);
-// `err` receives 1 if the kernel's bounded wait for its bulk copies ran out (the kernel then returns early).
-void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st,
-                 bool coarse64 = false, const double* cinv = nullptr);
+// `err` receives 1 if the single-CTA kernel's bounded wait for its bulk copies ran out (the kernel then
+// waits, at the full bound, for the copies in flight and returns without running the cycle).  wait_polls
+// bounds the first wait (TAIL_WAIT_POLLS; a fault-injection test lowers it).
+constexpr int TAIL_WAIT_POLLS = 1 << 22;
+cudaError_t launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st,
+                        bool coarse64 = false, const double* cinv = nullptr, int wait_polls = TAIL_WAIT_POLLS);
 // Opts the tail kernels into `max_tail_smem` bytes of dynamic shared memory on the current device.
 cudaError_t mg_configure(size_t max_tail_smem);
 // Batched forms: one launch per level operation over the simulations of a BatchMap.

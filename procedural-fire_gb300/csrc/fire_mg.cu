@@ -41,6 +41,19 @@ __device__ __forceinline__ float rb_update(const float* p, const float* b, int x
   // explicit FMA in every form of the sweep (launch per colour, shared-memory tails), so they give the same bits.
   return __fdividef(__fmaf_rn(-h2, b[c], sum), diag);
 }
+// The convergence studies' red-black update (research/webgpu-bench/wgsl/mg.wgsl smoothRB, poisson.mjs:28-35):
+// ghosts take the cell's old value (floor +p, open faces -p), summed x-, x+, y-, y+, z-, z+;
+// pg = (sum - h^2 b) / 6 and p <- mix(p, pg, omega) (pg itself when omega = 1).
+__device__ __forceinline__ float study_update(const float* p, const float* b, int x, int y, int z, int nx, int ny, int nz, float h2,
+                                              float omega) {
+  const int sy = nx, sz = nx * ny;
+  const int c = x + y * sy + z * sz;
+  const float pc = p[c];
+  const float s = (x > 0 ? p[c - 1] : -pc) + (x < nx - 1 ? p[c + 1] : -pc) + (y > 0 ? p[c - sy] : pc) +
+                  (y < ny - 1 ? p[c + sy] : -pc) + (z > 0 ? p[c - sz] : -pc) + (z < nz - 1 ? p[c + sz] : -pc);
+  const float pg = (s - h2 * b[c]) / 6.0f;
+  return omega == 1.0f ? pg : fmaf(omega, pg - pc, pc);
+}
 // Each thread updates SMZ cells of one colour, SMZ planes apart in z (unrolled and independent, so their
 // loads are in flight together): the sweep is latency-bound on L2 hits, and fewer, longer CTAs also cut the
 // CTA turnover that leaves warp slots idle.
@@ -50,7 +63,7 @@ __device__ __forceinline__ float rb_update(const float* p, const float* b, int x
 constexpr int SMZ = FIRE_SMOOTH_Z;
 // omega != 1 over-relaxes the update (p + omega (p_gs - p)); omega == 1 is the reference's Gauss-Seidel
 // update bit for bit.
-template <bool kRelax>
+template <bool kRelax, bool kStudy = false>
 __device__ __forceinline__ void smooth_body_t(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz, float h, int color,
                                               uint3 blk, float omega) {
   pdl_wait();
@@ -65,6 +78,10 @@ __device__ __forceinline__ void smooth_body_t(float* __restrict__ p, const float
     const int z = zb + k;
     const int x = gx * 2 + ((y + z + color) & 1);
     if (z < nz && x < nx) {
+      if (kStudy) {
+        v[k] = study_update(p, b, x, y, z, nx, ny, nz, h2, omega);
+        continue;
+      }
       v[k] = rb_update(p, b, x, y, z, nx, ny, nz, h2);
       if (kRelax) {
         const float old = p[x + nx * (y + ny * z)];
@@ -119,6 +136,7 @@ __device__ __forceinline__ void restrict_body(const float* __restrict__ p, const
 }
 
 // ---------------- prolongation with mirror ghosts (src/sim.js:468-495) ----------------
+template <bool kClamp = false>
 __device__ __forceinline__ float prolong_cell(const float* pc, int x, int y, int z, int ncx, int ncy, int ncz) {
   const float gx = ((float)x + 0.5f) * 0.5f - 0.5f, gy = ((float)y + 0.5f) * 0.5f - 0.5f, gz = ((float)z + 0.5f) * 0.5f - 0.5f;
   const int g0x = (int)floorf(gx), g0y = (int)floorf(gy), g0z = (int)floorf(gz);
@@ -129,10 +147,13 @@ __device__ __forceinline__ float prolong_cell(const float* pc, int x, int y, int
     const int ox = q & 1, oy = (q >> 1) & 1, oz = (q >> 2) & 1;
     const int qx = g0x + ox, qy = g0y + oy, qz = g0z + oz;
     float val = pc[min(max(qx, 0), ncx - 1) + ncx * (min(max(qy, 0), ncy - 1) + ncy * min(max(qz, 0), ncz - 1))];
-    // odd mirror (Dirichlet) on sides/top, even (Neumann) at the floor; one flip per axis outside
-    if (qx < 0 || qx >= ncx) val = -val;
-    if (qz < 0 || qz >= ncz) val = -val;
-    if (qy >= ncy) val = -val;
+    // odd mirror (Dirichlet) on sides/top, even (Neumann) at the floor; one flip per axis outside (the
+    // studies' prolongation clamps to the edge without flips)
+    if (!kClamp) {
+      if (qx < 0 || qx >= ncx) val = -val;
+      if (qz < 0 || qz >= ncz) val = -val;
+      if (qy >= ncy) val = -val;
+    }
     const float wx = ox ? fx : 1.0f - fx, wy = oy ? fy : 1.0f - fy, wz = oz ? fz : 1.0f - fz;
     acc += val * wx * wy * wz;
   }
@@ -142,6 +163,7 @@ __device__ __forceinline__ float prolong_cell(const float* pc, int x, int y, int
 // loaded once and the 8 fine children are formed from it.  For fine index c = 2 cc + d the trilinear base is
 // g0 = cc - 1 + d with fraction 0.75 (d = 0) or 0.25 (d = 1), so child d reads coarse offsets d-1 and d;
 // each child's sum runs in prolong_cell's order, so the result is identical.
+template <bool kClamp = false>
 __device__ __forceinline__ void prolong_body(float* __restrict__ p, const float* __restrict__ pc, int nx, int ny, int nz, uint3 blk) {
   pdl_wait();
   pdl_trigger();
@@ -157,9 +179,11 @@ __device__ __forceinline__ void prolong_body(float* __restrict__ p, const float*
       for (int c = 0; c < 3; ++c) {
         const int qx = cx + c - 1, qy = cy + bb - 1, qz = cz + a - 1;
         float val = __ldg(pc + min(max(qx, 0), ncx - 1) + ncx * (min(max(qy, 0), ncy - 1) + ncy * min(max(qz, 0), ncz - 1)));
-        if (qx < 0 || qx >= ncx) val = -val;
-        if (qz < 0 || qz >= ncz) val = -val;
-        if (qy >= ncy) val = -val;
+        if (!kClamp) {
+          if (qx < 0 || qx >= ncx) val = -val;
+          if (qz < 0 || qz >= ncz) val = -val;
+          if (qy >= ncy) val = -val;
+        }
         v[a][bb][c] = val;
       }
 #pragma unroll
@@ -193,6 +217,14 @@ __global__ void __launch_bounds__(GX * GY * GZ) k_restrict(const float* __restri
 }
 __global__ void __launch_bounds__(GX * GY * GZ) k_prolong(float* __restrict__ p, const float* __restrict__ pc, int nx, int ny, int nz) {
   prolong_body(p, pc, nx, ny, nz, blockIdx);
+}
+// The convergence studies' smoother and prolongation (MGLevel::study).
+__global__ void __launch_bounds__(GX * GY * GZ) k_smooth_study(float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
+                                                               float h, int color, float omega) {
+  smooth_body_t<false, true>(p, b, nx, ny, nz, h, color, blockIdx, omega);
+}
+__global__ void __launch_bounds__(GX * GY * GZ) k_prolong_clamp(float* __restrict__ p, const float* __restrict__ pc, int nx, int ny, int nz) {
+  prolong_body<true>(p, pc, nx, ny, nz, blockIdx);
 }
 __global__ void __launch_bounds__(GX * GY * GZ) k_smooth_b(const __grid_constant__ BatchMap m, const __grid_constant__ LevelBatch L, int color) {
   uint3 blk; int i;
@@ -233,6 +265,8 @@ struct TailLevels {
   int coarse64;                // 1: the coarsest level is solved in FP64: p = cinv b with the dense inverse
   int doff;                    //    (transposed, global memory) if cinv is set, else `coarse` FP64 sweeps on a
   const double* cinv;          //    double copy at float offset doff
+  int study;                   // 1: the convergence studies' smoother and prolongation (MGLevel::study)
+  int wait_polls;              // poll limit of the wait for the staging copies (TAIL_WAIT_POLLS; a test lowers it)
 };
 struct FastDiv {
   int d;
@@ -268,7 +302,7 @@ struct Box3 {
     if (z0 >= tz) z0 = 1 << 30;   // surplus thread: its loops never run (prolongation is read-modify-write)
   }
 };
-template <bool kWarp, bool kRelax>
+template <bool kWarp, bool kRelax, bool kStudy = false>
 __device__ void tail_smooth_t(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters, float omega) {
   const int hx = (nx + 1) >> 1;
   const float h2 = h * h;
@@ -281,6 +315,10 @@ __device__ void tail_smooth_t(const Team<kWarp>& tm, float* p, const float* b, i
             const int x = gx * 2 + ((y + z + color) & 1);
             if (x < nx) {
               const int c = x + nx * (y + ny * z);
+              if (kStudy) {
+                p[c] = study_update(p, b, x, y, z, nx, ny, nz, h2, omega);
+                continue;
+              }
               const float v = rb_update(p, b, x, y, z, nx, ny, nz, h2);
               p[c] = kRelax ? fmaf(omega, v - p[c], p[c]) : v;
             }
@@ -290,8 +328,10 @@ __device__ void tail_smooth_t(const Team<kWarp>& tm, float* p, const float* b, i
 }
 // `iters` red-black sweeps of one level (over-relaxed by omega when omega != 1).
 template <bool kWarp>
-__device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters, float omega) {
-  if (omega == 1.0f) tail_smooth_t<kWarp, false>(tm, p, b, nx, ny, nz, h, iters, omega);
+__device__ void tail_smooth(const Team<kWarp>& tm, float* p, const float* b, int nx, int ny, int nz, float h, int iters, float omega,
+                            int study = 0) {
+  if (study) tail_smooth_t<kWarp, false, true>(tm, p, b, nx, ny, nz, h, iters, omega);
+  else if (omega == 1.0f) tail_smooth_t<kWarp, false>(tm, p, b, nx, ny, nz, h, iters, omega);
   else tail_smooth_t<kWarp, true>(tm, p, b, nx, ny, nz, h, iters, omega);
 }
 // `iters` red-black sweeps in FP64 on a double copy (dp: p then b) of one level; p is written back in FP32.
@@ -374,7 +414,7 @@ __device__ void tail_prolong(const Team<kWarp>& tm, const TailLevels& T, float* 
     for (int y = bx.y0; y < ny; y += bx.ty)
       for (int x = bx.x0; x < nx; x += bx.tx) {
         const int t = x + nx * (y + ny * z);
-        p[t] = p[t] + prolong_cell(pc, x, y, z, nx / 2, ny / 2, nz / 2);
+        p[t] = p[t] + (T.study ? prolong_cell<true>(pc, x, y, z, nx / 2, ny / 2, nz / 2) : prolong_cell(pc, x, y, z, nx / 2, ny / 2, nz / 2));
       }
   tm.sync();
 }
@@ -384,7 +424,7 @@ __device__ void tail_vcycle(const Team<kWarp>& tm, const TailLevels& T, float* s
   const int n = T.n;
   for (int l = from; l < n - 1; ++l) {
     float* p = sm + T.off[l];
-    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega);
+    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega, T.study);
     tail_restrict(tm, T, sm, l);
   }
   {
@@ -395,12 +435,12 @@ __device__ void tail_vcycle(const Team<kWarp>& tm, const TailLevels& T, float* s
       tail_smooth_fp64(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse,
                        reinterpret_cast<double*>(sm + T.doff));
     else
-      tail_smooth(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse, T.omega);
+      tail_smooth(tm, p, p + T.nx[n - 1] * T.ny[n - 1] * T.nz[n - 1], T.nx[n - 1], T.ny[n - 1], T.nz[n - 1], T.h[n - 1], coarse, T.omega, T.study);
   }
   for (int l = n - 2; l >= from; --l) {
     tail_prolong(tm, T, sm, l);
     float* p = sm + T.off[l];
-    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega);
+    tail_smooth(tm, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega, T.study);
   }
 }
 // The V-cycle over all levels of T with one CTA of TAIL_THREADS threads: levels above T.small with the
@@ -437,14 +477,14 @@ __device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre
     const int n = T.n, top = min(S, n - 1);
     for (int l = 0; l < top; ++l) {
       float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega);
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega, T.study);
       tail_restrict(cta, T, sm, l);
     }
     if (tid < 32) {
       const Team<true> wp{tid};
       for (int l = top; l < n - 1; ++l) {
         float* p = sm + T.off[l];
-        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega);
+        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega, T.study);
         tail_restrict(wp, T, sm, l);
       }
     }
@@ -459,14 +499,14 @@ __device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre
       for (int l = n - 2; l >= top; --l) {
         tail_prolong(wp, T, sm, l);
         float* p = sm + T.off[l];
-        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega);
+        tail_smooth(wp, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega, T.study);
       }
     }
     __syncthreads();
     for (int l = top - 1; l >= 0; --l) {
       tail_prolong(cta, T, sm, l);
       float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega);
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega, T.study);
     }
     return;
   }
@@ -479,7 +519,7 @@ __device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre
     // large levels [0, S) with the whole CTA; the V-cycle below S (levels S..n-1) on warp 0
     for (int l = 0; l < S; ++l) {
       float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega);
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], pre, T.omega, T.study);
       tail_restrict(cta, T, sm, l);
     }
     if (tid < 32) tail_vcycle(Team<true>{tid}, T, sm, S, pre, post, coarse);
@@ -487,7 +527,7 @@ __device__ void tail_cta_vcycle(const TailLevels& T, float* sm, int tid, int pre
     for (int l = S - 1; l >= 0; --l) {
       tail_prolong(cta, T, sm, l);
       float* p = sm + T.off[l];
-      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega);
+      tail_smooth(cta, p, p + T.nx[l] * T.ny[l] * T.nz[l], T.nx[l], T.ny[l], T.nz[l], T.h[l], post, T.omega, T.study);
     }
   }
 }
@@ -509,11 +549,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Waits for phase 0 of the barrier for at most about a second (and at most 2^22 polls); returns false if the
-// limit was reached.
-__device__ __forceinline__ bool mbar_wait0(uint64_t* bar) {
+// Waits for phase 0 of the barrier for at most about a second and at most max_polls polls; returns false if
+// a limit was reached.
+__device__ __forceinline__ bool mbar_wait0(uint64_t* bar, int max_polls = TAIL_WAIT_POLLS) {
   const unsigned long long t0 = global_ns();
-  for (int it = 0; it < (1 << 22); ++it) {
+  for (int it = 0; it < max_polls; ++it) {
     unsigned done;
     asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
                  : "=r"(done) : "r"(smem_addr(bar)), "r"(0u) : "memory");
@@ -554,11 +594,11 @@ __device__ __forceinline__ void tail_body(const TailLevels& T, int pre, int post
         bulk_g2s(b, T.gb[0], bytes, &bar);
       }
       __syncthreads();                        // the barrier is initialised before anyone polls it
-      if (!mbar_wait0(&bar)) {                // bounded wait: report and leave instead of hanging
+      if (!mbar_wait0(&bar, T.wait_polls)) {  // bounded wait: report and leave instead of hanging
         if (tid == 0) atomicExch(err, 1);
-        // copies may still be landing in this CTA's shared memory: a second bounded wait for them before the
-        // CTA exits and its shared memory can be handed to another CTA
-        mbar_wait0(&bar);
+        // copies may still be landing in this CTA's shared memory: a second wait, at the full bound, for them
+        // before the CTA exits and its shared memory can be handed to another CTA
+        mbar_wait0(&bar, TAIL_WAIT_POLLS);
         return;
       }
     } else {
@@ -968,20 +1008,20 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
 static dim3 grid3(int x, int y, int z) { return dim3((x + GX - 1) / GX, (y + GY - 1) / GY, (z + GZ - 1) / GZ); }
 static const dim3 kBlock(GX, GY, GZ);
 
-void launch_smooth(const MGLevel& L, int color, cudaStream_t st) {
-  launch_pdl(k_smooth, grid3((L.nx + 1) >> 1, L.ny, (L.nz + SMZ - 1) / SMZ), kBlock, 0, st, L.p, (const float*)L.b, L.nx, L.ny,
-             L.nz, L.h, color, L.omega);
+cudaError_t launch_smooth(const MGLevel& L, int color, cudaStream_t st) {
+  return launch_pdl(L.study ? k_smooth_study : k_smooth, grid3((L.nx + 1) >> 1, L.ny, (L.nz + SMZ - 1) / SMZ), kBlock, 0, st, L.p,
+             (const float*)L.b, L.nx, L.ny, L.nz, L.h, color, L.omega);
 }
-void launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
-  launch_pdl(k_restrict, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (const float*)F.p, (const float*)F.b, F.nx, F.ny, F.nz, F.h, C.b, C.p);
+cudaError_t launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
+  return launch_pdl(k_restrict, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (const float*)F.p, (const float*)F.b, F.nx, F.ny, F.nz, F.h, C.b, C.p);
 }
-void launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
-  launch_pdl(k_prolong, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, F.p, (const float*)C.p, F.nx, F.ny, F.nz);
+cudaError_t launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
+  return launch_pdl(F.study ? k_prolong_clamp : k_prolong, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, F.p, (const float*)C.p, F.nx, F.ny, F.nz);
 }
 // Number of leading levels of [first, n) that the cluster tail distributes: each has z-planes for an even
 // number per CTA, at least CTAIL_MIN_CELLS cells per CTA, and a coarser level below it.
 static int tail_dist_levels(const MGLevel* levels, int first, int n) {
-  if (CTAIL_CLUSTER < 2) return 0;
+  if (CTAIL_CLUSTER < 2 || (first < n && levels[first].study)) return 0;   // the studies' variant runs single-CTA tails only
   int d = 0;
   for (int l = first; l < n - 1 && d < TAIL_MAX_LEVELS; ++l) {
     const MGLevel& L = levels[l];
@@ -1037,6 +1077,8 @@ static TailLevels make_tail_levels(const MGLevel* levels, int first, int n, int 
   }
   T.coarse = 0;
   T.omega = T.n > 0 ? levels[first].omega : 1.0f;
+  T.study = T.n > 0 ? levels[first].study : 0;
+  T.wait_polls = TAIL_WAIT_POLLS;
   T.coarse64 = coarse64 ? 1 : 0;
   T.doff = (int)tail_fp64_offset((size_t)off);
   T.cinv = coarse64 ? cinv : nullptr;
@@ -1059,13 +1101,14 @@ static CTailLevels make_ctail_levels(const MGLevel* levels, int first, int n, in
   T.G = make_tail_levels(levels, first + nd, n, off, coarse64, cinv);
   return T;
 }
-void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st, bool coarse64,
-                 const double* cinv) {
+cudaError_t launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int coarse, int* err, cudaStream_t st, bool coarse64,
+                        const double* cinv, int wait_polls) {
   const size_t smem = tail_smem_bytes(levels, first, n, coarse64);
   const int nd = tail_dist_levels(levels, first, n);
   if (nd == 0) {
-    launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), smem, st, make_tail_levels(levels, first, n, 0, coarse64, cinv), pre, post, coarse, err);
-    return;
+    TailLevels T = make_tail_levels(levels, first, n, 0, coarse64, cinv);
+    T.wait_polls = wait_polls;
+    return launch_pdl(k_tail, dim3(1), dim3(TAIL_THREADS), smem, st, T, pre, post, coarse, err);
   }
   const CTailLevels T = make_ctail_levels(levels, first, n, nd, coarse64, cinv);
   cudaLaunchConfig_t cfg = {};
@@ -1082,7 +1125,7 @@ void launch_tail(const MGLevel* levels, int first, int n, int pre, int post, int
   at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = 2;
-  cudaLaunchKernelEx(&cfg, k_ctail, T, pre, post, coarse);
+  return cudaLaunchKernelEx(&cfg, k_ctail, T, pre, post, coarse);
 }
 cudaError_t mg_configure(size_t max_tail_smem) {
   for (const void* k : {(const void*)k_tail, (const void*)k_ctail, (const void*)k_tail_b, (const void*)k_ctail_b}) {

@@ -7,8 +7,9 @@
 // right-hand side; every coarser multigrid level lives in one file-scope device array of fixed size that
 // the library holds on every GPU that loads it, until the process exits.
 //
-// The V-cycle is the step's own (same kernels, same level rules, same coarse sweep count), so the result
-// equals fire_sim_step's solve on the same arrays.
+// The V-cycle is the step's own (same kernels, same level rules, same coarse sweep count) with the
+// reference's Gauss-Seidel sweeps (omega 1), so the result equals the V-cycle fire_sim_step runs on the same
+// arrays with its default smoother, bit for bit.
 #include <cmath>
 #include <cstdint>
 #include <mutex>
@@ -33,7 +34,8 @@ std::mutex g_setup_mutex;
 DeviceSetup g_setup[64];
 
 // Once per device, with that device current: resolve the array's device address (in host code the
-// symbol name is only a host-side stand-in), opt the tail kernel into its shared memory, clear the flag.
+// symbol name is only a host-side stand-in) and opt the tail kernel into its shared memory.  No stream work
+// is issued: a file-scope device array starts zeroed when the module loads, so the timeout flag starts clear.
 int setup_device(int dev, unsigned char** base) {
   if (dev < 0 || dev >= 64) return FIRE_ERR_BAD_ARG;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -42,13 +44,16 @@ int setup_device(int dev, unsigned char** base) {
     void* ptr = nullptr;
     if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || ptr == nullptr) return FIRE_ERR_CUDA;
     if (mg_configure(TAIL_SMEM_BUDGET) != cudaSuccess) return FIRE_ERR_CUDA;
-    if (cudaMemset(static_cast<unsigned char*>(ptr) + NOALLOC_BYTES - NOALLOC_FLAG_BYTES, 0, NOALLOC_FLAG_BYTES) != cudaSuccess)
-      return FIRE_ERR_CUDA;
     s.base = static_cast<unsigned char*>(ptr);
     s.ready = true;
   }
   *base = s.base;
   return FIRE_OK;
+}
+bool device_ready(int dev) {
+  if (dev < 0 || dev >= 64) return false;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  return g_setup[dev].ready;
 }
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 }  // namespace
@@ -95,17 +100,41 @@ extern "C" int fire_poisson_vcycles_noalloc(float* p, const float* b, int nx, in
   const int T = tail_first(levels.data(), n);
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int top = std::min(T, n - 1);
-  for (int c = 0; c < cycles; ++c) {   // V(2,2) (src/sim.js:588-599), as the simulation records it
-    for (int i = 0; i < top; ++i) {
-      for (int k = 0; k < 2; ++k) { launch_smooth(levels[i], 0, st); launch_smooth(levels[i], 1, st); }
-      launch_restrict(levels[i], levels[i + 1], st);
+  // every launch's own status is checked, so an error left by the caller's earlier work is neither blamed on
+  // this call nor cleared by it
+  bool ok = true;
+  auto sweeps = [&](const MGLevel& L, int iters) {
+    for (int k = 0; k < iters && ok; ++k) ok = launch_smooth(L, 0, st) == cudaSuccess && launch_smooth(L, 1, st) == cudaSuccess;
+  };
+  for (int c = 0; c < cycles && ok; ++c) {   // V(2,2) (src/sim.js:588-599), as the simulation records it
+    for (int i = 0; i < top && ok; ++i) {
+      sweeps(levels[i], 2);
+      ok = ok && launch_restrict(levels[i], levels[i + 1], st) == cudaSuccess;
     }
-    if (T < n) launch_tail(levels.data(), T, n, 2, 2, coarse, err, st);
-    else for (int k = 0; k < coarse; ++k) { launch_smooth(levels[n - 1], 0, st); launch_smooth(levels[n - 1], 1, st); }
-    for (int i = top - 1; i >= 0; --i) {
-      launch_prolong(levels[i], levels[i + 1], st);
-      for (int k = 0; k < 2; ++k) { launch_smooth(levels[i], 0, st); launch_smooth(levels[i], 1, st); }
+    if (!ok) break;
+    if (T < n) ok = launch_tail(levels.data(), T, n, 2, 2, coarse, err, st) == cudaSuccess;
+    else sweeps(levels[n - 1], coarse);
+    for (int i = top - 1; i >= 0 && ok; --i) {
+      ok = launch_prolong(levels[i], levels[i + 1], st) == cudaSuccess;
+      sweeps(levels[i], 2);
     }
   }
-  return cudaGetLastError() == cudaSuccess ? FIRE_OK : FIRE_ERR_CUDA;
+  return ok ? FIRE_OK : FIRE_ERR_CUDA;
+}
+
+// Waits for `stream`, then reports and clears the timeout flag that the coarse-level kernel of the calls
+// above sets when its bounded wait for its staging copies runs out (it then skips that cycle's coarse
+// correction).  Synchronous; allocates nothing.
+extern "C" int fire_poisson_noalloc_status(void* stream) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return FIRE_ERR_CUDA;
+  if (!device_ready(dev)) return FIRE_OK;   // no call ran on this device
+  if (cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)) != cudaSuccess) return FIRE_ERR_CUDA;
+  int flag = 0;
+  const size_t at = NOALLOC_BYTES - NOALLOC_FLAG_BYTES;
+  if (cudaMemcpyFromSymbol(&flag, g_noalloc_scratch, sizeof flag, at) != cudaSuccess) return FIRE_ERR_CUDA;
+  if (!flag) return FIRE_OK;
+  const int zero = 0;
+  if (cudaMemcpyToSymbol(g_noalloc_scratch, &zero, sizeof zero, at) != cudaSuccess) return FIRE_ERR_CUDA;
+  return FIRE_ERR_CUDA;
 }

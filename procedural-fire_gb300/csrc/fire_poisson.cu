@@ -1176,6 +1176,17 @@ int fire_poisson_residual(FirePoisson* ps, const float* b, const float* x, const
   return FIRE_OK;
 }
 
+int fire_poisson_set_study(FirePoisson* ps, int coarse_sweeps) {
+  if (!ps || ps->ir || coarse_sweeps < 1 || coarse_sweeps > 4096) return FIRE_ERR_BAD_ARG;
+  DeviceGuard dg(ps->device);
+  if (cudaDeviceSynchronize() != cudaSuccess) return FIRE_ERR_CUDA;
+  for (MGLevel& L : ps->mg) L.study = 1;
+  ps->coarseIters = coarse_sweeps;
+  ps->tailFirst = tail_first(ps->mg.data(), (int)ps->mg.size(), false);   // single-CTA tails in this variant
+  if (ps->exec) { cudaGraphExecDestroy(ps->exec); ps->exec = nullptr; }
+  return FIRE_OK;
+}
+
 int fire_poisson_make_rhs(FirePoisson* ps, float* b, unsigned seed, int n_sources, float noise, void* stream) {
   if (!ps || !b || n_sources < 0 || n_sources > MAX_SOURCES) return FIRE_ERR_BAD_ARG;
   DeviceGuard dg(ps->device);

@@ -39,6 +39,7 @@ struct FireSim {
   std::vector<fire::MGLevel> levels;
   int coarseIters = 8;
   int tailFirst = 0;
+  int tailWaitPolls = fire::TAIL_WAIT_POLLS;   // bound of the tail's first bulk-copy wait (fire_sim_set_tail_wait_limit)
   uint2* noise = nullptr;
   uint2* curl = nullptr;
   float* dBlock = nullptr;

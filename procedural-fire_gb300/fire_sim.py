@@ -106,6 +106,7 @@ _SIGS = {
     "fire_build_campfire": (_ip, [ctypes.c_uint32, _vp, _ip]),
     "fire_make_spots": (_ip, [ctypes.c_uint32, _ip, _fp, _fp, _fp, _fp, _vp]),
     "fire_poisson_vcycles_noalloc": (_ip, [_vp, _vp, _ip, _ip, _ip, _fp, _ip, _vp]),
+    "fire_poisson_noalloc_status": (_ip, [_vp]),
     "fire_sparks_create": (_ip, [_vp, _ip, ctypes.POINTER(_vp)]),
     "fire_sparks_destroy": (_ip, [_vp]),
     "fire_sparks_reset": (_ip, [_vp]),
@@ -158,6 +159,7 @@ _SIGS = {
     "fire_poisson_residual": (_ip, [_vp, _vp, _vp, _vp, ctypes.POINTER(_dp)]),
     "fire_poisson_make_rhs": (_ip, [_vp, _vp, ctypes.c_uint, _ip, _fp, _vp]),
     "fire_poisson_sources": (_ip, [ctypes.c_uint, _ip, _vp, _vp]),
+    "fire_poisson_set_study": (_ip, [_vp, _ip]),
     "fire_adjoint_create": (_ip, [_vp, _ip, _ip, ctypes.POINTER(_vp)]),
     "fire_adjoint_destroy": (_ip, [_vp]),
     "fire_adjoint_forward": (_ip, [_vp, _fp, _vp]),
@@ -170,6 +172,7 @@ _SIGS = {
     "fire_adjoint_stage": (_ip, [_vp, _ip, _fp, _ip, _vp]),
     "fire_adjoint_timing": (_ip, [_vp, ctypes.POINTER(_fp), ctypes.POINTER(_fp)]),
     "fire_sim_set_mg_omega": (_ip, [_vp, _fp]),
+    "fire_sim_set_tail_wait_limit": (_ip, [_vp, _ip]),
     "fire_device_ok": (_ip, [_ip]),
     "fire_version": (ctypes.c_char_p, []),
 }
@@ -354,6 +357,10 @@ class FireSim:
 
     def set_bed_gain(self, gain: float):
         self._check(self._lib.fire_sim_set_bed_gain(self._h, gain), "set_bed_gain")
+
+    def set_tail_wait_limit(self, polls: int):
+        """Fault-injection hook: bound of the multigrid tail's first bulk-copy wait (0 = give up at once)."""
+        self._check(self._lib.fire_sim_set_tail_wait_limit(self._h, int(polls)), "set_tail_wait_limit")
 
     def set_mg_omega(self, omega: float):
         """Over-relaxation of the V-cycle's fine-level smoothing (1 = the reference's Gauss-Seidel)."""
@@ -988,6 +995,11 @@ class Poisson:
         self._check(self._lib.fire_poisson_residual(self._h, ctypes.c_void_p(_dev_ptr(b)), ctypes.c_void_p(_dev_ptr(x)), lo,
                                                     ctypes.byref(v)), "fire_poisson_residual")
         return v.value
+
+    def set_study(self, coarse_sweeps: int):
+        """FP32 form: switch to the V-cycle variant of the reference's multigrid convergence studies
+        (research/webgpu-bench/poisson.mjs, wgsl/mg.wgsl) with `coarse_sweeps` coarsest-level sweeps."""
+        self._check(self._lib.fire_poisson_set_study(self._h, int(coarse_sweeps)), "fire_poisson_set_study")
 
     def make_rhs(self, b, seed: int = 3, n_sources: int = 32, noise: float = 1e-3, stream=None):
         self._check(self._lib.fire_poisson_make_rhs(self._h, ctypes.c_void_p(_dev_ptr(b)), seed, n_sources, float(noise),

@@ -115,3 +115,27 @@ def test_no_silent_fallback_without_device():
     with pytest.raises(F.FireError) as ei:
         F.FireSim(res=(16, 16, 16), size=(0.2, 0.2, 0.2))
     assert ei.value.code == 4
+
+
+def test_oracle_restates_defaults_and_spots(oracle_mod):
+    """The oracle's own SIM_DEFAULTS block and seeded spots (used by bench.py's reference arm, which loads
+    no product library) equal the library's."""
+    np.testing.assert_array_equal(oracle_mod.sim_defaults(), F.param_defaults())
+    for args in [(2, 6, 1.0, 4.0, 0.02, 0.2), (11, 8, 1.0, 4.0, 0.02, 0.12), (1000, 2, 1.0, 4.0, 0.02, 0.18)]:
+        np.testing.assert_array_equal(oracle_mod.make_spots(*args), F.make_spots(*args))
+
+
+def test_reference_arm_inputs_load_no_product_library():
+    """bench.py's reference arm builds the workload from the oracle alone: after building its parameter block
+    neither the host mirror module nor libfiresim.so is loaded in the process."""
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    code = ("import sys; sys.path[:0] = ['oracle']; import bench, oracle; blk = bench.oracle_block(oracle); "
+            "maps = open('/proc/self/maps').read(); "
+            "assert 'fire_sim' not in sys.modules and 'libfiresim' not in maps, 'product library loaded'; "
+            "assert 'libfire_oracle' in maps; print(float(blk[34]), int(blk[64 + 3]))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == ["0.30000001192092896", "6"]

@@ -1,0 +1,111 @@
+"""The multigrid against the reference's own recorded convergence studies.
+
+The reference measured its multigrid twice on the same 128^3 problem (the divergence of an analytic plume,
+research/webgpu-bench/poisson.mjs:78-92; h^2 = 4^l per level, open sides and top with face ghosts, Neumann
+floor): on the CPU with poisson.mjs (30 coarsest sweeps, recorded in results/poisson-128-face.txt) and on a
+GPU with bench.js benchMG and wgsl/mg.wgsl (16 coarsest sweeps, recorded per size in
+results/result-new-mg.json).  Both use the studies' V-cycle variant (ghosts from the old cell value,
+clamp-to-edge prolongation), which fire_poisson_set_study selects on the standalone solver's FP32 form.
+
+* CPU: the oracle's restatement of the study reproduces the recorded GPU histories (the CPU history is
+  pinned digit for digit in test_oracle_kat.py).
+* GPU: the CUDA V-cycle in the studies' variant reproduces both records, and in the simulation's own variant
+  (src/sim.js mgSmooth / mgProlong) matches the oracle cycle by cycle on the same problem.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLD = Path(__file__).parent / "golden"
+CPU_REC = json.loads((GOLD / "poisson_128_face.json").read_text())
+GPU_REC = json.loads((GOLD / "mg_gpu_ratios.json").read_text())["ratios"]
+
+
+def _cpu_mg_line():
+    line = next(l for l in CPU_REC["lines"] if l["mode"] == "mg" and l["pre"] == 2)
+    return [float(v) for v in line["values"]]
+
+
+@pytest.mark.parametrize("N", [64, 128, 160])
+def test_oracle_study_reproduces_gpu_record(oracle_mod, N):
+    """poisson.mjs restated (JS double arithmetic, Float32Array storage) with benchMG's 16 coarsest sweeps
+    against the GPU record: the first three cycles to 1.5 %, the fourth to 7 %; later cycles sit on each
+    machine's FP32 floor."""
+    rec = GPU_REC[str(N)]["V(2,2)-rb"]
+    _, hist = oracle_mod.poisson_study(N, True, 2, coarse=16, cycles=6)
+    for k in range(3):
+        assert hist[k] == pytest.approx(rec[k], rel=0.015), (k, hist[k], rec[k])
+    assert hist[3] == pytest.approx(rec[3], rel=0.07)
+
+
+# ------------------------------------------------------------------ GPU
+def _torch():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _history(N, b_np, cycles, study_sweeps=None):
+    """Relative residual after each of `cycles` V-cycles of the standalone FP32 form from x = 0 (h = 1)."""
+    torch = _torch()
+    import fire_sim as F
+    ps = F.Poisson((N, N, N), 1.0, "fp32")
+    if study_sweeps:
+        ps.set_study(study_sweeps)
+    b = torch.from_numpy(np.ascontiguousarray(b_np, np.float32).ravel()).cuda()
+    x = torch.zeros_like(b)
+    hist = []
+    for _ in range(cycles):
+        ps.solve(b, x, tol=0.0, max_iters=1)
+        hist.append(ps.result()["rel_residual"])
+    ps.close()
+    return hist
+
+
+@pytest.mark.gpu
+def test_gpu_study_vcycle_reproduces_cpu_record(oracle_mod):
+    """The CUDA V-cycle in the studies' variant with poisson.mjs's 30 coarsest sweeps against the recorded
+    CPU history (results/poisson-128-face.txt, two significant digits) and the oracle's restatement."""
+    N = 128
+    hist = _history(N, oracle_mod.poisson_rhs(N), 6, study_sweeps=30)
+    rec = _cpu_mg_line()
+    _, orc = oracle_mod.poisson_study(N, True, 2, coarse=30, cycles=6)
+    for k in range(4):
+        assert hist[k] == pytest.approx(rec[k], rel=0.1), (k, hist, rec)
+        assert hist[k] == pytest.approx(orc[k], rel=0.03), (k, hist, orc)
+    assert max(hist[4:]) < 1.5e-4   # the FP32 floor (the record's double-arithmetic run reaches 2e-5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N", [64, 128, 160])
+def test_gpu_study_vcycle_reproduces_gpu_record(oracle_mod, N):
+    """The same with benchMG's 16 coarsest sweeps against the reference GPU's recorded ratios per size
+    (results/result-new-mg.json V(2,2)-rb)."""
+    hist = _history(N, oracle_mod.poisson_rhs(N), 6, study_sweeps=16)
+    rec = GPU_REC[str(N)]["V(2,2)-rb"]
+    for k in range(4):
+        assert hist[k] == pytest.approx(rec[k], rel=0.1), (k, hist, rec)
+    assert max(hist[4:]) < 1.5e-4
+
+
+@pytest.mark.gpu
+def test_gpu_sim_vcycle_on_study_problem(oracle_mod):
+    """The simulation's own V-cycle (mgSmooth's implicit ghost diagonal, mirror prolongation, coarseIters
+    sweeps) on the study's 128^3 problem, cycle by cycle against the oracle's FP32 restatement of it.  It
+    converges about three times faster per cycle than the studies' variant."""
+    N = 128
+    b = oracle_mod.poisson_rhs(N)
+    hist = _history(N, b, 5)
+    orc = oracle_mod.OracleSim((N, N, N), 1.0)
+    orc.put_level(0, "b", b)
+    rr0, _ = orc.residual()
+    want = []
+    for _ in range(5):
+        orc.vcycle()
+        want.append(np.sqrt(orc.residual()[0] / rr0))
+    for k in range(4):
+        assert hist[k] == pytest.approx(want[k], rel=0.02), (k, hist, want)
+    assert hist[0] < 0.5 * _cpu_mg_line()[0]
