@@ -296,13 +296,28 @@ def cpu_baseline(sim, steps: int = 2):
 POISSON = dict(name="poisson-256x512x256", res=(256, 512, 256), h=0.005, seed=3, sources=32, noise=1e-3, tol=1e-6)
 
 
-def run_poisson(dev: int, reps: int = 3):
+def run_poisson(dev: int, reps: int = 3, fixed_iters: int = 0):
     """Times each form of the standalone solver on the POISSON workload (device time, CUDA events).  The
     FP32 form (the step's V-cycle on an FP32 x) cannot get below the FP32 representation floor of the
-    solution (~2e-5 here); it is timed to 3e-5 and its floor reported."""
+    solution (~2e-5 here); it is timed to 3e-5 and its floor reported.  fixed_iters > 0 (profiling aid)
+    instead runs exactly that many iterations of each form once: the solve graph is then unrolled, with no
+    conditional node, so every kernel can be profiled."""
     import torch
     import fire_sim as F
     P = POISSON
+    if fixed_iters > 0:
+        n = P["res"][0] * P["res"][1] * P["res"][2]
+        b = torch.empty(n, dtype=torch.float32, device=f"cuda:{dev}")
+        x, lo = torch.zeros_like(b), torch.zeros_like(b)
+        out = {}
+        for prec in ("fp32", "ir32", "fp16", "bf16"):
+            ps = F.Poisson(P["res"], P["h"], prec, device=dev)
+            ps.make_rhs(b, seed=P["seed"], n_sources=P["sources"], noise=P["noise"])
+            x.zero_(); lo.zero_()
+            ps.solve(b, x, tol=0.0, max_iters=fixed_iters, x_lo=lo)
+            out[prec] = ps.result()
+            ps.close()
+        return {"workload": P["name"], "fixed_iterations": fixed_iters, "forms": out}
     n = P["res"][0] * P["res"][1] * P["res"][2]
     b = torch.empty(n, dtype=torch.float32, device=f"cuda:{dev}")
     x = torch.zeros_like(b)
@@ -785,6 +800,8 @@ def main(argv=None):
                     help="run just one of the side workloads and print its block (profiling aid)")
     ap.add_argument("--adjoint-steps", type=int, default=0, help="override the adjoint rollout length")
     ap.add_argument("--adjoint-iters", type=int, default=-1, help="override the number of fit iterations")
+    ap.add_argument("--poisson-iters", type=int, default=0,
+                    help="profiling aid for --only poisson: exactly N iterations per form, unrolled graphs")
     ap.add_argument("--mg-fixed", type=int, default=0,
                     help="profiling aid: N fixed V-cycles per step instead of the residual-driven solve")
     args = ap.parse_args(argv)
@@ -792,7 +809,7 @@ def main(argv=None):
     if args.only:
         import torch
         torch.cuda.init()
-        fn = {"poisson": lambda: run_poisson(0), "ensemble": lambda: run_ensemble(0),
+        fn = {"poisson": lambda: run_poisson(0, fixed_iters=args.poisson_iters), "ensemble": lambda: run_ensemble(0),
               "adjoint": lambda: run_adjoint(0, args.adjoint_steps, args.adjoint_iters, args.mg_fixed),
               "consumers": lambda: run_consumers(0)}[args.only]
         print(json.dumps({args.only: fn()}), flush=True)

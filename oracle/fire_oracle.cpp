@@ -313,6 +313,10 @@ template <class R> struct Sim {
   float omega = 1.0f;
   int store_half = 0;
   int filter_bits = 0;
+  // Spot fluxes in double, replacing the FP32 values of the extension block when set (lets finite differences
+  // of the FP64 oracle take steps far below the block's FP32 resolution).
+  int flux64_set = 0;
+  double flux64[16] = {};
 };
 // rgba16float store: rounds every component of a float4 field to the nearest IEEE half.
 template <class R> void round_field_half(std::vector<R>& f) {
@@ -513,7 +517,8 @@ template <class R> void k_forces(Sim<R>& s) {
             V3<R> d = p - V3<R>(sp[0], sp[1], sp[2]);
             R sg = sp[3];
             R d2 = dot3(d, d);
-            if (d2 < R(16) * sg * sg) acc += ((R)sp[4] / spotRef) * std::exp(-d2 / (R(2) * sg * sg));
+            const R flux = s.flux64_set ? (R)s.flux64[q] : (R)sp[4];
+            if (d2 < R(16) * sg * sg) acc += (flux / spotRef) * std::exp(-d2 / (R(2) * sg * sg));
           }
           src = fmx(src, clampf(acc, R(0), R(1)) * I);
         }
@@ -1179,6 +1184,12 @@ void orc_set_modes(void* h, double omega, int store_half, int filter_bits) {
   o->f.omega = o->d.omega = (float)omega;
   o->f.store_half = o->d.store_half = store_half;
   o->f.filter_bits = o->d.filter_bits = filter_bits;
+}
+// Spot fluxes (g/s) in double for the next steps, overriding the extension block's FP32 values; n = 0 clears.
+void orc_set_flux64(void* h, const double* flux, int n) {
+  OracleSim* o = (OracleSim*)h;
+  o->f.flux64_set = o->d.flux64_set = n > 0;
+  for (int i = 0; i < 16; ++i) o->f.flux64[i] = o->d.flux64[i] = i < n ? flux[i] : 0.0;
 }
 // Sweeps on the coarsest level (the constructor's coarseIters rule, src/sim.js:88-92, unless set here).
 void orc_set_coarse_iters(void* h, int iters) { OracleSim* o = (OracleSim*)h; o->f.coarseIters = o->d.coarseIters = iters; }

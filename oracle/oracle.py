@@ -66,7 +66,7 @@ def lib():
             "orc_volume_lights": (None, [vp, vp, ip, ip, ip, vp, vp, vp]),
             "orc_volume_render": (None, [vp, vp, vp, ip, ip, ip, vp, ip, vp, vp, vp, vp]),
             "orc_set_modes": (None, [vp, dp, ip, ip]), "orc_set_coarse_iters": (None, [vp, ip]),
-            "orc_sim_defaults": (None, [vp]),
+            "orc_sim_defaults": (None, [vp]), "orc_set_flux64": (None, [vp, vp, ip]),
             "orc_make_spots": (None, [ctypes.c_uint32, ip, fp, fp, fp, fp, vp]),
         }
         for name, (res, args) in sigs.items():
@@ -303,6 +303,14 @@ class OracleSim:
         field to IEEE half after the stage that writes it (the reference's rgba16float textures); filter_bits:
         fractional bits of the trilinear texture weights (0 = exact)."""
         lib().orc_set_modes(self.h, float(omega), int(bool(store_half)), int(filter_bits))
+
+    def set_flux64(self, flux=None):
+        """Spot fluxes (g/s) in double, overriding the extension block's FP32 values (None clears)."""
+        f = np.zeros(16, np.float64)
+        n = 0 if flux is None else len(flux)
+        if n:
+            f[:n] = np.asarray(flux, np.float64)
+        lib().orc_set_flux64(self.h, _ptr(f), n)
 
     def set_coarse_iters(self, iters: int):
         lib().orc_set_coarse_iters(self.h, int(iters))

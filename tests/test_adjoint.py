@@ -307,9 +307,12 @@ def test_tape_forward_matches_step_and_backward_restores():
     adj.close(); a.close(); b.close()
 
 
-def _oracle_rollout(O, sim, blocks, start, flux=None, spots=None):
-    """FP64 oracle rollout from `start` over the given per-step blocks; returns the final vel, S, S2."""
+def _oracle_rollout(O, sim, blocks, start, flux=None, spots=None, flux64=None):
+    """FP64 oracle rollout from `start` over the given per-step blocks; returns the final vel, S, S2.
+    flux: spot fluxes written into the (FP32) blocks; flux64: spot fluxes held in double instead."""
     orc = O.OracleSim(RES, sim.dx, dbl=True)
+    if flux64 is not None:
+        orc.set_flux64(flux64)
     orc.set_tables(sim.download("noise").astype(np.float32), sim.download("curl").astype(np.float32))
     orc.set_logs(np.zeros(0, np.float32))
     for k in ("vel", "S", "S2", "geo"):
@@ -405,6 +408,130 @@ def test_rollout_gradients_vs_fp64_differences(oracle_mod):
         assert abs(fdq - g_flux[q]) <= 1e-2 * max(abs(fdq), 1e-2 * np.abs(g_flux).max()), (q, fdq, g_flux[q])
     adj.close()
     sim.close()
+
+
+@pytest.mark.gpu
+def test_rollout_gradients_30_steps_vs_fp64_differences(oracle_mod):
+    """The same checks through 30 steps in three checkpointed segments of 10.  At this grid the FP32 forward
+    and the FP64 oracle stay within 1e-5 of each other over 30 steps (test_horizon_of_fp64_checks), so a
+    central difference of the FP64 oracle still describes the map the GPU adjoint differentiates, while the
+    sensitivity to the initial state has grown about sevenfold from 8 steps."""
+    import fire_sim as F
+    O = oracle_mod
+    n_steps, k = 30, 10
+    spots = F.make_spots(9, 4, 1.0, 4.0, 0.02, 0.08)
+    sim = _burning_sim(F, spots)
+    start = {n: sim.download(n).astype(np.float64) for n in ("vel", "S", "S2", "geo")}
+    start["p"] = sim.level(0, "p").astype(np.float64)
+    blocks = _blocks(sim, n_steps)
+    adj = F.Adjoint(sim, n_steps, k)
+    adj.forward(DT)
+    rng = np.random.default_rng(22)
+    shape = RES[::-1] + (4,)
+    lam = {n: rng.standard_normal(shape) for n in ("vel", "S", "S2")}
+    lam["vel"][..., 3] = 0.0
+    adj.seed(*[lam[n].astype(np.float32) for n in ("vel", "S", "S2")])
+    adj.backward()
+    sim.sync()
+    g = {n: adj.get(n).astype(np.float64) for n in ("vel", "S")}
+    g_flux = adj.grad_spots(len(spots))
+    J = lambda y: sum(float(np.sum(lam[n] * y[n])) for n in ("vel", "S", "S2"))
+
+    def fd_state(name, d, h):
+        sp, sm = dict(start), dict(start)
+        sp[name], sm[name] = start[name] + h * d, start[name] - h * d
+        return (J(_oracle_rollout(O, sim, blocks, sp)) - J(_oracle_rollout(O, sim, blocks, sm))) / (2 * h)
+
+    inner = np.zeros(shape[:3], bool)
+    inner[2:-2, 2:-2, 2:-2] = True
+    dv = _smooth(shape, rng, w_zero=True)
+    floor_clamped = start["vel"][:, 0, :, 1] == 0.0
+    dv[:, 0, :, 1][floor_clamped] = 0.0
+    dS = (1.0 + 0.2 * _smooth(shape, rng)) * start["S"]
+    for name, d, fld, tol in (("vel (interior)", dv * inner[..., None], "vel", 1e-3), ("vel", dv, "vel", 5e-2),
+                              ("S", dS, "S", 2e-2)):
+        ad = float(np.sum(g[fld] * d))
+        fd = fd_state(fld, d, H_ROLL)
+        print(f"30 steps, initial {name}: differences {fd:.9e} (h = {H_ROLL:g}); adjoint {ad:.9e}; rel {abs(fd - ad) / abs(fd):.2e}")
+        assert abs(fd - ad) <= tol * abs(fd), (name, fd, ad)
+    # spot fluxes: over 30 steps a difference step of 1e-3 g/s (the FP32 block's resolution allows no less)
+    # straddles limiter jumps, so the oracle holds the fluxes in double and the step is 1e-7 g/s
+    base = np.array([s[4] for s in spots], np.float64)
+    hq = 1e-7
+    for q in range(len(spots)):
+        fp, fm = base.copy(), base.copy()
+        fp[q] += hq
+        fm[q] -= hq
+        fdq = (J(_oracle_rollout(O, sim, blocks, start, flux64=fp)) - J(_oracle_rollout(O, sim, blocks, start, flux64=fm))) / (2 * hq)
+        print(f"30 steps, spot {q}: differences {fdq:.9e} (h = {hq:g} g/s); adjoint {g_flux[q]:.9e}")
+        assert abs(fdq - g_flux[q]) <= 1e-2 * max(abs(fdq), 1e-2 * np.abs(g_flux).max()), (q, fdq, g_flux[q])
+    adj.close()
+    sim.close()
+
+
+def test_horizon_of_fp64_checks(oracle_mod):
+    """Why the rollout gradient is checked against FP64 differences at 8 and 30 steps and not at the 120 of
+    the source-fit workload, on the oracle alone (24x48x24, the rollout tests' burning state): the FP32 and
+    FP64 trajectories from one state agree to 1e-4 through 30 steps but separate by more than 1e-2 by 120
+    steps, because the flow amplifies perturbations (the FP64 response to a 1e-9 change of the initial
+    velocity grows by more than 1e4 between 8 and 120 steps).  FP32 rounding alone moves the 120-step state
+    as far as any finite difference would probe: the discrete gradient there is that of a chaotic map."""
+    O = oracle_mod
+    O.set_threads(O.lib().orc_num_threads())
+    dx = np.float32(np.float64(np.float32(SIZE[0])) / RES[0])
+    noise = O.noise_table(128, 1)
+    curl = O.curl_table(noise)
+    spots = O.make_spots(9, 4, 1.0, 4.0, 0.02, 0.08)
+
+    def block(t, f):
+        b = np.zeros(208, np.float32)
+        b[:64] = O.sim_defaults()
+        b[0], b[1], b[2] = RES
+        b[3], b[4], b[5], b[6] = dx, np.float32(DT), np.float32(t), f
+        b[8] = b[10] = np.float32(-np.float32(SIZE[0]) / np.float32(2))
+        b[34], b[35] = 0.3, 0.2          # vortEps, turbAmp
+        e = b[64:]
+        e[0], e[1], e[2], e[3], e[4] = 0.02, 0.06, 0.0, len(spots), 4.0
+        for i, sp in enumerate(spots):
+            e[16 + 8 * i: 16 + 8 * i + 5] = sp
+        return b
+
+    def make(dbl):
+        o = O.OracleSim(RES, float(dx), dbl=dbl)
+        o.set_tables(noise, curl)
+        o.set_logs(np.zeros(0, np.float32))
+        return o
+
+    o, t = make(False), 0.0
+    for s in range(30):
+        b = block(t, s)
+        o.set_params(b[:64]); o.set_ext(b[64:]); o.step_raw(s == 0, VCYC)
+        t += float(np.float32(DT))
+    start = {k: o.get(k) for k in ("vel", "S", "S2", "geo")}
+    p0 = o.get_level(0, "p")
+
+    def run(dbl, n, dvel=None):
+        r = make(dbl)
+        for k, v in start.items():
+            r.put(k, v.astype(np.float64) if dbl else v)
+        if dvel is not None:
+            r.put("vel", start["vel"].astype(np.float64) + dvel)
+        r.put_level(0, "p", p0.astype(np.float64) if dbl else p0)
+        tt = t
+        for s in range(n):
+            b = block(tt, 30 + s)
+            r.set_params(b[:64]); r.set_ext(b[64:]); r.step_raw(False, VCYC)
+            tt += float(np.float32(DT))
+        return np.concatenate([r.get(k, np.float64).ravel() for k in ("vel", "S", "S2")])
+
+    sep = {n: np.linalg.norm(run(False, n) - run(True, n)) / np.linalg.norm(run(True, n)) for n in (30, 120)}
+    d = np.random.default_rng(3).standard_normal(start["vel"].shape)
+    d[..., 3] = 0.0
+    amp = {n: np.linalg.norm(run(True, n, 1e-9 * d) - run(True, n)) / (1e-9 * np.linalg.norm(d)) for n in (8, 120)}
+    print(f"\nFP32 vs FP64 separation: 30 steps {sep[30]:.2e}, 120 steps {sep[120]:.2e}; "
+          f"FP64 sensitivity: 8 steps {amp[8]:.3e}, 120 steps {amp[120]:.3e}")
+    assert sep[30] < 1e-4 and sep[120] > 1e-2, sep
+    assert amp[120] > 1e4 * amp[8], amp
 
 
 @pytest.mark.gpu

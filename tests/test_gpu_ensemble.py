@@ -67,6 +67,39 @@ def test_ensemble_equals_members_alone():
     ens.close()
 
 
+@pytest.mark.parametrize("member", [0, 3])
+def test_ensemble_member_step_vs_oracle(oracle_mod, member):
+    """A member of a batched ensemble against the oracle directly: after 10 batched steps (a developed fire),
+    the member's state goes into the FP32 oracle with the member's own parameter block for the next step,
+    and one more batched step must match one oracle step at the one-step tolerance of tests/test_gpu_step.py
+    (1e-3 relative + 1e-4 of each channel's scale, at most 0.5 % of cells beyond)."""
+    import fire_sim as F
+    ens = F.Ensemble(MEMBERS, vcycles=4)
+    for sim, m in zip(ens.members, MEMBERS):
+        _configure(sim, m)
+    ens.step(DT, 10)
+    ens.sync()
+    sim = ens.members[member]
+    m = MEMBERS[member]
+    orc = oracle_mod.OracleSim(m["res"], sim.dx)
+    orc.set_tables(sim.download("noise").astype(np.float32), sim.download("curl").astype(np.float32))
+    orc.set_logs(np.zeros(0, np.float32))
+    for name in ("vel", "S", "S2", "geo"):
+        orc.put(name, sim.download(name))
+    orc.put_level(0, "p", sim.level(0, "p"))
+    FC.sync_block(sim, orc, DT)
+    ens.step(DT, 1)
+    ens.sync()
+    orc.step_raw(False, 4)
+    assert float(sim.download("S")[..., 0].max()) > 0.05
+    for name in ("vel", "S", "S2"):
+        g, o = sim.download(name), orc.get(name)
+        for c in range(4):
+            FC.compare(g[..., c], o[..., c], 1e-3, 1e-4, 5e-3, what=f"member {member} {name}[{c}]")
+    FC.compare(sim.level(0, "p"), orc.get_level(0, "p"), 1e-3, 1e-4, 5e-3, what=f"member {member} p")
+    ens.close()
+
+
 def test_ensemble_rejects_bad_configs():
     import fire_sim as F
     with pytest.raises(F.FireError):
