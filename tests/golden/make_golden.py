@@ -4,7 +4,7 @@ Reads (as text) the reference project's multigrid convergence records:
   research/webgpu-bench/results/poisson-128-face.txt   CPU poisson.mjs study, 128^3, face ghosts
   research/webgpu-bench/results/result-new-mg.json     GPU V-cycle residual ratios (bench.js benchMG)
 and writes poisson_128_face.json and mg_gpu_ratios.json.  Run from the repo root:
-  python tests/golden/make_golden.py [path-to-reference]
+  python tests/golden/make_golden.py <path-to-reference>
 The fixtures are committed; tests never read the reference tree.
 """
 import json
@@ -43,4 +43,6 @@ def main(ref: Path):
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path-to-reference-checkout>")
+    main(Path(sys.argv[1]))
