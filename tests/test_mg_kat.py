@@ -71,6 +71,7 @@ def test_gpu_study_vcycle_reproduces_cpu_record(oracle_mod):
     CPU history (results/poisson-128-face.txt, two significant digits) and the oracle's restatement."""
     N = 128
     hist = _history(N, oracle_mod.poisson_rhs(N), 6, study_sweeps=30)
+    print(f"\nstudy variant, 30 coarsest sweeps, 128^3: " + ", ".join(f"{v:.3g}" for v in hist))
     rec = _cpu_mg_line()
     _, orc = oracle_mod.poisson_study(N, True, 2, coarse=30, cycles=6)
     for k in range(4):
@@ -85,6 +86,7 @@ def test_gpu_study_vcycle_reproduces_gpu_record(oracle_mod, N):
     """The same with benchMG's 16 coarsest sweeps against the reference GPU's recorded ratios per size
     (results/result-new-mg.json V(2,2)-rb)."""
     hist = _history(N, oracle_mod.poisson_rhs(N), 6, study_sweeps=16)
+    print(f"\nstudy variant, 16 coarsest sweeps, {N}^3: " + ", ".join(f"{v:.3g}" for v in hist))
     rec = GPU_REC[str(N)]["V(2,2)-rb"]
     for k in range(4):
         assert hist[k] == pytest.approx(rec[k], rel=0.1), (k, hist, rec)
