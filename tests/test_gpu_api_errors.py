@@ -53,3 +53,28 @@ def test_ensemble_tile_api_misuse():
     ens.sync()
     assert all(np.isfinite(m.download("vel")).all() for m in ens.members)
     ens.close()
+
+
+def test_study_variant_and_wait_limit_arguments():
+    """fire_poisson_set_study applies to the FP32 form only and needs at least one coarsest sweep;
+    fire_sim_set_tail_wait_limit refuses a negative bound."""
+    import fire_sim as F
+    ir = F.Poisson((16, 32, 16), 1.0, "ir32")
+    with pytest.raises(F.FireError) as e:
+        ir.set_study(30)
+    assert e.value.code == 1
+    ir.close()
+    ps = F.Poisson((16, 32, 16), 1.0, "fp32")
+    for bad in (0, -3):
+        with pytest.raises(F.FireError):
+            ps.set_study(bad)
+    ps.set_study(16)
+    ps.close()
+    sim = F.FireSim(res=(16, 32, 16), size=(0.2, 0.4, 0.2), vcycles=2)
+    with pytest.raises(F.FireError) as e:
+        sim.set_tail_wait_limit(-1)
+    assert e.value.code == 1
+    sim.set_tail_wait_limit(1 << 22)
+    sim.step(0.01, 1)
+    sim.sync()
+    sim.close()
