@@ -197,6 +197,16 @@ int fire_sim_field(FireSim* sim, int which, FireFieldDesc* out);
 /* Synchronous copies between a field and host memory (`bytes` must equal FireFieldDesc.bytes).
  * Readback as FIRE.stats does it (src/main.js:268-294); upload sets state for tests and restarts.  */
 int fire_sim_download(FireSim* sim, int which, void* host, size_t bytes);
+/* Checkpoint and resume (no counterpart in the reference, which resumes a capture by re-simulating from
+ * the start, tools/render_video.mjs:79-82).  fire_sim_save writes the state a later step depends on into a
+ * host buffer: time and frame, the parameter block and its extension, the logs, the event envelopes, the
+ * residual-driven loop's cycle prediction, vel, S, S2 and the level-0 pressure (the warm start).  With
+ * buf = NULL it only reports the size in *bytes.  fire_sim_load restores it into a simulation created with
+ * the same grid and size (other configuration, e.g. the solver settings, is the caller's); the emitter
+ * geometry is rebuilt from the restored logs at the next step.  Steps after a load give the same bits as the
+ * saved simulation's steps would have.  Both synchronise the device.                                   */
+int fire_sim_save(FireSim* sim, void* buf, size_t capacity, size_t* bytes);
+int fire_sim_load(FireSim* sim, const void* buf, size_t bytes);
 int fire_sim_upload(FireSim* sim, int which, const void* host, size_t bytes);
 int fire_sim_info(FireSim* sim, FireInfo* out);
 const char* fire_sim_last_error(FireSim* sim);

@@ -662,6 +662,116 @@ int fire_sim_reset(FireSim* sim) {
   return FIRE_OK;
 }
 
+// ---- checkpoint / resume ----
+namespace {
+// Header of a saved state; the payload follows: vel, S, S2 (float4 per cell each) and level-0 p (float).
+struct SaveHeader {
+  char magic[8];
+  uint32_t version, header_bytes;
+  int32_t res[3];
+  float size[3];
+  double time;
+  int64_t frame, stepsRun;
+  float params[P_STRIDE];
+  float ext[E_COUNT];
+  float logs[MAX_LOGS * 8];
+  int32_t nLogs;
+  double burstUntil;
+  float burstAmt;
+  int32_t burstActive;
+  double gustLeft, gustDur;
+  float gustStrength;
+  int32_t gustActive;
+  float windBase[2];
+  int32_t counters[4];   // the residual loop's counters (cumulative cycles, first cycle the next step tests)
+  int32_t lastCycles;
+  double lastRel;
+};
+const char kSaveMagic[8] = {'F', 'I', 'R', 'E', 'S', 'I', 'M', '1'};
+size_t save_bytes(const FireSim* s) {
+  const size_t cells = (size_t)s->res[0] * s->res[1] * s->res[2];
+  return sizeof(SaveHeader) + cells * (3 * sizeof(float4) + sizeof(float));
+}
+}  // namespace
+
+int fire_sim_save(FireSim* sim, void* buf, size_t capacity, size_t* bytes_out) {
+  if (!sim || !bytes_out) return FIRE_ERR_BAD_ARG;
+  const size_t need = save_bytes(sim);
+  *bytes_out = need;
+  if (!buf) return FIRE_OK;
+  if (capacity < need) return set_err(sim, FIRE_ERR_BAD_ARG, "save: need %zu bytes, got %zu", need, capacity);
+  CK(cudaSetDevice(sim->device));
+  CK(cudaDeviceSynchronize());
+  SaveHeader h;
+  std::memset(&h, 0, sizeof h);
+  std::memcpy(h.magic, kSaveMagic, sizeof h.magic);
+  h.version = 1;
+  h.header_bytes = (uint32_t)sizeof h;
+  for (int i = 0; i < 3; ++i) { h.res[i] = sim->res[i]; h.size[i] = sim->size[i]; }
+  h.time = sim->time;
+  h.frame = sim->frame;
+  h.stepsRun = sim->stepsRun;
+  std::memcpy(h.params, sim->params, sizeof h.params);
+  std::memcpy(h.ext, sim->ext, sizeof h.ext);
+  std::memcpy(h.logs, sim->logs, sizeof h.logs);
+  h.nLogs = sim->nLogs;
+  h.burstUntil = sim->burstUntil; h.burstAmt = sim->burstAmt; h.burstActive = sim->burstActive;
+  h.gustLeft = sim->gustLeft; h.gustDur = sim->gustDur; h.gustStrength = sim->gustStrength; h.gustActive = sim->gustActive;
+  h.windBase[0] = sim->windBase[0]; h.windBase[1] = sim->windBase[1];
+  CK(cudaMemcpy(h.counters, sim->dCounter, sizeof h.counters, cudaMemcpyDeviceToHost));
+  h.counters[0] = 0;
+  h.counters[2] = 0;   // per-step cycle count and wait-timeout flag are not state
+  h.lastCycles = sim->lastCycles;
+  h.lastRel = sim->lastRel;
+  char* o = static_cast<char*>(buf);
+  std::memcpy(o, &h, sizeof h);
+  o += sizeof h;
+  const size_t cells = (size_t)sim->res[0] * sim->res[1] * sim->res[2];
+  for (const float4* f : {sim->f.vel, sim->f.S, sim->f.S2}) {
+    CK(cudaMemcpy(o, f, cells * sizeof(float4), cudaMemcpyDeviceToHost));
+    o += cells * sizeof(float4);
+  }
+  CK(cudaMemcpy(o, sim->levels[0].p, cells * sizeof(float), cudaMemcpyDeviceToHost));
+  return FIRE_OK;
+}
+
+int fire_sim_load(FireSim* sim, const void* buf, size_t bytes) {
+  if (!sim || !buf) return FIRE_ERR_BAD_ARG;
+  if (bytes != save_bytes(sim)) return set_err(sim, FIRE_ERR_BAD_ARG, "load: %zu bytes, this simulation's state is %zu", bytes, save_bytes(sim));
+  SaveHeader h;
+  std::memcpy(&h, buf, sizeof h);
+  if (std::memcmp(h.magic, kSaveMagic, sizeof h.magic) != 0 || h.version != 1 || h.header_bytes != sizeof h)
+    return set_err(sim, FIRE_ERR_BAD_ARG, "load: not a saved simulation state of this version");
+  for (int i = 0; i < 3; ++i)
+    if (h.res[i] != sim->res[i] || h.size[i] != sim->size[i]) return set_err(sim, FIRE_ERR_BAD_ARG, "load: saved for another grid");
+  if (h.nLogs < 0 || h.nLogs > MAX_LOGS) return set_err(sim, FIRE_ERR_BAD_ARG, "load: bad log count");
+  CK(cudaSetDevice(sim->device));
+  CK(cudaDeviceSynchronize());
+  const char* in = static_cast<const char*>(buf) + sizeof h;
+  const size_t cells = (size_t)sim->res[0] * sim->res[1] * sim->res[2];
+  for (float4* f : {sim->f.vel, sim->f.S, sim->f.S2}) {
+    CK(cudaMemcpy(f, in, cells * sizeof(float4), cudaMemcpyHostToDevice));
+    in += cells * sizeof(float4);
+  }
+  CK(cudaMemcpy(sim->levels[0].p, in, cells * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(sim->dCounter, h.counters, sizeof h.counters, cudaMemcpyHostToDevice));
+  sim->time = h.time;
+  sim->frame = h.frame;
+  sim->stepsRun = h.stepsRun;
+  std::memcpy(sim->params, h.params, sizeof h.params);
+  std::memcpy(sim->ext, h.ext, sizeof h.ext);
+  std::memcpy(sim->logs, h.logs, sizeof h.logs);
+  sim->nLogs = h.nLogs;
+  sim->burstUntil = h.burstUntil; sim->burstAmt = h.burstAmt; sim->burstActive = h.burstActive != 0;
+  sim->gustLeft = h.gustLeft; sim->gustDur = h.gustDur; sim->gustStrength = h.gustStrength; sim->gustActive = h.gustActive != 0;
+  sim->windBase[0] = h.windBase[0]; sim->windBase[1] = h.windBase[1];
+  sim->lastCycles = h.lastCycles;
+  sim->lastRel = h.lastRel;
+  sim->geoReady = false;    // the emitter geometry is rebuilt from the restored logs at the next step
+  sim->logsDirty = true;
+  return FIRE_OK;
+}
+
 int fire_sim_upload_logs(FireSim* sim, const float* logs, int n_logs) {
   if (!sim || n_logs < 0 || n_logs > MAX_LOGS || (n_logs > 0 && !logs)) return FIRE_ERR_BAD_ARG;
   std::memset(sim->logs, 0, sizeof sim->logs);

@@ -173,6 +173,8 @@ _SIGS = {
     "fire_adjoint_timing": (_ip, [_vp, ctypes.POINTER(_fp), ctypes.POINTER(_fp)]),
     "fire_sim_set_mg_omega": (_ip, [_vp, _fp]),
     "fire_sim_set_tail_wait_limit": (_ip, [_vp, _ip]),
+    "fire_sim_save": (_ip, [_vp, _vp, _sz, ctypes.POINTER(_sz)]),
+    "fire_sim_load": (_ip, [_vp, _vp, _sz]),
     "fire_device_ok": (_ip, [_ip]),
     "fire_version": (ctypes.c_char_p, []),
 }
@@ -357,6 +359,19 @@ class FireSim:
 
     def set_bed_gain(self, gain: float):
         self._check(self._lib.fire_sim_set_bed_gain(self._h, gain), "set_bed_gain")
+
+    def save(self) -> bytes:
+        """The simulation's state as a checkpoint blob (fire_sim_save)."""
+        n = ctypes.c_size_t()
+        self._check(self._lib.fire_sim_save(self._h, None, 0, ctypes.byref(n)), "save")
+        buf = ctypes.create_string_buffer(n.value)
+        self._check(self._lib.fire_sim_save(self._h, buf, n.value, ctypes.byref(n)), "save")
+        return buf.raw
+
+    def load(self, blob: bytes):
+        """Restores a checkpoint made by save() on a simulation of the same grid (fire_sim_load)."""
+        buf = ctypes.create_string_buffer(bytes(blob), len(blob))
+        self._check(self._lib.fire_sim_load(self._h, buf, len(blob)), "load")
 
     def set_tail_wait_limit(self, polls: int):
         """Fault-injection hook: bound of the multigrid tail's first bulk-copy wait (0 = give up at once)."""
