@@ -78,3 +78,17 @@ def test_study_variant_and_wait_limit_arguments():
     sim.step(0.01, 1)
     sim.sync()
     sim.close()
+
+
+def test_allocation_failure_is_reported_and_harmless():
+    """A grid whose fields exceed device memory (1000 x 1000 x 2000 cells: ~350 GB of fields, within the
+    32-bit cell-offset limit) fails at allocation with FIRE_ERR_OOM, and the device stays usable."""
+    import fire_sim as F
+    with pytest.raises(F.FireError) as e:
+        F.FireSim(res=(1000, 1000, 2000), size=(1.0, 1.0, 2.0), vcycles=1)
+    assert e.value.code == 5
+    sim = F.FireSim(res=(16, 32, 16), size=(0.2, 0.4, 0.2), vcycles=2)
+    sim.step(0.01, 2)
+    sim.sync()
+    assert np.isfinite(sim.download("vel")).all()
+    sim.close()
