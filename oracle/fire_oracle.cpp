@@ -2,7 +2,7 @@
 //
 // This file restates, in plain C++, the WGSL compute kernels of the reference solver so that the CUDA
 // implementation can be checked against it.  Only the test suite, the smoke check and the CPU-baseline
-// leg of bench.py load it; the product library never links or calls it.
+// and reference legs of bench.py load it; the product library never links or calls it.
 //
 // Every kernel below cites the reference file:line it follows (paths relative to the reference project):
 //   src/sim.js          FireSim: advection, curl, forces, divergence, multigrid, projection, geometry
@@ -19,6 +19,15 @@
 //   * clamp(x, lo, hi) = min(max(x, lo), hi) with NaN-ignoring min/max (so clamp(NaN, 0, 1) = 0);
 //   * mix(a, b, t) = a * (1 - t) + b * t;  smoothstep per the WGSL definition;
 //   * normalize(v) = v / sqrt(dot(v, v)); tables are rounded to IEEE half (rgba16float) on store.
+// Modes (per simulation): the multigrid's over-relaxation factor; the reference's rgba16float storage of
+// every float4 field and the texture unit's ~8-bit filter weights (to state how far the FP32 path sits from
+// the reference's own numerics); spot fluxes held in double (finite differences below FP32 resolution).
+//
+// Pinning.  The multigrid is pinned to the reference's own recorded numbers: the restatement of
+// poisson.mjs reproduces results/poisson-128-face.txt digit for digit and results/result-new-mg.json to a
+// few per cent.  Advection, the source terms and projection are parity unpinned by the reference: it holds
+// no golden vectors for them and its WGSL cannot run here (no WebGPU device, no Node); they are pinned only
+// by this line-by-line restatement and by independent numpy restatements of each stage (tests/).
 #include <cmath>
 #include <cstdint>
 #include <cstring>
