@@ -36,6 +36,7 @@
 #include "fire_device.cuh"
 #include "fire_launch.cuh"
 #include "fire_simobj.h"
+#include "fire_nvtx.h"
 
 namespace fire {
 
@@ -1010,6 +1011,7 @@ float4* adj_buf4(FireAdjoint* A, int which) {
 extern "C" {
 
 int fire_adjoint_create(FireSim* sim, int n_steps, int checkpoint_every, FireAdjoint** out) {
+  FIRE_RANGE("fire_adjoint_create");
   if (!sim || !out || n_steps < 1 || checkpoint_every < 1 || checkpoint_every > 512) return FIRE_ERR_BAD_ARG;
   *out = nullptr;
   if (cudaSetDevice(sim->device) != cudaSuccess) return FIRE_ERR_CUDA;
@@ -1074,6 +1076,7 @@ int fire_adjoint_destroy(FireAdjoint* A) {
 }
 
 int fire_adjoint_forward(FireAdjoint* A, float dt, void* stream) {
+  FIRE_RANGE("fire_adjoint_forward");
   if (!A || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
   FireSim* sim = A->sim;
   ACK(cudaSetDevice(sim->device));
@@ -1149,6 +1152,7 @@ int fire_adjoint_seed(FireAdjoint* A, const float* d_vel, const float* d_S, cons
 }
 
 int fire_adjoint_backward(FireAdjoint* A, void* stream) {
+  FIRE_RANGE("fire_adjoint_backward");
   if (!A) return FIRE_ERR_BAD_ARG;
   FireSim* sim = A->sim;
   if (!A->forwardDone) return set_err(sim, FIRE_ERR_STATE, "fire_adjoint_backward before fire_adjoint_forward");
@@ -1204,6 +1208,7 @@ int fire_adjoint_clear(FireAdjoint* A) {
 }
 
 int fire_adjoint_stage(FireAdjoint* A, int stage, float dt, int arg, void* stream) {
+  FIRE_RANGE("fire_adjoint_stage");
   if (!A || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
   FireSim* sim = A->sim;
   ACK(cudaSetDevice(sim->device));

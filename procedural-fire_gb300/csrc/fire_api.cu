@@ -63,6 +63,7 @@ size_t align_up(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
 }  // namespace
 
 #include "fire_simobj.h"
+#include "fire_nvtx.h"
 
 namespace fire {
 namespace rt {
@@ -348,6 +349,7 @@ int fire_device_ok(int device) {
 }
 
 int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSim** out) {
+  FIRE_RANGE("fire_sim_create");
   FireSim* sim = nullptr;
   if (!cfg || !out) return FIRE_ERR_BAD_ARG;
   *out = nullptr;
@@ -487,6 +489,7 @@ int fire_sim_destroy(FireSim* sim) {
 }
 
 int fire_sim_step(FireSim* sim, float dt, int n_steps, void* stream) {
+  FIRE_RANGE("fire_sim_step");
   if (!sim || n_steps < 0 || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
@@ -695,6 +698,7 @@ size_t save_bytes(const FireSim* s) {
 }  // namespace
 
 int fire_sim_save(FireSim* sim, void* buf, size_t capacity, size_t* bytes_out) {
+  FIRE_RANGE("fire_sim_save");
   if (!sim || !bytes_out) return FIRE_ERR_BAD_ARG;
   const size_t need = save_bytes(sim);
   *bytes_out = need;
@@ -736,6 +740,7 @@ int fire_sim_save(FireSim* sim, void* buf, size_t capacity, size_t* bytes_out) {
 }
 
 int fire_sim_load(FireSim* sim, const void* buf, size_t bytes) {
+  FIRE_RANGE("fire_sim_load");
   if (!sim || !buf) return FIRE_ERR_BAD_ARG;
   if (bytes != save_bytes(sim)) return set_err(sim, FIRE_ERR_BAD_ARG, "load: %zu bytes, this simulation's state is %zu", bytes, save_bytes(sim));
   SaveHeader h;
@@ -866,12 +871,16 @@ int fire_sim_info(FireSim* sim, FireInfo* out) {
 const char* fire_sim_last_error(FireSim* sim) { return sim ? sim->err.c_str() : "null handle"; }
 
 int fire_sim_run_stage(FireSim* sim, int stage, float dt, void* stream) {
+  FIRE_RANGE("fire_sim_run_stage");
   if (!sim || stage < 0 || stage >= FIRE_STAGE_COUNT) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
   int rc = upload_block(sim, dt, st, stage == FIRE_STAGE_GEO);
   if (rc) return rc;
   const float* P = sim->dBlock;
+  static const char* const kStageRange[FIRE_STAGE_COUNT] = {"stage:geo", "stage:adv1", "stage:adv2", "stage:curl",
+                                                            "stage:forces", "stage:div", "stage:vcycle", "stage:project"};
+  FIRE_RANGE(kStageRange[stage]);
   switch (stage) {
     case FIRE_STAGE_GEO: sim->geoReady = false; rc = ensure_geo(sim, st); if (rc) return rc; break;
     case FIRE_STAGE_ADV1: launch_adv1(P, sim->f, sim->d, st); break;
@@ -887,6 +896,7 @@ int fire_sim_run_stage(FireSim* sim, int stage, float dt, void* stream) {
 }
 
 int fire_sim_run_mg(FireSim* sim, int op, int level, int arg, void* stream) {
+  FIRE_RANGE("fire_sim_run_mg");
   if (!sim || level < 0 || level >= (int)sim->levels.size()) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
@@ -958,6 +968,7 @@ int fire_sim_stage_times(FireSim* sim, float* ms, int n) {
 }
 
 int fire_sim_residual(FireSim* sim, double* rel, void* stream) {
+  FIRE_RANGE("fire_sim_residual");
   if (!sim || !rel) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
@@ -970,6 +981,7 @@ int fire_sim_residual(FireSim* sim, double* rel, void* stream) {
 }
 
 int fire_sim_stats(FireSim* sim, int which, double* out16, void* stream) {
+  FIRE_RANGE("fire_sim_stats");
   if (!sim || !out16) return FIRE_ERR_BAD_ARG;
   float* f = field_ptr4(sim, which);
   if (!f) return set_err(sim, FIRE_ERR_BAD_ARG, "stats: field %d is not a 4-channel grid field", which);
@@ -983,6 +995,7 @@ int fire_sim_stats(FireSim* sim, int which, double* out16, void* stream) {
   return FIRE_OK;
 }
 int fire_sim_hrr(FireSim* sim, double* q_kw, void* stream) {
+  FIRE_RANGE("fire_sim_hrr");
   if (!sim || !q_kw) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
@@ -994,6 +1007,7 @@ int fire_sim_hrr(FireSim* sim, double* q_kw, void* stream) {
   return FIRE_OK;
 }
 int fire_sim_height_profile(FireSim* sim, double* rows6, int max_rows, int* n_rows, void* stream) {
+  FIRE_RANGE("fire_sim_height_profile");
   if (!sim || !rows6 || !n_rows) return FIRE_ERR_BAD_ARG;
   const int n = height_profile_rows(sim->d);
   *n_rows = n;
@@ -1011,6 +1025,7 @@ int fire_sim_height_profile(FireSim* sim, double* rows6, int max_rows, int* n_ro
   return FIRE_OK;
 }
 int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream) {
+  FIRE_RANGE("fire_sim_stats_async");
   if (!sim || !pinned_out17) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
@@ -1222,6 +1237,7 @@ int fire_ensemble_destroy(FireEnsemble* e) {
 }
 
 int fire_ensemble_create(const FireConfig* cfgs, int n, FireEnsemble** out) {
+  FIRE_RANGE("fire_ensemble_create");
   if (!cfgs || !out || n < 1 || n > BATCH_MAX) return FIRE_ERR_BAD_ARG;
   *out = nullptr;
   for (int i = 0; i < n; ++i) {
@@ -1284,6 +1300,7 @@ int fire_ensemble_sim(FireEnsemble* e, int i, FireSim** out) {
 }
 
 int fire_ensemble_step(FireEnsemble* e, float dt, int n_steps, void* stream) {
+  FIRE_RANGE("fire_ensemble_step");
   if (!e || n_steps < 0 || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
   if (cudaSetDevice(e->device) != cudaSuccess) return FIRE_ERR_CUDA;
   cudaStream_t st = as_stream(stream);
@@ -1426,6 +1443,7 @@ SparkU spark_uniforms(FireSparks* s, float dt, bool commit) {
 extern "C" {
 
 int fire_sparks_create(FireSim* sim, int count, FireSparks** out) {
+  FIRE_RANGE("fire_sparks_create");
   if (!sim || !out || count < 1 || count > (1 << 24)) return FIRE_ERR_BAD_ARG;
   *out = nullptr;
   CK(cudaSetDevice(sim->device));
@@ -1500,6 +1518,7 @@ int fire_sparks_peek(FireSparks* s, float dt, float* out27) {
 
 // One spark step after the simulation's step on the same stream (it reads the simulation's velocity).
 int fire_sparks_step(FireSparks* s, float dt, void* stream) {
+  FIRE_RANGE("fire_sparks_step");
   if (!s || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
   if (cudaSetDevice(s->sim->device) != cudaSuccess) return FIRE_ERR_CUDA;
   const SparkU U = spark_uniforms(s, dt, true);

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include "../../include/fire_sim.h"
 #include "fire_internal.h"
+#include "fire_nvtx.h"
 
 namespace fire {
 
@@ -62,6 +63,7 @@ size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 using namespace fire;
 
 extern "C" int fire_poisson_vcycles_noalloc(float* p, const float* b, int nx, int ny, int nz, float h, int cycles, void* stream) {
+  FIRE_RANGE("fire_poisson_vcycles_noalloc");
   if (!p || !b || nx < 2 || ny < 2 || nz < 2 || !(h > 0.0f) || cycles < 0) return FIRE_ERR_BAD_ARG;
   // level hierarchy and coarse sweep count as the simulation builds them (src/sim.js:79-92)
   std::vector<MGLevel> levels;

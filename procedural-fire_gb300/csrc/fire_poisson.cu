@@ -27,6 +27,7 @@
 #include "fire_internal.h"
 #include "fire_device.cuh"
 #include "fire_launch.cuh"
+#include "fire_nvtx.h"
 
 namespace fire {
 namespace {
@@ -1025,6 +1026,7 @@ constexpr int COARSE_DIRECT_MAX = 512;   // coarsest levels up to this many cell
 extern "C" {
 
 int fire_poisson_create(const int res[3], float h, int precision, int device, FirePoisson** out) {
+  FIRE_RANGE("fire_poisson_create");
   if (!out) return FIRE_ERR_BAD_ARG;
   *out = nullptr;
   if (!res || res[0] < 2 || res[1] < 2 || res[2] < 2 || !(h > 0.0f)) return FIRE_ERR_BAD_ARG;
@@ -1127,6 +1129,7 @@ int fire_poisson_destroy(FirePoisson* ps) {
 }
 
 int fire_poisson_solve(FirePoisson* ps, const float* b, float* x, float* x_lo, double tol, int max_iters, int inner_cycles, void* stream) {
+  FIRE_RANGE("fire_poisson_solve");
   if (!ps || !b || !x || !(tol >= 0.0) || max_iters < 0 || (const void*)b == (const void*)x) return FIRE_ERR_BAD_ARG;
   if (x_lo && ((const void*)x_lo == (const void*)x || (const void*)x_lo == (const void*)b)) return FIRE_ERR_BAD_ARG;
   if (ps->ir && (inner_cycles < 1 || inner_cycles > 16)) return FIRE_ERR_BAD_ARG;
@@ -1188,6 +1191,7 @@ int fire_poisson_set_study(FirePoisson* ps, int coarse_sweeps) {
 }
 
 int fire_poisson_make_rhs(FirePoisson* ps, float* b, unsigned seed, int n_sources, float noise, void* stream) {
+  FIRE_RANGE("fire_poisson_make_rhs");
   if (!ps || !b || n_sources < 0 || n_sources > MAX_SOURCES) return FIRE_ERR_BAD_ARG;
   DeviceGuard dg(ps->device);
   std::vector<float> src((size_t)std::max(1, n_sources) * 5, 0.0f);

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/fire_sim.h"
+#include "fire_nvtx.h"
 
 namespace {
 
@@ -315,6 +316,7 @@ static int fire_event(FireSparks* sp, const FireTimelineEvent& e) {
 // capStep(j) (src/main.js:153-160): parameters and log offsets at t = j / (FPS n), the events in
 // [t, t_next), then one simulation step and one spark step (simStep, src/main.js:70-76) of 1 / (FPS n).
 int fire_timeline_step(FireTimeline* tl, FireSim* sim, FireSparks* sparks, long long j, void* stream) {
+  FIRE_RANGE("fire_timeline_step");
   if (!tl || !sim) return FIRE_ERR_BAD_ARG;
   const double t = fire_timeline_step_time(tl, j), tNext = fire_timeline_step_time(tl, j + 1);
   double p[7];

@@ -21,6 +21,7 @@
 #include "../../include/fire_sim.h"
 #include "fire_device.cuh"
 #include "fire_launch.cuh"
+#include "fire_nvtx.h"
 
 namespace fire {
 namespace {
@@ -294,6 +295,7 @@ struct FireVolume {
 extern "C" {
 
 int fire_volume_create(FireSim* sim, int width, int height, float vol_scale, float white_balance_k, FireVolume** out) {
+  FIRE_RANGE("fire_volume_create");
   if (!sim || !out || width < 1 || height < 1 || !(vol_scale > 0.0f)) return FIRE_ERR_BAD_ARG;
   *out = nullptr;
   FireInfo info;
@@ -401,6 +403,7 @@ int fire_volume_uniforms(FireVolume* v, double time, int frame, float* out, int 
 
 // One render: lights, the optional prefilter, the march (renderHDR's fire passes, src/renderer.js:666-690).
 int fire_volume_render(FireVolume* v, double time, int frame, void* stream) {
+  FIRE_RANGE("fire_volume_render");
   if (!v) return FIRE_ERR_BAD_ARG;
   float raw[VOLU_FLOATS];
   if (fire_volume_uniforms(v, time, frame, raw, VOLU_FLOATS) < 0) return FIRE_ERR_STATE;
