@@ -140,9 +140,8 @@ struct ParamsByValue {
 };
 template <class PA, class Nb>
 __device__ __forceinline__ void forces_cell(const PA& pa, const Fields& f, const uint2* __restrict__ noiseT,
-                                            const uint2* __restrict__ curlT, Dims d, int i, int j, int k, const Nb& nb,
-                                            float4 s, float4 s2, const float4 geo) {
-  const size_t ci = cell(i, j, k, d.nx, d.ny);
+                                            const uint2* __restrict__ curlT, Dims d, int i, int j, int k, unsigned ci,
+                                            const Nb& nb, float4 s, float4 s2, const float4 geo) {
   const float dt = pa[P_dt], dx = pa[P_dx], I = pa[P_intensity];
   const float seed = pa[P_seed], time = pa[P_time];
   f3 p = mk3(pa[P_ox], pa[P_oy], pa[P_oz]) + mk3((float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f) * dx;
@@ -351,7 +350,8 @@ __global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fie
   if (!id.ok) return;
   GlobalNb<kFusedCurl> nb{f, d, id.i, id.j, id.k};
   const size_t ci = cell(id.i, id.j, id.k, d.nx, d.ny);
-  forces_cell(ParamsGlobal{P}, f, noiseT, curlT, d, id.i, id.j, id.k, nb, __ldg(f.SY + ci), __ldg(f.S2Y + ci), __ldg(f.geo + ci));
+  forces_cell(ParamsGlobal{P}, f, noiseT, curlT, d, id.i, id.j, id.k, (unsigned)ci, nb, __ldg(f.SY + ci), __ldg(f.S2Y + ci),
+              __ldg(f.geo + ci));
 }
 
 // ---- z-marching shared-memory variant of curl + forces ----
@@ -389,73 +389,118 @@ struct TileNb {
   }
 };
 __device__ __forceinline__ int clampi(int v, int n) { return min(max(v, 0), n - 1); }
-// Loads logical plane z (clamped) of velY for the tile at (x0, y0) into `dst`.
-__device__ __forceinline__ void load_vplane(float4* dst, const float4* __restrict__ velY, int x0, int y0, int z, Dims d) {
-  const int zc = clampi(z, d.nz);
-  for (int t = threadIdx.y * FT_X + threadIdx.x; t < VX * VY; t += FT_X * FT_Y) {
-    const int lx = t % VX, ly = t / VX;
-    dst[t] = __ldg(velY + cell(clampi(x0 + lx - 2, d.nx), clampi(y0 + ly - 2, d.ny), zc, d.nx, d.ny));
+// 16-byte asynchronous global -> shared copy (cached in L2 only), and its group commit / wait.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+// The plane-independent part of a thread's share of the ring traffic for one column tile, worked out once
+// per march: each thread copies velY elements t = tid and tid + 256 of a plane and forms vorticity elements
+// t = tid and tid + 256.
+//  * vsrc[k]: x + nx * y of velY element k's source, clamped to the domain as `ld` does (-1: no element);
+//  * wtap[k]: vorticity element k's velY ring offset (bits 0-9) and which of its x-, x+, y-, y+ neighbours lie
+//    inside the domain (bits 10-13; a clamped neighbour is the centre itself) (-1: no element).
+constexpr int FT_N = FT_X * FT_Y;
+static_assert(VX * VY <= 2 * FT_N && WX * WY <= 2 * FT_N && VX * VY < 1024, "two ring elements per thread, 10-bit offsets");
+struct MarchPlan {
+  int vsrc[2], wtap[2];
+};
+__device__ __forceinline__ MarchPlan march_plan(int x0, int y0, Dims d) {
+  MarchPlan m;
+  const int tid = threadIdx.y * FT_X + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int t = tid + k * FT_N;
+    m.vsrc[k] = -1;
+    m.wtap[k] = -1;
+    if (t < VX * VY) {
+      const int lx = t % VX, ly = t / VX;
+      m.vsrc[k] = clampi(x0 + lx - 2, d.nx) + d.nx * clampi(y0 + ly - 2, d.ny);
+    }
+    if (t < WX * WY) {
+      const int lx = t % WX, ly = t / WX;
+      // clamp the position to the domain, then express it in tile coordinates (velY tile origin at -2)
+      const int gx = clampi(x0 + lx - 1, d.nx), gy = clampi(y0 + ly - 1, d.ny);
+      const int c = (gy - y0 + 2) * VX + (gx - x0 + 2);
+      m.wtap[k] = c | (gx > 0) << 10 | (gx < d.nx - 1) << 11 | (gy > 0) << 12 | (gy < d.ny - 1) << 13;
+    }
   }
+  return m;
+}
+// Starts the copy of logical plane z (clamped) of velY for the march's tile into `dst`; the caller commits and
+// waits.
+__device__ __forceinline__ void load_vplane(float4* dst, const float4* __restrict__ velY, const MarchPlan& m, int z, Dims d) {
+  const unsigned zo = (unsigned)clampi(z, d.nz) * (unsigned)(d.nx * d.ny);
+  const int tid = threadIdx.y * FT_X + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    if (m.vsrc[k] >= 0) cp_async16(dst + tid + k * FT_N, velY + (zo + (unsigned)m.vsrc[k]));
 }
 // Vorticity of logical plane zlog into `dst` (positions clamped to the domain), from the velY ring.  The
 // planes it reads (clamp(zlog) and its clamped z neighbours) are resident in the ring when this is called.
-__device__ __forceinline__ void curl_plane(float4* dst, float4* vbuf, int zlog, int x0, int y0, Dims d) {
+__device__ __forceinline__ void curl_plane(float4* dst, float4* vbuf, const MarchPlan& m, int zlog, Dims d) {
   const int zc = clampi(zlog, d.nz);
   const float4* PK = vslot(vbuf, clampi(zc - 1, d.nz));
   const float4* P0 = vslot(vbuf, zc);
   const float4* PF = vslot(vbuf, clampi(zc + 1, d.nz));
-  for (int t = threadIdx.y * FT_X + threadIdx.x; t < WX * WY; t += FT_X * FT_Y) {
-    const int lx = t % WX, ly = t / WX;
-    // clamp the position to the domain, then express it in tile coordinates (velY tile origin at -2)
-    const int gx = clampi(x0 + lx - 1, d.nx), gy = clampi(y0 + ly - 1, d.ny);
-    const int vx = gx - x0 + 2, vy = gy - y0 + 2;
-    const int xm = clampi(gx - 1, d.nx) - x0 + 2, xp = clampi(gx + 1, d.nx) - x0 + 2;
-    const int ym = clampi(gy - 1, d.ny) - y0 + 2, yp = clampi(gy + 1, d.ny) - y0 + 2;
-    f3 L = xyz(P0[vy * VX + xm]), R = xyz(P0[vy * VX + xp]);
-    f3 B = xyz(P0[ym * VX + vx]), T = xyz(P0[yp * VX + vx]);
-    f3 K = xyz(PK[vy * VX + vx]), F = xyz(PF[vy * VX + vx]);
+  const int tid = threadIdx.y * FT_X + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int tap = m.wtap[k];
+    if (tap < 0) continue;
+    const int c = tap & 1023;
+    f3 L = xyz(P0[c - ((tap >> 10) & 1)]), R = xyz(P0[c + ((tap >> 11) & 1)]);
+    f3 B = xyz(P0[c - ((tap >> 12) & 1) * VX]), T = xyz(P0[c + ((tap >> 13) & 1) * VX]);
+    f3 K = xyz(PK[c]), F = xyz(PF[c]);
     f3 w = mk3((T.z - B.z) - (F.y - K.y), (F.x - K.x) - (R.z - L.z), (R.y - L.y) - (T.x - B.x)) * 0.5f;
-    dst[t] = make_float4(w.x, w.y, w.z, len3(w));
+    dst[tid + k * FT_N] = make_float4(w.x, w.y, w.z, len3(w));
   }
 }
-// Marches the column tile at (x0, y0) through planes [z0, z1), z1 > z0.
+// Marches the column tile at (x0, y0) through planes [z0, z1), z1 > z0.  The copy of the next velY plane is
+// started before the current plane's source terms and completes behind them: it goes to the slot of plane
+// z - 2, which nothing reads any more (the vorticity of z - 1 was formed three planes ago, and the previous
+// plane's Laplacian finished before the last barrier).
 template <class PA>
 __device__ __forceinline__ void forces_march(const PA& pa, const Fields& f, const uint2* __restrict__ noiseT,
                                              const uint2* __restrict__ curlT, Dims d, int x0, int y0, int z0, int z1,
                                              float4* fsm) {
   float4* vbuf = fsm;                    // 5 * VX * VY
   float4* wbuf = fsm + 5 * VX * VY;      // 3 * WX * WY
-  for (int z = z0 - 2; z <= z0 + 2; ++z) load_vplane(vslot(vbuf, z), f.velY, x0, y0, z, d);
+  const MarchPlan m = march_plan(x0, y0, d);
+  for (int z = z0 - 2; z <= z0 + 2; ++z) load_vplane(vslot(vbuf, z), f.velY, m, z, d);
+  cp_async_commit();
+  cp_async_wait_all();
   __syncthreads();
-  for (int z = z0 - 1; z <= z0 + 1; ++z) curl_plane(wslot(wbuf, z), vbuf, z, x0, y0, d);
+  for (int z = z0 - 1; z <= z0 + 1; ++z) curl_plane(wslot(wbuf, z), vbuf, m, z, d);
   __syncthreads();
   const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
   const bool mine = i < d.nx && j < d.ny;
+  const unsigned plane = (unsigned)(d.nx * d.ny);
+  unsigned ci = mine ? (unsigned)i + (unsigned)d.nx * ((unsigned)j + (unsigned)d.ny * (unsigned)z0) : 0u;
   // this thread's SY, S2Y, geo for the current plane, loaded one plane ahead
   float4 s_n = make_float4(0.0f, 0.0f, 0.0f, 0.0f), s2_n = s_n, g_n = s_n;
-  if (mine) {
-    const size_t c0 = cell(i, j, z0, d.nx, d.ny);
-    s_n = __ldg(f.SY + c0); s2_n = __ldg(f.S2Y + c0); g_n = __ldg(f.geo + c0);
-  }
-  for (int z = z0; z < z1; ++z) {
+  if (mine) { s_n = __ldg(f.SY + ci); s2_n = __ldg(f.S2Y + ci); g_n = __ldg(f.geo + ci); }
+  for (int z = z0; z < z1; ++z, ci += plane) {
     const float4 s = s_n, s2 = s2_n, g = g_n;
-    if (mine && z + 1 < z1) {
-      const size_t c1 = cell(i, j, z + 1, d.nx, d.ny);
-      s_n = __ldg(f.SY + c1); s2_n = __ldg(f.S2Y + c1); g_n = __ldg(f.geo + c1);
+    const bool more = z + 1 < z1;
+    if (more) {
+      load_vplane(vslot(vbuf, z + 3), f.velY, m, z + 3, d);   // into the slot of plane z - 2
+      cp_async_commit();
     }
+    if (mine && more) { s_n = __ldg(f.SY + ci + plane); s2_n = __ldg(f.S2Y + ci + plane); g_n = __ldg(f.geo + ci + plane); }
     if (mine) {
       TileNb nb;
       nb.vm = vslot(vbuf, z - 1); nb.v0 = vslot(vbuf, z); nb.vp = vslot(vbuf, z + 1);
       nb.wm = wslot(wbuf, z - 1); nb.w0 = wslot(wbuf, z); nb.wp = wslot(wbuf, z + 1);
       nb.tx = threadIdx.x;
       nb.ty = threadIdx.y;
-      forces_cell(pa, f, noiseT, curlT, d, i, j, z, nb, s, s2, g);
+      forces_cell(pa, f, noiseT, curlT, d, i, j, z, ci, nb, s, s2, g);
     }
-    if (z + 1 < z1) {
-      __syncthreads();                                   // everyone is done with vorticity plane z - 1
-      load_vplane(vslot(vbuf, z + 3), f.velY, x0, y0, z + 3, d);   // replaces plane z - 2
-      __syncthreads();
-      curl_plane(wslot(wbuf, z + 2), vbuf, z + 2, x0, y0, d);       // replaces vorticity plane z - 1
+    if (more) {
+      cp_async_wait_all();
+      __syncthreads();          // plane z + 3 is visible; everyone is done with vorticity plane z - 1
+      curl_plane(wslot(wbuf, z + 2), vbuf, m, z + 2, d);       // replaces vorticity plane z - 1
       __syncthreads();
     }
   }
