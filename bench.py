@@ -178,9 +178,10 @@ def make_sim(F, device: int, mg_fixed: int = 0):
 def launches_per_step(sim, cycles_per_step: float) -> float:
     """Kernels launched per step by the captured graph: 5 stencil kernels and the cycle-counter reset, and per
     V-cycle 10 per level above the shared-memory tail (2 + 2 red-black sweeps of 2 colour launches each,
-    restriction, prolongation), the tail kernel, the residual norm and the decision kernel.  The tail starts at
-    the finest level that fits in 200 KB of shared memory (one CTA, or 8 CTAs with distributed levels) and has
-    at most 8192 cells."""
+    restriction, prolongation) less one per level below the finest (its first colour-0 sweep runs inside the
+    restriction onto it), the tail kernel, the residual norm and the decision kernel.  The tail starts at the
+    finest level that fits in 200 KB of shared memory (one CTA, or 8 CTAs with distributed levels) and has at
+    most 8192 cells."""
     n = len(sim.levels)
     T = n
     for l in range(n - 1, -1, -1):
@@ -196,7 +197,8 @@ def launches_per_step(sim, cycles_per_step: float) -> float:
             T = l
         else:
             break
-    per_cycle = 10 * T + (1 if T < n else 0) + 2
+    top = min(T, n - 1)
+    per_cycle = 10 * top - max(top - 1, 0) + (1 if T < n else 0) + 2
     return 6 + per_cycle * cycles_per_step
 
 

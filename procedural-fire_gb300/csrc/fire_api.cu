@@ -183,15 +183,25 @@ int upload_block(FireSim* sim, float dt, cudaStream_t st, bool with_logs, const 
 }
 
 // `iters` red-black sweeps of level l (src/sim.js:576-586): colour 0 then colour 1, one launch each.
-void record_smooth(FireSim* s, int l, int iters, cudaStream_t st) {
-  for (int k = 0; k < iters; ++k) { launch_smooth(s->levels[l], 0, st); launch_smooth(s->levels[l], 1, st); }
+// `iters` red-black sweeps of level l; with first_done the first colour-0 sweep has already been applied
+// (by the fused restriction).
+void record_smooth(FireSim* s, int l, int iters, cudaStream_t st, bool first_done = false) {
+  for (int k = 0; k < iters; ++k) {
+    if (k > 0 || !first_done) launch_smooth(s->levels[l], 0, st);
+    launch_smooth(s->levels[l], 1, st);
+  }
 }
-// One V(2,2) cycle (src/sim.js:588-599).  Levels [tailFirst, n) run inside one single-CTA kernel.
+// One V(2,2) cycle (src/sim.js:588-599).  Levels [tailFirst, n) run inside one tail kernel.  A restriction
+// onto a level that is smoothed by launches also applies that level's first colour-0 sweep.
 void record_vcycle(FireSim* s, cudaStream_t st) {
   const int n = (int)s->levels.size();
   const int T = s->tailFirst;
   const int top = std::min(T, n - 1);
-  for (int i = 0; i < top; ++i) { record_smooth(s, i, 2, st); launch_restrict(s->levels[i], s->levels[i + 1], st); }
+  for (int i = 0; i < top; ++i) {
+    record_smooth(s, i, 2, st, i > 0);
+    if (i + 1 < top) launch_restrict_smooth(s->levels[i], s->levels[i + 1], st);
+    else launch_restrict(s->levels[i], s->levels[i + 1], st);
+  }
   if (T < n) launch_tail(s->levels.data(), T, n, 2, 2, s->coarseIters, s->dCounter + 2, st, false, nullptr, s->tailWaitPolls);
   else record_smooth(s, n - 1, s->coarseIters, st);
   for (int i = top - 1; i >= 0; --i) { launch_prolong(s->levels[i], s->levels[i + 1], st); record_smooth(s, i, 2, st); }

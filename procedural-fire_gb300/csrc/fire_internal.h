@@ -142,6 +142,9 @@ void launch_project_batch(const BatchMap& m, const StepBatch& I, int tile, cudaS
 // ---- kernel launchers (fire_mg.cu) ----
 cudaError_t launch_smooth(const MGLevel& L, int color, cudaStream_t st);
 cudaError_t launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st);
+// Restriction fused with the coarse level's first colour-0 sweep (bit-identical to launch_restrict followed
+// by launch_smooth(C, 0)); not for study levels.
+cudaError_t launch_restrict_smooth(const MGLevel& F, const MGLevel& C, cudaStream_t st);
 cudaError_t launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st);
 // One launch runs the V-cycle over levels [first, n) out of shared memory: a single CTA when every level
 // fits in its shared memory, or a thread-block cluster whose CTAs each hold a z-slab of the finer tail

@@ -134,6 +134,37 @@ __device__ __forceinline__ void restrict_body(const float* __restrict__ p, const
   bc[t] = restrict_cell(p, b, cx, cy, cz, nx, ny, nz, ih2);
   pc[t] = 0.0f;
 }
+// Restriction fused with the coarse level's first colour-0 sweep.  The coarse pressure starts at zero, so that
+// sweep's update of a colour-0 cell reads only the cell's own right-hand side: it is formed here from the value
+// just restricted with the smoother's arithmetic (rb_update over zero neighbours: the same diagonal, the same
+// explicit FMA and quotient, the same relaxation from an old value of zero), so the result is bit-identical
+// to restricting and then sweeping.  Colour-1 cells keep zero.
+template <bool kRelax>
+__device__ __forceinline__ void restrict_smooth_body(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
+                                                     float h, float* __restrict__ bc, float* __restrict__ pc, float hc, float omega,
+                                                     uint3 blk) {
+  pdl_wait();
+  pdl_trigger();
+  const int cnx = nx / 2, cny = ny / 2, cnz = nz / 2;
+  const int cx = blk.x * GX + threadIdx.x, cy = blk.y * GY + threadIdx.y, cz = blk.z * GZ + threadIdx.z;
+  if (cx >= cnx || cy >= cny || cz >= cnz) return;
+  const int t = cx + cnx * (cy + cny * cz);
+  const float r = restrict_cell(p, b, cx, cy, cz, nx, ny, nz, 1.0f / (h * h));
+  bc[t] = r;
+  float v = 0.0f;
+  if (((cx + cy + cz) & 1) == 0) {
+    float diag = 6.0f;   // rb_update's ghost rules: open sides and top add 1, the floor subtracts 1
+    if (cx == 0) diag += 1.0f;
+    if (cx == cnx - 1) diag += 1.0f;
+    if (cz == 0) diag += 1.0f;
+    if (cz == cnz - 1) diag += 1.0f;
+    if (cy == 0) diag -= 1.0f;
+    if (cy == cny - 1) diag += 1.0f;
+    v = __fdividef(__fmaf_rn(-(hc * hc), r, 0.0f), diag);
+    if (kRelax) v = fmaf(omega, v - 0.0f, 0.0f);
+  }
+  pc[t] = v;
+}
 
 // ---------------- prolongation with mirror ghosts (src/sim.js:468-495) ----------------
 template <bool kClamp = false>
@@ -214,6 +245,12 @@ __global__ void __launch_bounds__(GX * GY * GZ) k_smooth(float* __restrict__ p, 
 __global__ void __launch_bounds__(GX * GY * GZ) k_restrict(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
                                                            float h, float* __restrict__ bc, float* __restrict__ pc) {
   restrict_body(p, b, nx, ny, nz, h, bc, pc, blockIdx);
+}
+template <bool kRelax>
+__global__ void __launch_bounds__(GX * GY * GZ) k_restrict_smooth(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny,
+                                                                  int nz, float h, float* __restrict__ bc, float* __restrict__ pc, float hc,
+                                                                  float omega) {
+  restrict_smooth_body<kRelax>(p, b, nx, ny, nz, h, bc, pc, hc, omega, blockIdx);
 }
 __global__ void __launch_bounds__(GX * GY * GZ) k_prolong(float* __restrict__ p, const float* __restrict__ pc, int nx, int ny, int nz) {
   prolong_body(p, pc, nx, ny, nz, blockIdx);
@@ -1014,6 +1051,11 @@ cudaError_t launch_smooth(const MGLevel& L, int color, cudaStream_t st) {
 }
 cudaError_t launch_restrict(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
   return launch_pdl(k_restrict, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, (const float*)F.p, (const float*)F.b, F.nx, F.ny, F.nz, F.h, C.b, C.p);
+}
+cudaError_t launch_restrict_smooth(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
+  if (C.study) return cudaErrorInvalidValue;   // the studies' smoother has its own update; not fused
+  return launch_pdl(C.omega == 1.0f ? k_restrict_smooth<false> : k_restrict_smooth<true>, grid3(C.nx, C.ny, C.nz), kBlock, 0, st,
+                    (const float*)F.p, (const float*)F.b, F.nx, F.ny, F.nz, F.h, C.b, C.p, C.h, C.omega);
 }
 cudaError_t launch_prolong(const MGLevel& F, const MGLevel& C, cudaStream_t st) {
   return launch_pdl(F.study ? k_prolong_clamp : k_prolong, grid3(C.nx, C.ny, C.nz), kBlock, 0, st, F.p, (const float*)C.p, F.nx, F.ny, F.nz);
