@@ -699,6 +699,7 @@ struct SaveHeader {
   int32_t counters[4];   // the residual loop's counters (cumulative cycles, first cycle the next step tests)
   int32_t lastCycles;
   double lastRel;
+  double predictor[3];   // the residual loop's predictor state (reduction per cycle, last tested residual, its cycle)
 };
 const char kSaveMagic[8] = {'F', 'I', 'R', 'E', 'S', 'I', 'M', '1'};
 size_t save_bytes(const FireSim* s) {
@@ -719,7 +720,7 @@ int fire_sim_save(FireSim* sim, void* buf, size_t capacity, size_t* bytes_out) {
   SaveHeader h;
   std::memset(&h, 0, sizeof h);
   std::memcpy(h.magic, kSaveMagic, sizeof h.magic);
-  h.version = 1;
+  h.version = 2;
   h.header_bytes = (uint32_t)sizeof h;
   for (int i = 0; i < 3; ++i) { h.res[i] = sim->res[i]; h.size[i] = sim->size[i]; }
   h.time = sim->time;
@@ -737,6 +738,7 @@ int fire_sim_save(FireSim* sim, void* buf, size_t capacity, size_t* bytes_out) {
   h.counters[2] = 0;   // per-step cycle count and wait-timeout flag are not state
   h.lastCycles = sim->lastCycles;
   h.lastRel = sim->lastRel;
+  CK(cudaMemcpy(h.predictor, sim->dSmall + 20, sizeof h.predictor, cudaMemcpyDeviceToHost));
   char* o = static_cast<char*>(buf);
   std::memcpy(o, &h, sizeof h);
   o += sizeof h;
@@ -755,7 +757,7 @@ int fire_sim_load(FireSim* sim, const void* buf, size_t bytes) {
   if (bytes != save_bytes(sim)) return set_err(sim, FIRE_ERR_BAD_ARG, "load: %zu bytes, this simulation's state is %zu", bytes, save_bytes(sim));
   SaveHeader h;
   std::memcpy(&h, buf, sizeof h);
-  if (std::memcmp(h.magic, kSaveMagic, sizeof h.magic) != 0 || h.version != 1 || h.header_bytes != sizeof h)
+  if (std::memcmp(h.magic, kSaveMagic, sizeof h.magic) != 0 || h.version != 2 || h.header_bytes != sizeof h)
     return set_err(sim, FIRE_ERR_BAD_ARG, "load: not a saved simulation state of this version");
   for (int i = 0; i < 3; ++i)
     if (h.res[i] != sim->res[i] || h.size[i] != sim->size[i]) return set_err(sim, FIRE_ERR_BAD_ARG, "load: saved for another grid");
@@ -770,6 +772,7 @@ int fire_sim_load(FireSim* sim, const void* buf, size_t bytes) {
   }
   CK(cudaMemcpy(sim->levels[0].p, in, cells * sizeof(float), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(sim->dCounter, h.counters, sizeof h.counters, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(sim->dSmall + 20, h.predictor, sizeof h.predictor, cudaMemcpyHostToDevice));
   sim->time = h.time;
   sim->frame = h.frame;
   sim->stepsRun = h.stepsRun;

@@ -1010,9 +1010,11 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
   __shared__ int skip;
   pdl_wait();
   pdl_trigger();
-  // Cycles before counter[3] (one less than the previous step needed, kept below max_cycles) run without a
-  // convergence test: the previous step's count is a good predictor, and each skipped test saves the
-  // norm's pass over level 0.  The solve still stops only on a tested residual <= tol (or max_cycles).
+  // Cycles before counter[3] run without a convergence test (each skipped test saves the norm's pass over
+  // level 0 and the sum); the solve still stops only on a tested residual <= tol (or at max_cycles).
+  // counter[3] is set when a step stops (below) from the cycle count it needed and the per-cycle reduction
+  // of the residual; sums2[20..22] hold that reduction (0: not measured yet), the residual of the most recent
+  // tested cycle and that cycle's index in counter[1].
   if (threadIdx.x == 0) {
     const int c = counter[0] + 1;
     skip = c < counter[3];
@@ -1032,11 +1034,24 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
     sums2[1] = s1;
     const int c = counter[0] + 1;
     counter[0] = c;
-    counter[1] += 1;
+    const int k = counter[1] + 1;   // this cycle's index since creation
+    counter[1] = k;
     const double rel = s1 > 0.0 ? sqrt(s0 / s1) : 0.0;
     rel_out[0] = rel;
+    // the previous cycle of this step was tested too: its residual and this one give the reduction per cycle
+    if (c >= 2 && sums2[22] == (double)(k - 1) && sums2[21] > 0.0) sums2[20] = rel / sums2[21];
+    sums2[21] = rel;
+    sums2[22] = (double)k;
     const bool more = rel > tol && c < max_cycles;
-    if (!more) counter[3] = min(max(1, c - 1), max_cycles - 1);
+    if (!more) {
+      // The next step tests first at this step's count c, or at c - 1 when one cycle fewer would probably
+      // have reached the tolerance here (rel / reduction <= tol) or the reduction is not known yet (testing at
+      // c - 1 and c measures it).  A step that needs fewer cycles than predicted runs one more than it needs,
+      // and its smaller final residual moves the next prediction down.
+      const double rho = sums2[20];
+      const bool fewer = !(rho > 0.0 && rho < 1.0) || rel <= tol * rho;
+      counter[3] = min(max(1, fewer ? c - 1 : c), max_cycles - 1);
+    }
     cudaGraphSetConditional(h, more ? 1u : 0u);
   }
 }

@@ -46,7 +46,8 @@ struct FireSim {
   float* dLogs = nullptr;
   double* dPartials = nullptr;
   int partialsCount = 0;
-  double* dSmall = nullptr;     // [0..1] residual sums, [2..17] stats, [18] hrr, [19] rel residual
+  double* dSmall = nullptr;     // [0..1] residual sums, [2..17] stats, [18] hrr, [19] rel residual, [20..22] the
+                                // residual loop's predictor (reduction per cycle, last tested residual and cycle)
   int* dCounter = nullptr;      // [0] V-cycles of this step's residual-driven loop, [1] cycles since creation,
                                 // [2] device wait timeout flag, [3] first cycle the next step tests
 
