@@ -51,7 +51,6 @@ const float kParamDefaults[P_STRIDE] = {
 cudaError_t kernels_probe();
 void launch_residual_decide(const MGLevel& L, double* partials, double* sums2, double tol, int max_cycles, int* counter,
                             double* rel_out, cudaGraphConditionalHandle h, cudaStream_t st);
-void launch_mg_counter_reset(int* counter, cudaStream_t st);
 
 }  // namespace fire
 
@@ -225,7 +224,7 @@ int record_mg(FireSim* sim, cudaStream_t st) {
   size_t ndeps;
   CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
   if (cs != cudaStreamCaptureStatusActive) return set_err(sim, FIRE_ERR_STATE, "residual-driven solve needs graph capture");
-  launch_mg_counter_reset(sim->dCounter, st);
+  // the per-step cycle count was cleared by the divergence kernel recorded just before (record_step)
   CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
   cudaGraphConditionalHandle h;
   CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
@@ -274,7 +273,7 @@ int record_step(FireSim* sim, cudaStream_t st, bool prof) {
     sim->forcesNode = deps[0];
   }
   if ((rc = record_ev(sim, 4, st, prof))) return rc;
-  launch_div(P, sim->f, sim->levels[0].b, d, st);
+  launch_div(P, sim->f, sim->levels[0].b, d, st, sim->mg_max_cycles > 0 ? sim->dCounter : nullptr);
   if ((rc = record_ev(sim, 5, st, prof))) return rc;
   if ((rc = record_mg(sim, st))) return rc;
   if ((rc = record_ev(sim, 6, st, prof))) return rc;

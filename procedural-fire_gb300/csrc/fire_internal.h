@@ -124,7 +124,7 @@ void launch_forces_unfused(const float* P, Fields f, const uint2* noise, const u
 void launch_forces_recompute(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st);
 // Opts the shared-memory kernels of fire_step.cu into their dynamic shared memory on the current device.
 cudaError_t step_configure();
-void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st);
+void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st, int* mg_counter = nullptr);
 void launch_project(const float* P, Fields f, const float* p0, Dims d, cudaStream_t st);
 // Tile candidates of the batched stages: CELL_TILES cell tiles for adv1, adv2, div and project (0 is the
 // per-simulation kernels' 32x4x2; then 32x8x1, 32x2x4, 64x4x1) and FORCES_TILES z-march depths of the forces

@@ -1260,9 +1260,3 @@ void launch_residual_decide(const MGLevel& L, double* partials, double* sums2, d
 
 }  // namespace fire
 
-// ---------------- residual-driven loop control (conditional WHILE node body tail) ----------------
-namespace fire {
-// The loop test itself is k_residual_decide (above); this resets the per-step cycle counter before the loop.
-__global__ void k_mg_counter_reset(int* counter) { if (threadIdx.x == 0) counter[0] = 0; }
-void launch_mg_counter_reset(int* counter, cudaStream_t st) { k_mg_counter_reset<<<1, 32, 0, st>>>(counter); }
-}  // namespace fire

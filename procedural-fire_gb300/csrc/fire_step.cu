@@ -594,8 +594,12 @@ __global__ void __launch_bounds__(FT_X * FT_Y, FIRE_FORCES_MIN_CTAS) k_forces_ti
   extern __shared__ float4 fsm[];
   forces_persistent(ParamsByValue{pb}, f, noiseT, curlT, d, fsm);
 }
-__global__ void __launch_bounds__(256) k_div(const float* __restrict__ P, const float4* __restrict__ velX, float* __restrict__ b0, Dims d) {
+// mg_counter (the residual-driven step graph only, else null): the solve that follows counts its V-cycles
+// from zero, so this kernel clears the count instead of a separate launch.
+__global__ void __launch_bounds__(256) k_div(const float* __restrict__ P, const float4* __restrict__ velX, float* __restrict__ b0, Dims d,
+                                             int* __restrict__ mg_counter) {
   div_body(P, velX, b0, d, blockIdx);
+  if (mg_counter && (blockIdx.x | blockIdx.y | blockIdx.z | threadIdx.x | threadIdx.y | threadIdx.z) == 0) *mg_counter = 0;
 }
 __global__ void __launch_bounds__(256) k_project(const float* __restrict__ P, const float4* __restrict__ velX, const float* __restrict__ p0,
                                                  const unsigned char* __restrict__ solid, float4* __restrict__ vel, Dims d) {
@@ -752,8 +756,8 @@ void launch_project_batch(const BatchMap& m, const StepBatch& I, int tile, cudaS
 void launch_forces_unfused(const float* P, Fields f, const uint2* noise, const uint2* curl, Dims d, cudaStream_t st) {
   launch_pdl(k_forces<false>, grid_for(d), block_shape(), 0, st, P, f, noise, curl, d);
 }
-void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st) {
-  launch_pdl(k_div, grid_for(d), block_shape(), 0, st, P, (const float4*)f.velX, b0, d);
+void launch_div(const float* P, Fields f, float* b0, Dims d, cudaStream_t st, int* mg_counter) {
+  launch_pdl(k_div, grid_for(d), block_shape(), 0, st, P, (const float4*)f.velX, b0, d, mg_counter);
 }
 void launch_project(const float* P, Fields f, const float* p0, Dims d, cudaStream_t st) {
   launch_pdl(k_project, grid_for(d), block_shape(), 0, st, P, (const float4*)f.velX, p0, (const unsigned char*)f.solid, f.vel, d);
