@@ -49,6 +49,7 @@ const float kParamDefaults[P_STRIDE] = {
 
 // ---- kernels defined in other translation units that the runtime launches directly ----
 cudaError_t kernels_probe();
+void launch_mg_counter_reset(int* counter, cudaStream_t st);
 void launch_residual_decide(const MGLevel& L, double* partials, double* sums2, double tol, int max_cycles, int* counter,
                             double* rel_out, cudaGraphConditionalHandle h, cudaStream_t st);
 
@@ -212,8 +213,10 @@ int record_ev(FireSim* sim, int idx, cudaStream_t st, bool prof) {
 }
 
 // Records the multigrid solve: a fixed number of cycles, or (residual-driven mode) a conditional
-// WHILE loop whose body is one cycle plus the FP64 residual norm and the device-side decision.
-int record_mg(FireSim* sim, cudaStream_t st) {
+// WHILE loop whose body is one cycle plus the FP64 residual norm and the device-side decision.  The loop
+// counts its cycles from zero: counter_cleared says a divergence kernel recorded just before has cleared the
+// count (launch_div with the counter), else a clearing kernel is recorded here.
+int record_mg(FireSim* sim, cudaStream_t st, bool counter_cleared) {
   if (sim->mg_max_cycles <= 0) {
     for (int c = 0; c < sim->vcycles; ++c) record_vcycle(sim, st);
     return FIRE_OK;
@@ -224,7 +227,7 @@ int record_mg(FireSim* sim, cudaStream_t st) {
   size_t ndeps;
   CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
   if (cs != cudaStreamCaptureStatusActive) return set_err(sim, FIRE_ERR_STATE, "residual-driven solve needs graph capture");
-  // the per-step cycle count was cleared by the divergence kernel recorded just before (record_step)
+  if (!counter_cleared) launch_mg_counter_reset(sim->dCounter, st);
   CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
   cudaGraphConditionalHandle h;
   CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
@@ -275,7 +278,7 @@ int record_step(FireSim* sim, cudaStream_t st, bool prof) {
   if ((rc = record_ev(sim, 4, st, prof))) return rc;
   launch_div(P, sim->f, sim->levels[0].b, d, st, sim->mg_max_cycles > 0 ? sim->dCounter : nullptr);
   if ((rc = record_ev(sim, 5, st, prof))) return rc;
-  if ((rc = record_mg(sim, st))) return rc;
+  if ((rc = record_mg(sim, st, sim->mg_max_cycles > 0))) return rc;
   if ((rc = record_ev(sim, 6, st, prof))) return rc;
   launch_project(P, sim->f, sim->levels[0].p, d, st);
   if ((rc = record_ev(sim, 7, st, prof))) return rc;
@@ -698,7 +701,6 @@ struct SaveHeader {
   int32_t counters[4];   // the residual loop's counters (cumulative cycles, first cycle the next step tests)
   int32_t lastCycles;
   double lastRel;
-  double predictor[3];   // the residual loop's predictor state (reduction per cycle, last tested residual, its cycle)
 };
 const char kSaveMagic[8] = {'F', 'I', 'R', 'E', 'S', 'I', 'M', '1'};
 size_t save_bytes(const FireSim* s) {
@@ -719,7 +721,7 @@ int fire_sim_save(FireSim* sim, void* buf, size_t capacity, size_t* bytes_out) {
   SaveHeader h;
   std::memset(&h, 0, sizeof h);
   std::memcpy(h.magic, kSaveMagic, sizeof h.magic);
-  h.version = 2;
+  h.version = 1;
   h.header_bytes = (uint32_t)sizeof h;
   for (int i = 0; i < 3; ++i) { h.res[i] = sim->res[i]; h.size[i] = sim->size[i]; }
   h.time = sim->time;
@@ -737,7 +739,6 @@ int fire_sim_save(FireSim* sim, void* buf, size_t capacity, size_t* bytes_out) {
   h.counters[2] = 0;   // per-step cycle count and wait-timeout flag are not state
   h.lastCycles = sim->lastCycles;
   h.lastRel = sim->lastRel;
-  CK(cudaMemcpy(h.predictor, sim->dSmall + 20, sizeof h.predictor, cudaMemcpyDeviceToHost));
   char* o = static_cast<char*>(buf);
   std::memcpy(o, &h, sizeof h);
   o += sizeof h;
@@ -756,7 +757,7 @@ int fire_sim_load(FireSim* sim, const void* buf, size_t bytes) {
   if (bytes != save_bytes(sim)) return set_err(sim, FIRE_ERR_BAD_ARG, "load: %zu bytes, this simulation's state is %zu", bytes, save_bytes(sim));
   SaveHeader h;
   std::memcpy(&h, buf, sizeof h);
-  if (std::memcmp(h.magic, kSaveMagic, sizeof h.magic) != 0 || h.version != 2 || h.header_bytes != sizeof h)
+  if (std::memcmp(h.magic, kSaveMagic, sizeof h.magic) != 0 || h.version != 1 || h.header_bytes != sizeof h)
     return set_err(sim, FIRE_ERR_BAD_ARG, "load: not a saved simulation state of this version");
   for (int i = 0; i < 3; ++i)
     if (h.res[i] != sim->res[i] || h.size[i] != sim->size[i]) return set_err(sim, FIRE_ERR_BAD_ARG, "load: saved for another grid");
@@ -771,7 +772,6 @@ int fire_sim_load(FireSim* sim, const void* buf, size_t bytes) {
   }
   CK(cudaMemcpy(sim->levels[0].p, in, cells * sizeof(float), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(sim->dCounter, h.counters, sizeof h.counters, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(sim->dSmall + 20, h.predictor, sizeof h.predictor, cudaMemcpyHostToDevice));
   sim->time = h.time;
   sim->frame = h.frame;
   sim->stepsRun = h.stepsRun;

@@ -935,6 +935,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 // thread accumulate in double-float (df64, fire_device.cuh) in a fixed order, so the result is
 // deterministic and carries ~48 bits without FP64 instructions.  Partials: float4 (rr.hi, rr.lo, bb.hi, bb.lo).
 constexpr int RZ = 8;
+// Residual reduction per V-cycle assumed by the residual-driven loop's prediction of the first cycle it tests.
+constexpr double MG_PREDICT_RHO = 0.3;
 // Sums of r^2 and b^2 over planes z0 .. z0+RZ-1 of column (x, y), r = b - A p with the ghost rules of
 // pghost.  The column is marched in z with the z neighbours carried in registers; the x/y face tests are
 // per column, so a cell costs 6 loads and a handful of selects.
@@ -1012,9 +1014,7 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
   pdl_trigger();
   // Cycles before counter[3] run without a convergence test (each skipped test saves the norm's pass over
   // level 0 and the sum); the solve still stops only on a tested residual <= tol (or at max_cycles).
-  // counter[3] is set when a step stops (below) from the cycle count it needed and the per-cycle reduction
-  // of the residual; sums2[20..22] hold that reduction (0: not measured yet), the residual of the most recent
-  // tested cycle and that cycle's index in counter[1].
+  // counter[3] is set when a step stops (below) from the cycle count it needed and its final residual.
   if (threadIdx.x == 0) {
     const int c = counter[0] + 1;
     skip = c < counter[3];
@@ -1034,24 +1034,15 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
     sums2[1] = s1;
     const int c = counter[0] + 1;
     counter[0] = c;
-    const int k = counter[1] + 1;   // this cycle's index since creation
-    counter[1] = k;
+    counter[1] += 1;
     const double rel = s1 > 0.0 ? sqrt(s0 / s1) : 0.0;
     rel_out[0] = rel;
-    // the previous cycle of this step was tested too: its residual and this one give the reduction per cycle
-    if (c >= 2 && sums2[22] == (double)(k - 1) && sums2[21] > 0.0) sums2[20] = rel / sums2[21];
-    sums2[21] = rel;
-    sums2[22] = (double)k;
     const bool more = rel > tol && c < max_cycles;
-    if (!more) {
-      // The next step tests first at this step's count c, or at c - 1 when one cycle fewer would probably
-      // have reached the tolerance here (rel / reduction <= tol) or the reduction is not known yet (testing at
-      // c - 1 and c measures it).  A step that needs fewer cycles than predicted runs one more than it needs,
-      // and its smaller final residual moves the next prediction down.
-      const double rho = sums2[20];
-      const bool fewer = !(rho > 0.0 && rho < 1.0) || rel <= tol * rho;
-      counter[3] = min(max(1, fewer ? c - 1 : c), max_cycles - 1);
-    }
+    // The next step tests first at this step's count c, or at c - 1 when one cycle fewer could have reached
+    // the tolerance: when rel <= MG_PREDICT_RHO * tol, with MG_PREDICT_RHO above the residual reduction of one
+    // cycle (about 0.1 for the over-relaxed V(2,2)).  A step that needs fewer cycles than predicted runs one
+    // more than it needs, and its smaller final residual moves the next prediction down.
+    if (!more) counter[3] = min(max(1, rel <= MG_PREDICT_RHO * tol ? c - 1 : c), max_cycles - 1);
     cudaGraphSetConditional(h, more ? 1u : 0u);
   }
 }
@@ -1257,6 +1248,9 @@ void launch_residual_decide(const MGLevel& L, double* partials, double* sums2, d
   launch_pdl(k_sum_decide, dim3(1), dim3(RB), 0, st, (const float4*)part4, residual_partials_count(L), sums2, tol, max_cycles,
              counter, rel_out, h);
 }
+// Clears the per-step cycle count before a residual-driven solve that no clearing divergence kernel precedes.
+__global__ void k_mg_counter_reset(int* counter) { if (threadIdx.x == 0) counter[0] = 0; }
+void launch_mg_counter_reset(int* counter, cudaStream_t st) { k_mg_counter_reset<<<1, 32, 0, st>>>(counter); }
 
 }  // namespace fire
 

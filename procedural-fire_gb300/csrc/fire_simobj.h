@@ -46,8 +46,7 @@ struct FireSim {
   float* dLogs = nullptr;
   double* dPartials = nullptr;
   int partialsCount = 0;
-  double* dSmall = nullptr;     // [0..1] residual sums, [2..17] stats, [18] hrr, [19] rel residual, [20..22] the
-                                // residual loop's predictor (reduction per cycle, last tested residual and cycle)
+  double* dSmall = nullptr;     // [0..1] residual sums, [2..17] stats, [18] hrr, [19] rel residual
   int* dCounter = nullptr;      // [0] V-cycles of this step's residual-driven loop, [1] cycles since creation,
                                 // [2] device wait timeout flag, [3] first cycle the next step tests
 
@@ -94,7 +93,7 @@ void fill_block(FireSim* s, float dt, float* out);
 void advance_events(FireSim* s, float dt);
 // Records the pressure solve of one step on `st` (fixed V-cycles, or the residual-driven loop, which needs
 // stream capture).
-int record_mg(FireSim* sim, cudaStream_t st);
+int record_mg(FireSim* sim, cudaStream_t st, bool counter_cleared = false);
 // Rebuilds the emitter geometry when stale (src/sim.js:632).
 int ensure_geo(FireSim* sim, cudaStream_t st);
 // Stages the block for dt (and the log buffer) in the pinned ring and copies it to the device on `st`;

@@ -272,8 +272,12 @@ SIZE = (0.3, 0.6, 0.3)
 VCYC = 10   # near-exact solves: the adjoint treats the pressure solve as A^-1
 
 
-def _burning_sim(F, spots, preroll=30):
-    sim = F.FireSim(res=RES, size=SIZE, vcycles=VCYC)
+def _burning_sim(F, spots, preroll=30, residual_driven=False):
+    if residual_driven:   # the source-fit workload's solve: over-relaxed V(2,2) to 1e-5, at most 8 cycles
+        sim = F.FireSim(res=RES, size=SIZE, vcycles=VCYC, mg_max_cycles=8, mg_tol=1e-5)
+        sim.set_mg_omega(1.2)
+    else:
+        sim = F.FireSim(res=RES, size=SIZE, vcycles=VCYC)
     sim.set_params({"vortEps": 0.3, "turbAmp": 0.2})
     sim.set_soot_age(0.02, 0.06)
     sim.set_bed_gain(0.0)
@@ -284,10 +288,15 @@ def _burning_sim(F, spots, preroll=30):
 
 
 @pytest.mark.gpu
-def test_tape_forward_matches_step_and_backward_restores():
+@pytest.mark.parametrize("residual_driven", [False, True])
+def test_tape_forward_matches_step_and_backward_restores(residual_driven):
+    """The taped forward is the step bit for bit, with fixed cycles and with the residual-driven solve (same
+    cycle counts: every solve of the tape counts its cycles from zero and tests as the step's graph does), and
+    stepping on after a backward gives the same bits as a simulation that never ran one."""
     import fire_sim as F
     spots = F.make_spots(9, 4, 1.0, 4.0, 0.02, 0.08)
-    a, b = _burning_sim(F, spots), _burning_sim(F, spots)
+    a, b = _burning_sim(F, spots, residual_driven=residual_driven), _burning_sim(F, spots, residual_driven=residual_driven)
+    c0 = a.info().total_cycles
     adj = F.Adjoint(a, 7, 3)
     adj.forward(DT)
     b.step(DT, 7)
@@ -296,6 +305,9 @@ def test_tape_forward_matches_step_and_backward_restores():
         assert np.array_equal(a.download(name), b.download(name)), name
     assert np.array_equal(a.level(0, "p"), b.level(0, "p"))
     assert a.info().time == b.info().time and a.info().frame == b.info().frame
+    if residual_driven:
+        ca, cb = a.info().total_cycles - c0, b.info().total_cycles - c0
+        assert ca == cb and ca >= 7, (ca, cb)
     adj.seed(S=np.ones(RES[::-1] + (4,), np.float32))
     adj.backward()
     a.sync()
