@@ -240,6 +240,14 @@ int fire_sim_hrr(FireSim* sim, double* q_kw, void* stream);
  * out[0..15] = S stats as in fire_sim_stats, out[16] = heat release (kW).  The values are valid once
  * `stream` has reached this point (fire_sim_sync or a stream/event wait).                          */
 int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream);
+/* Per-step diagnostics (enable = 1): every fire_sim_step forms the values of fire_sim_stats_async (same
+ * kernels, same bits) on a graph branch that runs beside the divergence, pressure solve and projection,
+ * and fire_sim_stats_async after a step only queues their copy to the host.  A call that changes S
+ * through the API (upload, load, reset, stage runs, the adjoint, an ensemble step) makes the next
+ * fire_sim_stats_async compute them again; writes through fire_sim_field's pointer are not seen, so call
+ * this with 0 before writing S that way.  The change takes effect at the next step (the step graph is
+ * rebuilt; this call synchronises the device).  Off by default.                                        */
+int fire_sim_set_step_stats(FireSim* sim, int enable);
 /* FIRE.profile's height profile (src/main.js:322-340): for rows j = 0, 4, 8, ... of y, over the x-z plane
  * of S, with T = 293 + 1000 S.x: h = (j + 0.5) dx, the mean T of the centreline cells (|i - nx/2| < 3 and
  * |k - nz/2| < 3), the maximum T (from 0), the maximum soot S.z and fuel S.y (from 0) and the count of

@@ -1079,6 +1079,7 @@ int fire_adjoint_forward(FireAdjoint* A, float dt, void* stream) {
   FIRE_RANGE("fire_adjoint_forward");
   if (!A || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
   FireSim* sim = A->sim;
+  sim->stepStatsValid = false;   // the tape writes the simulation's fields
   ACK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
   int rc;
@@ -1155,6 +1156,7 @@ int fire_adjoint_backward(FireAdjoint* A, void* stream) {
   FIRE_RANGE("fire_adjoint_backward");
   if (!A) return FIRE_ERR_BAD_ARG;
   FireSim* sim = A->sim;
+  sim->stepStatsValid = false;   // the tape writes the simulation's fields
   if (!A->forwardDone) return set_err(sim, FIRE_ERR_STATE, "fire_adjoint_backward before fire_adjoint_forward");
   ACK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
@@ -1211,6 +1213,7 @@ int fire_adjoint_stage(FireAdjoint* A, int stage, float dt, int arg, void* strea
   FIRE_RANGE("fire_adjoint_stage");
   if (!A || !(dt > 0.0f)) return FIRE_ERR_BAD_ARG;
   FireSim* sim = A->sim;
+  sim->stepStatsValid = false;   // stage runs may write the simulation's fields
   ACK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
   int rc = upload_block(sim, dt, st, false);

@@ -276,12 +276,22 @@ int record_step(FireSim* sim, cudaStream_t st, bool prof) {
     sim->forcesNode = deps[0];
   }
   if ((rc = record_ev(sim, 4, st, prof))) return rc;
+  if (sim->stepStats) {
+    // S is final after the forces stage (projection only changes vel): its diagnostics run on a branch that
+    // overlaps the divergence, the pressure solve and the projection, and joins at the end of the step
+    CK(cudaEventRecord(sim->forkEv, st));
+    CK(cudaStreamWaitEvent(sim->sideStream, sim->forkEv, 0));
+    launch_diag(sim->f.S, d, (float)sim->dx, sim->dDiagPartials, sim->dSmall + 24, sim->sideStream);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(sim->joinEv, sim->sideStream));
+  }
   launch_div(P, sim->f, sim->levels[0].b, d, st, sim->mg_max_cycles > 0 ? sim->dCounter : nullptr);
   if ((rc = record_ev(sim, 5, st, prof))) return rc;
   if ((rc = record_mg(sim, st, sim->mg_max_cycles > 0))) return rc;
   if ((rc = record_ev(sim, 6, st, prof))) return rc;
   launch_project(P, sim->f, sim->levels[0].p, d, st);
   if ((rc = record_ev(sim, 7, st, prof))) return rc;
+  if (sim->stepStats) CK(cudaStreamWaitEvent(st, sim->joinEv, 0));
   CK(cudaGetLastError());
   return FIRE_OK;
 }
@@ -433,7 +443,8 @@ int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSi
   size_t logsOff = off; off = align_up(off + sizeof(float) * MAX_LOGS * 8);
   sim->partialsCount = std::max(stats_partials_count(sim->d), residual_partials_count(sim->levels[0]));
   size_t partOff = off; off = align_up(off + sizeof(double) * 16 * (size_t)sim->partialsCount);
-  size_t smallOff = off; off = align_up(off + sizeof(double) * 32);
+  size_t diagPartOff = off; off = align_up(off + sizeof(double) * 16 * (size_t)stats_partials_count(sim->d));
+  size_t smallOff = off; off = align_up(off + sizeof(double) * 48);
   size_t cntOff = off; off = align_up(off + sizeof(int) * 4);
   sim->arenaBytes = off;
   cudaError_t e = cudaMalloc(&sim->arena, off);
@@ -453,6 +464,7 @@ int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSi
   sim->dLogs = (float*)(A + logsOff);
   sim->dPartials = (double*)(A + partOff);
   sim->dSmall = (double*)(A + smallOff);
+  sim->dDiagPartials = (double*)(A + diagPartOff);
   sim->dCounter = (int*)(A + cntOff);
 
   auto fail = [&](int code) { fire_sim_destroy(sim); return code; };
@@ -467,6 +479,10 @@ int fire_sim_create(const FireConfig* cfg, const float* logs, int n_logs, FireSi
     if (cudaEventCreate(&sim->stageEv[k]) != cudaSuccess) return fail(FIRE_ERR_CUDA);
   if (cudaEventCreateWithFlags(&sim->doneEv, cudaEventDisableTiming) != cudaSuccess) return fail(FIRE_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&sim->capStream, cudaStreamNonBlocking) != cudaSuccess) return fail(FIRE_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&sim->sideStream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&sim->forkEv, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&sim->joinEv, cudaEventDisableTiming) != cudaSuccess)
+    return fail(FIRE_ERR_CUDA);
   if (mg_configure(TAIL_SMEM_BUDGET) != cudaSuccess) return fail(set_err(sim, FIRE_ERR_CUDA, "tail kernel smem opt-in failed"));
   if (step_configure() != cudaSuccess) return fail(set_err(sim, FIRE_ERR_CUDA, "forces kernel smem opt-in failed"));
 
@@ -492,6 +508,9 @@ int fire_sim_destroy(FireSim* sim) {
   for (int k = 0; k <= FIRE_STAGE_COUNT; ++k) if (sim->stageEv[k]) cudaEventDestroy(sim->stageEv[k]);
   if (sim->doneEv) cudaEventDestroy(sim->doneEv);
   if (sim->capStream) cudaStreamDestroy(sim->capStream);
+  if (sim->sideStream) cudaStreamDestroy(sim->sideStream);
+  if (sim->forkEv) cudaEventDestroy(sim->forkEv);
+  if (sim->joinEv) cudaEventDestroy(sim->joinEv);
   if (sim->hRing) cudaFreeHost(sim->hRing);
   if (sim->hSmall) cudaFreeHost(sim->hSmall);
   if (sim->hCounter) cudaFreeHost(sim->hCounter);
@@ -520,6 +539,7 @@ int fire_sim_step(FireSim* sim, float dt, int n_steps, void* stream) {
     std::memcpy(pb.v, staged, sizeof pb.v);
     CK(forces_pb_set(sim->exec, sim->forcesNode, pb, sim->f, sim->noise, sim->curl, sim->d));
     CK(cudaGraphLaunch(sim->exec, st));
+    sim->stepStatsValid = sim->stepStats;
     sim->time += dt;                                                          // src/sim.js:646-647
     sim->frame += 1;
     sim->stepsRun += 1;
@@ -667,6 +687,7 @@ int fire_sim_gust(FireSim* sim, float strength, float duration) {
 
 int fire_sim_reset(FireSim* sim) {
   if (!sim) return FIRE_ERR_BAD_ARG;
+  sim->stepStatsValid = false;
   CK(cudaSetDevice(sim->device));
   CK(cudaDeviceSynchronize());
   const size_t cells = (size_t)sim->res[0] * sim->res[1] * sim->res[2];
@@ -757,6 +778,7 @@ int fire_sim_load(FireSim* sim, const void* buf, size_t bytes) {
   if (bytes != save_bytes(sim)) return set_err(sim, FIRE_ERR_BAD_ARG, "load: %zu bytes, this simulation's state is %zu", bytes, save_bytes(sim));
   SaveHeader h;
   std::memcpy(&h, buf, sizeof h);
+  sim->stepStatsValid = false;
   if (std::memcmp(h.magic, kSaveMagic, sizeof h.magic) != 0 || h.version != 1 || h.header_bytes != sizeof h)
     return set_err(sim, FIRE_ERR_BAD_ARG, "load: not a saved simulation state of this version");
   for (int i = 0; i < 3; ++i)
@@ -838,6 +860,7 @@ int fire_sim_upload(FireSim* sim, int which, const void* host, size_t bytes) {
   int rc = fire_sim_field(sim, which, &d);
   if (rc) return rc;
   if (!host || bytes != d.bytes) return set_err(sim, FIRE_ERR_BAD_ARG, "upload: need %zu bytes, got %zu", d.bytes, bytes);
+  sim->stepStatsValid = false;
   CK(cudaSetDevice(sim->device));
   CK(cudaDeviceSynchronize());
   CK(cudaMemcpy(d.data, host, bytes, cudaMemcpyHostToDevice));
@@ -885,6 +908,7 @@ const char* fire_sim_last_error(FireSim* sim) { return sim ? sim->err.c_str() : 
 int fire_sim_run_stage(FireSim* sim, int stage, float dt, void* stream) {
   FIRE_RANGE("fire_sim_run_stage");
   if (!sim || stage < 0 || stage >= FIRE_STAGE_COUNT) return FIRE_ERR_BAD_ARG;
+  sim->stepStatsValid = false;
   CK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
   int rc = upload_block(sim, dt, st, stage == FIRE_STAGE_GEO);
@@ -1041,9 +1065,25 @@ int fire_sim_stats_async(FireSim* sim, double* pinned_out17, void* stream) {
   if (!sim || !pinned_out17) return FIRE_ERR_BAD_ARG;
   CK(cudaSetDevice(sim->device));
   cudaStream_t st = as_stream(stream);
+  if (sim->stepStats && sim->stepStatsValid) {   // the last step's graph formed them (same kernels)
+    CK(cudaMemcpyAsync(pinned_out17, sim->dSmall + 24, 17 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    return FIRE_OK;
+  }
   launch_diag(sim->f.S, sim->d, (float)sim->dx, sim->dPartials, sim->dSmall + 2, st);   // dSmall[2..18]
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(pinned_out17, sim->dSmall + 2, 17 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  return FIRE_OK;
+}
+
+int fire_sim_set_step_stats(FireSim* sim, int enable) {
+  if (!sim || (enable != 0 && enable != 1)) return FIRE_ERR_BAD_ARG;
+  if (sim->stepStats != (enable == 1)) {
+    CK(cudaSetDevice(sim->device));
+    CK(cudaDeviceSynchronize());   // no replay of the current graph is in flight when it is replaced
+    drop_graph(sim);
+  }
+  sim->stepStats = enable == 1;
+  sim->stepStatsValid = false;
   return FIRE_OK;
 }
 
@@ -1317,6 +1357,7 @@ int fire_ensemble_step(FireEnsemble* e, float dt, int n_steps, void* stream) {
   if (cudaSetDevice(e->device) != cudaSuccess) return FIRE_ERR_CUDA;
   cudaStream_t st = as_stream(stream);
   const int n = (int)e->sims.size();
+  for (FireSim* s : e->sims) s->stepStatsValid = false;   // members are stepped by the ensemble's graph
   for (int step = 0; step < n_steps; ++step) {
     const int k = e->ringPos;
     e->ringPos = (k + 1) % ENS_RING;

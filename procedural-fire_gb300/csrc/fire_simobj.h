@@ -46,7 +46,9 @@ struct FireSim {
   float* dLogs = nullptr;
   double* dPartials = nullptr;
   int partialsCount = 0;
-  double* dSmall = nullptr;     // [0..1] residual sums, [2..17] stats, [18] hrr, [19] rel residual
+  double* dSmall = nullptr;     // [0..1] residual sums, [2..17] stats, [18] hrr, [19] rel residual,
+                                // [24..40] the step graph's diagnostics (per-step diagnostics mode)
+  double* dDiagPartials = nullptr;   // scratch of the step graph's diagnostics branch (it runs beside the solve)
   int* dCounter = nullptr;      // [0] V-cycles of this step's residual-driven loop, [1] cycles since creation,
                                 // [2] device wait timeout flag, [3] first cycle the next step tests
 
@@ -59,6 +61,11 @@ struct FireSim {
   int* hCounter = nullptr;
 
   cudaStream_t capStream = nullptr;
+  // per-step diagnostics: the step graph forms fire_sim_stats_async's values on a branch beside the solve
+  bool stepStats = false;
+  bool stepStatsValid = false;   // dSmall[24..40] hold the diagnostics of the current S
+  cudaStream_t sideStream = nullptr;
+  cudaEvent_t forkEv = nullptr, joinEv = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaGraphNode_t forcesNode = nullptr;   // the step graph's forces launch, which takes the block by value

@@ -102,6 +102,7 @@ _SIGS = {
     "fire_sim_stats": (_ip, [_vp, _ip, _vp, _vp]),
     "fire_sim_hrr": (_ip, [_vp, ctypes.POINTER(_dp), _vp]),
     "fire_sim_stats_async": (_ip, [_vp, _vp, _vp]),
+    "fire_sim_set_step_stats": (_ip, [_vp, _ip]),
     "fire_sim_height_profile": (_ip, [_vp, _vp, _ip, ctypes.POINTER(_ip), _vp]),
     "fire_build_campfire": (_ip, [ctypes.c_uint32, _vp, _ip]),
     "fire_make_spots": (_ip, [ctypes.c_uint32, _ip, _fp, _fp, _fp, _fp, _vp]),
@@ -483,6 +484,10 @@ class FireSim:
         q = ctypes.c_double()
         self._check(self._lib.fire_sim_hrr(self._h, ctypes.byref(q), _stream_handle(stream)), "hrr")
         return q.value
+
+    def set_step_stats(self, enable: bool = True):
+        """Per-step diagnostics: each step's graph forms stats_async's values beside the pressure solve."""
+        self._check(self._lib.fire_sim_set_step_stats(self._h, int(bool(enable))), "set_step_stats")
 
     def stats_async(self, out_ptr: int, stream=None):
         """Queues S stats + heat release into a pinned host buffer of 17 doubles (no wait)."""

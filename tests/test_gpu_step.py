@@ -209,6 +209,48 @@ def test_stats_and_hrr_match_numpy(campfire):
     assert got.tolist() == want17
 
 
+def test_step_stats_branch(campfire):
+    """Per-step diagnostics (fire_sim_set_step_stats): the step graph's branch gives fire_sim_stats_async the
+    same bits as the stand-alone pass of a simulation without it, every step, and leaves the step's fields
+    unchanged; after S is changed through the API, stats_async forms the values of the new S."""
+    import torch
+    dt = FC.C1["dt"]
+    a = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=2)
+    b = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=2)
+    a.set_step_stats(True)
+    pa = torch.zeros(17, dtype=torch.float64, pin_memory=True)
+    pb = torch.zeros(17, dtype=torch.float64, pin_memory=True)
+    for _ in range(6):
+        a.step(dt, 1)
+        b.step(dt, 1)
+        a.stats_async(pa.data_ptr())
+        b.stats_async(pb.data_ptr())
+        a.sync()
+        b.sync()
+        assert pa.numpy().tolist() == pb.numpy().tolist()
+    for name in ("vel", "S", "S2"):
+        assert np.array_equal(a.download(name), b.download(name)), name
+    assert float(pa[16]) > 0.0   # the fire is burning
+    S = a.download("S")
+    S[..., 0] *= 0.5
+    a.upload("S", S)
+    a.stats_async(pa.data_ptr())
+    a.sync()
+    st = a.stats("S")
+    want17 = [v for c in st for v in (c["min"], c["max"], c["mean"], float(c["bad"]))] + [a.hrr()]
+    assert pa.numpy().tolist() == want17
+    a.set_step_stats(False)
+    a.step(dt, 1)
+    a.stats_async(pa.data_ptr())
+    a.sync()
+    st = a.stats("S")
+    assert pa.numpy().tolist() == [v for c in st for v in (c["min"], c["max"], c["mean"], float(c["bad"]))] + [a.hrr()]
+    with pytest.raises(F.FireError):
+        a._check(a._lib.fire_sim_set_step_stats(a._h, 2), "step stats 2")
+    a.close()
+    b.close()
+
+
 def test_height_profile_matches_numpy(campfire):
     """FIRE.profile's rows (src/main.js:322-340) restated in numpy on the downloaded S field."""
     sim = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=2)
