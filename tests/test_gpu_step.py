@@ -44,6 +44,45 @@ def test_one_step_from_state(campfire):
     FC.compare(g["p"], o["p"], 1e-3, 1e-4, 5e-3, what="step:p")
 
 
+# Ragged grids (1.25 cm cells): the level hierarchy stops where a dimension turns odd (src/sim.js:79-92), so
+# these exercise coarsest levels smoothed by launches instead of a shared-memory tail (40x70x36 -> 20x35x18,
+# 50x98x50 -> 25x49x25), a whole V-cycle inside the single-CTA tail and partial forces tiles (8x12x8 -> 4x6x4),
+# and a single-level solve on an all-odd grid (33x47x29).
+RAGGED = [
+    (dict(res=(40, 70, 36), size=(0.5, 0.875, 0.45), dt=1.0 / 120.0, vcycles=3), 2),
+    (dict(res=(50, 98, 50), size=(0.625, 1.225, 0.625), dt=1.0 / 120.0, vcycles=3), 2),
+    (dict(res=(8, 12, 8), size=(0.1, 0.15, 0.1), dt=1.0 / 120.0, vcycles=3), 2),
+    (dict(res=(33, 47, 29), size=(0.4125, 0.5875, 0.3625), dt=1.0 / 120.0, vcycles=3), 1),
+]
+
+
+@pytest.mark.parametrize("cfg,levels", RAGGED, ids=lambda v: "x".join(map(str, v["res"])) if isinstance(v, dict) else None)
+def test_one_step_ragged_grids(campfire, cfg, levels):
+    """One step from a mid-burn state on grids whose sizes are not multiples of the tiles, against the FP32
+    oracle at the one-step tolerance; then 5 more steps stay finite and close."""
+    sim, orc = FC.make_pair(cfg, logs=campfire, params={"windX": 0.3})
+    assert len(sim.levels) == levels
+    dt = cfg["dt"]
+    FC.put_state(sim, orc, FC.random_state(cfg["res"], 23))
+    for s in range(6):
+        FC.sync_block(sim, orc, dt)
+        sim.step(dt, 1)
+        orc.step_raw(s == 0, cfg["vcycles"])
+        if s == 0:
+            sim.sync()
+            g, o = _fields(sim, True), _fields(orc, False)
+            for k in ("vel", "S", "S2", "velX"):
+                for c in range(4):
+                    FC.compare(g[k][..., c], o[k][..., c], 1e-3, 1e-4, 5e-3, what=f"ragged step:{k}[{c}]")
+            FC.compare(g["p"], o["p"], 1e-3, 1e-4, 5e-3, what="ragged step:p")
+    sim.sync()
+    g, o = _fields(sim, True), _fields(orc, False)
+    for k in ("vel", "S", "S2"):
+        assert np.isfinite(g[k]).all(), k
+        assert FC.rel_l2(g[k], o[k]) < 5e-3, (k, FC.rel_l2(g[k], o[k]))
+    sim.close()
+
+
 def _run(cfg, logs, spots, nsteps, dbl):
     sim, orc = FC.make_pair(cfg, logs=logs, dbl=dbl, spots=spots, bed_gain=0.0 if spots is not None else None)
     dt = cfg["dt"]
