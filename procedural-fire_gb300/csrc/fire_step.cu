@@ -357,26 +357,43 @@ __global__ void __launch_bounds__(256) k_forces(const float* __restrict__ P, Fie
 // ---- z-marching shared-memory variant of curl + forces ----
 // A CTA of 32 x 8 threads owns a 32 x 8 column tile and marches through a run of planes (FZ planes per CTA
 // in the batched kernel; an equal share of all (column, plane) units in the one-wave kernel).  Shared memory holds a
-// ring of 5 velY planes (tile + 2-cell halo, clamped to the domain like `ld`) and a ring of 3 vorticity
-// planes (tile + 1-cell halo).  Vorticity at a halo position outside the domain is the vorticity of the
-// clamped position, which is what `ld(vortT, c +- e)` returns.  Each velY value is loaded ~2x per cell
-// (halo overhead) instead of the 42 gathers of the per-cell recompute.
+// ring of 5 velY planes (tile + 2-cell halo, clamped to the domain like `ld`) and a ring of 3 planes of the
+// vorticity magnitude |w| (tile + 1-cell halo), which is all the confinement gradient reads; the vorticity
+// vector itself is needed only at the cell, where confinement acts, and is formed there from the velY ring
+// with the same arithmetic.  |w| at a halo position outside the domain is that of the clamped position,
+// which is what `ld(vortT, c +- e)` returns.  Each velY value is loaded ~2x per cell (halo overhead) instead
+// of the 42 gathers of the per-cell recompute.
 constexpr int FT_X = 32, FT_Y = 8, FZ = 16;
 constexpr int VX = FT_X + 4, VY = FT_Y + 4;      // velY plane with 2-cell halo
 constexpr int WX = FT_X + 2, WY = FT_Y + 2;      // vorticity plane with 1-cell halo
 // Ring slots are addressed by logical z (z >= -2): velY plane z lives in slot (z + 10) % 5, vorticity
 // plane z in slot (z + 9) % 3.
 __device__ __forceinline__ float4* vslot(float4* vbuf, int z) { return vbuf + ((z + 10) % 5) * (VX * VY); }
-__device__ __forceinline__ float4* wslot(float4* wbuf, int z) { return wbuf + ((z + 9) % 3) * (WX * WY); }
+__device__ __forceinline__ float* wslot(float* wbuf, int z) { return wbuf + ((z + 9) % 3) * (WX * WY); }
+// The curl of velY at tile position c (a VX*VY offset) from planes K (z-1), P0 (z), F (z+1), given the
+// positions of its x and y neighbours (clamped to the domain by the caller); the arithmetic of curl_at.
+__device__ __forceinline__ f3 curl_tile(const float4* K, const float4* P0, const float4* F, int c, int cxm, int cxp, int cym,
+                                        int cyp) {
+  f3 L = xyz(P0[cxm]), R = xyz(P0[cxp]);
+  f3 B = xyz(P0[cym]), T = xyz(P0[cyp]);
+  f3 Kv = xyz(K[c]), Fv = xyz(F[c]);
+  return mk3((T.z - B.z) - (Fv.y - Kv.y), (Fv.x - Kv.x) - (R.z - L.z), (R.y - L.y) - (T.x - B.x)) * 0.5f;
+}
 struct TileNb {
   const float4 *vm, *v0, *vp;   // velY planes z-1, z, z+1 (VX*VY each)
-  const float4 *wm, *w0, *wp;   // vorticity planes z-1, z, z+1 (WX*WY each)
+  const float *wm, *w0, *wp;    // |w| planes z-1, z, z+1 (WX*WY each)
   int tx, ty;                   // thread position in the tile
   __device__ float4 vel_center() const { return v0[(ty + 2) * VX + tx + 2]; }
-  __device__ float4 vort_center() const { return w0[(ty + 1) * WX + tx + 1]; }
+  // The cell is inside the domain and the ring's halo holds clamped positions, so its four in-plane
+  // neighbours in the ring are the clamped neighbours; vm / vp are the clamped planes z -+ 1.
+  __device__ float4 vort_center() const {
+    const int c = (ty + 2) * VX + tx + 2;
+    const f3 w = curl_tile(vm, v0, vp, c, c - 1, c + 1, c - VX, c + VX);
+    return make_float4(w.x, w.y, w.z, 0.0f);
+  }
   __device__ f3 grad_w() const {
     const int c = (ty + 1) * WX + tx + 1;
-    return mk3(w0[c + 1].w - w0[c - 1].w, w0[c + WX].w - w0[c - WX].w, wp[c].w - wm[c].w);
+    return mk3(w0[c + 1] - w0[c - 1], w0[c + WX] - w0[c - WX], wp[c] - wm[c]);
   }
   __device__ f3 lap_v() const {   // src/sim.js:340-343, same summation order
     const int c = (ty + 2) * VX + tx + 2;
@@ -437,9 +454,9 @@ __device__ __forceinline__ void load_vplane(float4* dst, const float4* __restric
   for (int k = 0; k < 2; ++k)
     if (m.vsrc[k] >= 0) cp_async16(dst + tid + k * FT_N, velY + (zo + (unsigned)m.vsrc[k]));
 }
-// Vorticity of logical plane zlog into `dst` (positions clamped to the domain), from the velY ring.  The
-// planes it reads (clamp(zlog) and its clamped z neighbours) are resident in the ring when this is called.
-__device__ __forceinline__ void curl_plane(float4* dst, float4* vbuf, const MarchPlan& m, int zlog, Dims d) {
+// |w| of logical plane zlog into `dst` (positions clamped to the domain), from the velY ring.  The planes it
+// reads (clamp(zlog) and its clamped z neighbours) are resident in the ring when this is called.
+__device__ __forceinline__ void curl_plane(float* dst, float4* vbuf, const MarchPlan& m, int zlog, Dims d) {
   const int zc = clampi(zlog, d.nz);
   const float4* PK = vslot(vbuf, clampi(zc - 1, d.nz));
   const float4* P0 = vslot(vbuf, zc);
@@ -450,11 +467,9 @@ __device__ __forceinline__ void curl_plane(float4* dst, float4* vbuf, const Marc
     const int tap = m.wtap[k];
     if (tap < 0) continue;
     const int c = tap & 1023;
-    f3 L = xyz(P0[c - ((tap >> 10) & 1)]), R = xyz(P0[c + ((tap >> 11) & 1)]);
-    f3 B = xyz(P0[c - ((tap >> 12) & 1) * VX]), T = xyz(P0[c + ((tap >> 13) & 1) * VX]);
-    f3 K = xyz(PK[c]), F = xyz(PF[c]);
-    f3 w = mk3((T.z - B.z) - (F.y - K.y), (F.x - K.x) - (R.z - L.z), (R.y - L.y) - (T.x - B.x)) * 0.5f;
-    dst[tid + k * FT_N] = make_float4(w.x, w.y, w.z, len3(w));
+    const f3 w = curl_tile(PK, P0, PF, c, c - ((tap >> 10) & 1), c + ((tap >> 11) & 1), c - ((tap >> 12) & 1) * VX,
+                           c + ((tap >> 13) & 1) * VX);
+    dst[tid + k * FT_N] = len3(w);
   }
 }
 // Marches the column tile at (x0, y0) through planes [z0, z1), z1 > z0.  The copy of the next velY plane is
@@ -465,8 +480,8 @@ template <class PA>
 __device__ __forceinline__ void forces_march(const PA& pa, const Fields& f, const uint2* __restrict__ noiseT,
                                              const uint2* __restrict__ curlT, Dims d, int x0, int y0, int z0, int z1,
                                              float4* fsm) {
-  float4* vbuf = fsm;                    // 5 * VX * VY
-  float4* wbuf = fsm + 5 * VX * VY;      // 3 * WX * WY
+  float4* vbuf = fsm;                                        // 5 * VX * VY
+  float* wbuf = reinterpret_cast<float*>(fsm + 5 * VX * VY);  // 3 * WX * WY
   const MarchPlan m = march_plan(x0, y0, d);
   for (int z = z0 - 2; z <= z0 + 2; ++z) load_vplane(vslot(vbuf, z), f.velY, m, z, d);
   cp_async_commit();
@@ -514,7 +529,7 @@ __device__ __forceinline__ void forces_tiled_body(const float* __restrict__ P, c
   const int z0 = blk.z * ZD;
   forces_march(ParamsGlobal{P}, f, noiseT, curlT, d, blk.x * FT_X, blk.y * FT_Y, z0, min(z0 + ZD, d.nz), fsm);
 }
-constexpr size_t FORCES_TILED_SMEM = sizeof(float4) * (5 * VX * VY + 3 * WX * WY);
+constexpr size_t FORCES_TILED_SMEM = sizeof(float4) * 5 * VX * VY + sizeof(float) * 3 * WX * WY;
 
 // ---------------- divergence minus the expansion target (src/sim.js:399-413) ----------------
 template <class TileT = Tile0>
