@@ -935,8 +935,17 @@ __device__ __forceinline__ double warp_sum(double v) {
 // thread accumulate in double-float (df64, fire_device.cuh) in a fixed order, so the result is
 // deterministic and carries ~48 bits without FP64 instructions.  Partials: float4 (rr.hi, rr.lo, bb.hi, bb.lo).
 constexpr int RZ = 8;
-// Residual reduction per V-cycle assumed by the residual-driven loop's prediction of the first cycle it tests.
+// The residual-driven loop's prediction of the first cycle a step tests, kept in counter slot 3 (the solve's
+// only state between steps, so checkpoints and the adjoint's recomputation carry it): bits 0-7 the cycle,
+// bits 8-15 the steps left until the next probe (a step that tests one cycle earlier than the last step
+// needed, to find a falling need), bits 16-23 the probe interval, bit 24 set while a probe step runs.  After
+// a probe that succeeds (the need fell) the next step probes again, and so does every step until one fails;
+// a failed probe doubles the interval, up to MG_PROBE_MAX steps.  The next step also probes at once after a step whose need rose (a burst or a moved
+// log often raises it for a single step) or whose final residual lies MG_PREDICT_RHO below the tolerance
+// (one cycle fewer would have reached it if a cycle reduces the residual at least that much).
 constexpr double MG_PREDICT_RHO = 0.3;
+constexpr int MG_PROBE_MAX = 8;
+__device__ __forceinline__ int mg_first_test(int slot3) { return slot3 & 0xff; }
 // Sums of r^2 and b^2 over planes z0 .. z0+RZ-1 of column (x, y), r = b - A p with the ghost rules of
 // pghost.  The column is marched in z with the z neighbours carried in registers; the x/y face tests are
 // per column, so a cell costs 6 loads and a handful of selects.
@@ -969,13 +978,13 @@ __device__ __forceinline__ void residual_column(const float* __restrict__ p, con
   }
 }
 // gate (residual-driven loop only, else null): the loop's counters; the norm is skipped while the cycle
-// about to complete (gate[0] + 1) is below gate[3], the first cycle at which this step tests convergence.
+// about to complete (gate[0] + 1) is below the first cycle at which this step tests convergence (gate[3]).
 __global__ void __launch_bounds__(RB) k_residual(const float* __restrict__ p, const float* __restrict__ b, int nx, int ny, int nz,
                                                  float ih2, float4* __restrict__ partials, const int* __restrict__ gate) {
   __shared__ df64 sr[RB / 32], sb[RB / 32];
   pdl_wait();
   pdl_trigger();
-  if (gate && gate[0] + 1 < gate[3]) return;   // uniform over the grid
+  if (gate && gate[0] + 1 < mg_first_test(gate[3])) return;   // uniform over the grid
   const int x = blockIdx.x * GX + threadIdx.x, y = blockIdx.y * GY + threadIdx.y;
   const int z0 = (blockIdx.z * GZ + threadIdx.z) * RZ;
   const int tid = threadIdx.x + GX * (threadIdx.y + GY * threadIdx.z);
@@ -1012,12 +1021,12 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
   __shared__ int skip;
   pdl_wait();
   pdl_trigger();
-  // Cycles before counter[3] run without a convergence test (each skipped test saves the norm's pass over
-  // level 0 and the sum); the solve still stops only on a tested residual <= tol (or at max_cycles).
-  // counter[3] is set when a step stops (below) from the cycle count it needed and its final residual.
+  // Cycles before the predicted first test run without a convergence test (each skipped test saves the norm's
+  // pass over level 0 and the sum); the solve still stops only on a tested residual <= tol (or at max_cycles).
+  // The prediction is set when a step stops (below) from the cycle count it needed and its final residual.
   if (threadIdx.x == 0) {
     const int c = counter[0] + 1;
-    skip = c < counter[3];
+    skip = c < mg_first_test(counter[3]);
     if (skip) {
       counter[0] = c;
       counter[1] += 1;   // cumulative cycles since creation
@@ -1038,11 +1047,20 @@ __global__ void __launch_bounds__(RB) k_sum_decide(const float4* __restrict__ pa
     const double rel = s1 > 0.0 ? sqrt(s0 / s1) : 0.0;
     rel_out[0] = rel;
     const bool more = rel > tol && c < max_cycles;
-    // The next step tests first at this step's count c, or at c - 1 when one cycle fewer could have reached
-    // the tolerance: when rel <= MG_PREDICT_RHO * tol, with MG_PREDICT_RHO above the residual reduction of one
-    // cycle (about 0.1 for the over-relaxed V(2,2)).  A step that needs fewer cycles than predicted runs one
-    // more than it needs, and its smaller final residual moves the next prediction down.
-    if (!more) counter[3] = min(max(1, rel <= MG_PREDICT_RHO * tol ? c - 1 : c), max_cycles - 1);
+    // The next step tests first at this step's count c, or at c - 1 (a probe) when one cycle fewer could
+    // have reached the tolerance (rel <= MG_PREDICT_RHO * tol) or the probe interval has run out.  A step
+    // whose need fell runs at most one cycle more than it needs until the next probe.
+    if (!more) {
+      const int slot = counter[3], first = mg_first_test(slot);
+      const bool probed = (slot & (1 << 24)) != 0;
+      const bool fell = probed && c == first;   // the probe's earlier test passed
+      int left = (slot >> 8) & 0xff, every = (slot >> 16) & 0xff;
+      if (probed) every = fell ? 1 : min(max(2 * every, 1), MG_PROBE_MAX);
+      const bool rose = c > first + (probed ? 1 : 0);
+      const bool probe = fell || rose || rel <= MG_PREDICT_RHO * tol || left <= 0;
+      left = probe ? max(every, 1) - 1 : left - 1;
+      counter[3] = min(max(1, probe ? c - 1 : c), max_cycles - 1) | (left << 8) | (every << 16) | (probe ? 1 << 24 : 0);
+    }
     cudaGraphSetConditional(h, more ? 1u : 0u);
   }
 }
