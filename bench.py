@@ -177,8 +177,8 @@ def make_sim(F, device: int, mg_fixed: int = 0):
 
 
 def launches_per_step(sim, cycles_per_step: float) -> float:
-    """Kernels launched per step by the captured graph: 5 stencil kernels and the cycle-counter reset, and per
-    V-cycle 10 per level above the shared-memory tail (2 + 2 red-black sweeps of 2 colour launches each,
+    """Kernels launched per step by the captured graph: 5 stencil kernels (the divergence kernel also clears
+    the solve's cycle count), and per V-cycle 10 per level above the shared-memory tail (2 + 2 red-black sweeps of 2 colour launches each,
     restriction, prolongation) less one per level below the finest (its first colour-0 sweep runs inside the
     restriction onto it), the tail kernel, the residual norm and the decision kernel.  The tail starts at the
     finest level that fits in 200 KB of shared memory (one CTA, or 8 CTAs with distributed levels) and has at
@@ -200,7 +200,7 @@ def launches_per_step(sim, cycles_per_step: float) -> float:
             break
     top = min(T, n - 1)
     per_cycle = 10 * top - max(top - 1, 0) + (1 if T < n else 0) + 2
-    return 6 + per_cycle * cycles_per_step
+    return 5 + per_cycle * cycles_per_step
 
 
 def workload_config(preroll: int) -> dict:
