@@ -91,6 +91,10 @@ typedef struct FireConfig {
   int mg_max_cycles;   /* > 0: residual-driven solve, at most this many cycles (0 = fixed vcycles) */
   double mg_tol;       /* relative residual ||b - A p|| / ||b|| target of the residual-driven mode   */
 } FireConfig;
+/* The residual-driven solve runs inside the step graph (a conditional loop decided on the device) and stops
+ * only on a tested residual <= mg_tol or after mg_max_cycles.  The test is skipped on cycles the previous
+ * steps predict are still needed, with periodic probes one cycle earlier; a step whose need fell since the
+ * last probe runs one cycle more than it needs.                                                      */
 
 typedef struct FireFieldDesc {
   void* data;          /* device pointer, owned by the simulation, valid until destroy              */
