@@ -182,9 +182,8 @@ int upload_block(FireSim* sim, float dt, cudaStream_t st, bool with_logs, const 
   return FIRE_OK;
 }
 
-// `iters` red-black sweeps of level l (src/sim.js:576-586): colour 0 then colour 1, one launch each.
-// `iters` red-black sweeps of level l; with first_done the first colour-0 sweep has already been applied
-// (by the fused restriction).
+// `iters` red-black sweeps of level l (src/sim.js:576-586): colour 0 then colour 1, one launch each; with
+// first_done the first colour-0 sweep has already been applied (by the fused restriction).
 void record_smooth(FireSim* s, int l, int iters, cudaStream_t st, bool first_done = false) {
   for (int k = 0; k < iters; ++k) {
     if (k > 0 || !first_done) launch_smooth(s->levels[l], 0, st);
