@@ -348,6 +348,46 @@ def test_residual_driven_solve(campfire):
     assert sim.residual() == pytest.approx(info.last_rel_residual, rel=1e-6)
 
 
+def test_residual_driven_solve_through_events(campfire):
+    """The residual-driven solve with the campfire's logs (where a cycle reduces the residual less than in the
+    open-floor benchmark): from rest through a burst and a gust, every step ends at or below the tolerance (or
+    at the cycle limit), and after the start-up the prediction of the first tested cycle has followed the
+    falling need: one step from the GPU state, checked against the oracle's loop that tests every cycle, runs
+    the cycles that loop needs or one more."""
+    import oracle as O
+    tol, cmax = 1e-5, 8
+    sim = F.FireSim(res=FC.C1["res"], size=FC.C1["size"], logs=campfire, vcycles=4, mg_max_cycles=cmax, mg_tol=tol)
+    sim.set_mg_omega(1.2)
+    dt = FC.C1["dt"]
+    counts = []
+    for k in range(45):
+        if k == 25:
+            sim.inject((0.0, 0.1, 0.0), 1.0, 0.05)
+        if k == 32:
+            sim.gust(1.0, 0.1)
+        sim.step(dt, 1)
+        sim.sync()
+        info = sim.info()
+        assert info.last_rel_residual <= tol or info.last_cycles == cmax, (k, info.last_cycles, info.last_rel_residual)
+        counts.append(info.last_cycles)
+    print("cycles per step:", "".join(str(c) for c in counts))
+    orc = O.OracleSim(FC.C1["res"], sim.dx)
+    orc.set_tables(sim.download("noise").astype(np.float32), sim.download("curl").astype(np.float32))
+    orc.set_logs(campfire)
+    orc.set_modes(omega=1.2)
+    for name in FC.FIELD_NAMES:
+        orc.put(name, sim.download(name))
+    for w in ("p", "b"):
+        orc.put_level(0, w, sim.level(0, w))
+    FC.sync_block(sim, orc, dt)
+    sim.step(dt, 1)
+    sim.sync()
+    need = orc.step_raw(False, -cmax, tol)
+    got = sim.info().last_cycles
+    assert got in (need, need + 1), (got, need, counts)
+    sim.close()
+
+
 def test_over_relaxed_smoothing(campfire):
     """The over-relaxed fine-level smoothing (omega = 1.2) still converges: every step ends at or below the
     tolerance, in no more cycles than Gauss-Seidel; omega = 1 stays the reference's smoother bit for bit."""
